@@ -1,0 +1,292 @@
+"""Benchmark: Cliffs time stepping on the 2048x2048 Cartesian shelf basin.
+
+One step = one time step of the whole grid (x-sweep over all rows, y-sweep
+over all columns with the fused max-wave update), i.e. one pass of the hot
+path of cliffs_main.f:303-355.  Metric: Mcell-updates/s = nx*ny*steps/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference solver (the
+Fortran reference cannot be compiled on these hosts) with all host threads on
+the same workload.  With N > 1 (torchrun) every rank runs an independent
+replica on its own GPU: the plain solver does not shard (replicas only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 2048
+DX = 100.0
+SEED = 0
+B_X = 28   # algorithmic bytes per cell, x-sweep: read dep,eta,u,v; write eta,u,v (FP32)
+B_Y = 44   # y-sweep with the fused max-wave: 28 + read/write hmax, velmax
+B_STEP = B_X + B_Y
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def workload():
+    import importlib
+    W = importlib.import_module("cliffs-src_gb300.workloads")
+    case = W.shelf_2d(seed=SEED, nx=NX, ny=NY, dx=DX, steps=3000, ngauges=64)
+    case["crough"] = 0.000625  # Manning n = 0.025, as in the reference's Okushiri example
+    return case
+
+
+def config_dict(case, impl_note):
+    return {"workload": f"shelf_2d {NX}x{NY} dx={DX:g} m, FP32 state, 3000-step run, "
+                        f"64 gauges every 10 steps",
+            "grid": [NX, NY], "dt_s": round(case["dt"], 6), "ground_m": case["ground"],
+            "crough": case["crough"], "source": "elliptical Gaussian uplift 100x50 km, 2 m",
+            "l2": "working set ~151 MB per step > 129 MB L2; no flush",
+            "parallelism": "replicas only (one independent grid per GPU)", "impl": impl_note}
+
+
+def cpu_baseline(case, steps, threads):
+    """The CPU restatement (oracle) timed on a bounded sample of the workload."""
+    import oracle
+    from tests.runners import oracle_model
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    m = oracle_model(case)
+    m.step(1)  # warm-up
+    t0 = time.perf_counter()
+    m.step(steps)
+    dt = time.perf_counter() - t0
+    val = NX * NY * steps / dt / 1e6
+    return {"value": round(val, 3), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
+            "sample": f"{NX}x{NY} grid, {steps} time steps after 1 warm-up step, "
+                      f"OpenMP over lines ({threads} threads), FP64"}
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    # The oracle library reads OMP_NUM_THREADS when it first starts OpenMP.
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle  # noqa: F401  (builds/loads the CPU restatement)
+    case = workload()
+    steps = max(1, min(args.steps, 60))
+    cb = cpu_baseline(case, steps, threads)
+    line = {"metric": "Mcell-updates/s", "value": cb["value"], "unit": "Mcell-updates/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "ms_per_step": round(1e3 * NX * NY / (cb["value"] * 1e6), 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(case, "CPU restatement of cliffs.f + cliffs_main.f time loop"),
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import importlib
+
+    import numpy as np
+    import torch
+
+    rank, world, local = _env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    pkg = importlib.import_module("cliffs-src_gb300")
+    pkg.build.build()
+    case = workload()
+    cells = NX * NY
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident throughput (value) ----------------------------------
+    stream = torch.cuda.Stream()
+    g = pkg.GpuGrid.from_case(case)
+    g.set_stream(stream.cuda_stream)
+    g.step(args.warmup)
+    torch.cuda.synchronize()
+    g.profile(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        done, _ = g.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    prof = g.profile_read()
+    g.profile(False)
+    r, flags = g.status()
+    if r != 0:
+        raise RuntimeError(f"solver status {r} flags {flags}")
+    g.close()
+    t_local = ms / 1e3
+    if dist is not None:
+        t = torch.tensor([t_local], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    else:
+        t_max = t_local
+    value = world * cells * args.steps / t_max / 1e6
+
+    # ---- end to end through the C ABI with host buffers (e2e) -----------------
+    barrier()
+    t0 = time.perf_counter()
+    g2 = pkg.GpuGrid(case["dep"], dx=np.full(NX - 1, DX), dy=np.full(NY - 1, DX),
+                     ground=case["ground"], crough=case["crough"], dt=case["dt"])
+    g2.set_initial(case["H0"], case["u0"], case["v0"])
+    I, J = case["gauges"]
+    nrec = 0
+    for s0 in range(0, args.steps, 10):
+        g2.step(min(10, args.steps - s0))
+        g2.gauges(I, J)
+        nrec += 1
+    cel, u, v = g2.download_state()
+    me, mv = g2.maxwave()
+    t_e2e = time.perf_counter() - t0
+    g2.close()
+    if dist is not None:
+        t = torch.tensor([t_e2e], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    h2d = cells * 8 * 4 + (NX + NY) * 8 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), spacing, gauge indices
+    d2h = cells * 8 * 3 + cells * 4 * 2 + nrec * 64 * 3 * 8
+    e2e = {"value": round(world * cells * args.steps / t_e2e / 1e6, 3), "unit": "Mcell-updates/s",
+           "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps)}
+
+    # ---- roofline of the dominant kernel ---------------------------------------
+    peak, peak_kind = _peaks()
+    kx, ky = prof["x_ms"], prof["y_ms"]
+    if ky >= kx:
+        kname, kms, bpc = "sweep_kernel<1> (y-sweep + max-wave)", ky, B_Y
+    else:
+        kname, kms, bpc = "sweep_kernel<0> (x-sweep)", kx, B_X
+    achieved = bpc * cells / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tr = json.load(f)
+        key = "y" if ky >= kx else "x"
+        if key in tr:
+            traffic = int(tr[key]["bytes_per_cell"] * cells)
+    roof = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+            "bytes_per_cell": bpc, "launch_ms": round(kms, 5), "peak_source": peak_kind,
+            "x_ms": round(kx, 5), "y_ms": round(ky, 5)}
+
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        cb = cpu_baseline(case, 40, threads) if world == 1 or rank == 0 else None
+        clocks = clk.summary()
+        line = {"metric": "Mcell-updates/s", "value": round(value, 3), "unit": "Mcell-updates/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config_dict(case, "CUDA sm_103a, include/cliffs_gpu.h"),
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+                "gpu_launches": int(prof["x_n"] + prof["y_n"]),
+                "hbm_frac_step": round(B_STEP * cells * args.steps / (ms / 1e3) / 1e9 / peak, 4)}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

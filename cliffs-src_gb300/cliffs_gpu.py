@@ -1,0 +1,339 @@
+"""Python binding of the C ABI in include/cliffs_gpu.h (ctypes).
+
+GpuGrid mirrors the state a Cliffs run keeps in module MASTER
+(global_modules.f:16-35) and the operations the time loop of
+cliffs_main.f:303-378 applies to it.  Every compute call goes to the CUDA
+library; there is no CPU path, and loading fails loudly when the library is
+missing.  Arrays are numpy arrays of shape (ny, nx), C order, which is the
+Fortran (nx, ny) column-major layout.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcliffs_gpu.so")
+
+CLIFFS_OK = 0
+CLIFFS_FEED_ENDED = 1
+GRAV = 9.800000190734863
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("dep", _dp),
+                ("dx", _dp), ("row_scale", _dp), ("dy", _dp), ("zeta", _dp),
+                ("ground", ctypes.c_double), ("crough", ctypes.c_double),
+                ("dt", ctypes.c_double)]
+
+
+class NestDesc(ctypes.Structure):
+    _fields_ = [("mm", ctypes.c_int32), ("nn", ctypes.c_int32),
+                ("W_nx", ctypes.c_int32), ("E_nx", ctypes.c_int32),
+                ("S_ny", ctypes.c_int32), ("N_ny", ctypes.c_int32),
+                ("W_cx", ctypes.c_double), ("E_cx", ctypes.c_double),
+                ("S_cy", ctypes.c_double), ("N_cy", ctypes.c_double),
+                ("WE_ny", _ip), ("WE_cy", _dp), ("SN_nx", _ip), ("SN_cx", _dp)]
+
+
+class Runup(ctypes.Structure):
+    _fields_ = [("max_runup", ctypes.c_double), ("i", ctypes.c_int32),
+                ("j", ctypes.c_int32), ("wetted_land", ctypes.c_int64),
+                ("wet_now", ctypes.c_int64)]
+
+
+class CliffsError(RuntimeError):
+    def __init__(self, code, what):
+        self.code = code
+        super().__init__(f"{what}: {strerror(code)} ({code})")
+
+
+# Every symbol declared in include/cliffs_gpu.h with its ctypes signature.
+_V = ctypes.c_void_p
+_I = ctypes.c_int32
+_D = ctypes.c_double
+SIGNATURES = {
+    "cliffs_gpu_metrics": ([_I, _I, _I, _dp, _dp, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_create": ([ctypes.POINTER(GridDesc), ctypes.POINTER(_V)], ctypes.c_int),
+    "cliffs_gpu_destroy": ([_V], None),
+    "cliffs_gpu_set_stream": ([_V, _V], ctypes.c_int),
+    "cliffs_gpu_set_initial": ([_V, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_upload_state": ([_V, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_download_state": ([_V, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_set_feed": ([_V, _I, _dp, _dp, _dp, _dp, _dp, _I, _I], ctypes.c_int),
+    "cliffs_gpu_feed_start": ([_V, _D], ctypes.c_int),
+    "cliffs_gpu_step": ([_V, _I, _dp, _ip], ctypes.c_int),
+    "cliffs_gpu_sweep": ([_V, _I], ctypes.c_int),
+    "cliffs_gpu_set_edges": ([_V, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_maxwave_update": ([_V], ctypes.c_int),
+    "cliffs_gpu_get_maxwave": ([_V, _fp, _fp], ctypes.c_int),
+    "cliffs_gpu_get_max_raw": ([_V, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_get_sea_state": ([_V, _I, _I, _fp, _fp, _fp], ctypes.c_int),
+    "cliffs_gpu_get_gauges": ([_V, _I, _ip, _ip, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_runup": ([_V, ctypes.POINTER(Runup)], ctypes.c_int),
+    "cliffs_gpu_nest_add": ([_V, ctypes.POINTER(NestDesc), _ip], ctypes.c_int),
+    "cliffs_gpu_feed_child": ([_V, _I, _D, _ip, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_status": ([_V, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
+    "cliffs_gpu_sync": ([_V], ctypes.c_int),
+    "cliffs_gpu_profile": ([_V, _I], ctypes.c_int),
+    "cliffs_gpu_profile_read": ([_V, _dp, ctypes.POINTER(ctypes.c_int64), _dp,
+                                 ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
+    "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Load the CUDA library; raises when it was not built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"CUDA library not built: {p} (run the package's build.py)")
+    L = ctypes.CDLL(p)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = L
+    return L
+
+
+def strerror(code):
+    try:
+        return load().cliffs_gpu_strerror(int(code)).decode()
+    except Exception:  # pragma: no cover - library absent
+        return "unknown"
+
+
+def _chk(code, what):
+    if code < 0:
+        raise CliffsError(code, what)
+    return code
+
+
+def _p(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None else ctypes.cast(None, t)
+
+
+def _f64(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+def metrics(xcrd, ycrd, cartesian):
+    """MasterGrid.f:237-268 through the library: (dx, row_scale, dy, zeta)."""
+    xcrd = _f64(xcrd)
+    ycrd = _f64(ycrd)
+    nx, ny = len(xcrd), len(ycrd)
+    dx = np.zeros(max(nx - 1, 1))
+    rs = np.ones(ny)
+    dy = np.zeros(max(ny - 1, 1))
+    zeta = np.zeros(ny)
+    _chk(load().cliffs_gpu_metrics(nx, ny, int(bool(cartesian)), _p(xcrd), _p(ycrd),
+                                   _p(dx), _p(rs), _p(dy), _p(zeta)), "metrics")
+    return (dx if nx > 2 else None, rs if nx > 2 and not cartesian else None,
+            dy if ny > 2 else None, zeta if ny > 2 else None)
+
+
+class GpuGrid:
+    """Device-resident state of one Cliffs grid."""
+
+    def __init__(self, dep, *, dx=None, row_scale=None, dy=None, zeta=None,
+                 ground, crough, dt):
+        self.L = load()
+        self.dep = _f64(dep)
+        self.ny, self.nx = self.dep.shape
+        self._keep = [_f64(dx), _f64(row_scale), _f64(dy), _f64(zeta)]
+        kdx, krs, kdy, kz = self._keep
+        d = GridDesc(nx=self.nx, ny=self.ny, dep=_p(self.dep), dx=_p(kdx),
+                     row_scale=_p(krs), dy=_p(kdy), zeta=_p(kz),
+                     ground=float(ground), crough=float(crough), dt=float(dt))
+        h = ctypes.c_void_p()
+        _chk(self.L.cliffs_gpu_create(ctypes.byref(d), ctypes.byref(h)), "create")
+        self.h = h
+        self.ground, self.crough, self.dt = float(ground), float(crough), float(dt)
+        self.celmin = float(np.sqrt(GRAV * self.ground))
+        self.t = ctypes.c_double(0.0)
+        self._streamref = None
+
+    @classmethod
+    def from_case(cls, case):
+        dx, rs, dy, zeta = metrics(case["xcrd"], case["ycrd"], case["cartesian"])
+        if case.get("zeta") is not None:
+            zeta = case["zeta"]
+        g = cls(case["dep"], dx=dx, row_scale=rs, dy=dy, zeta=zeta,
+                ground=case["ground"], crough=case["crough"], dt=case["dt"])
+        g.set_initial(case["H0"], case.get("u0"), case.get("v0"))
+        g.t.value = float(case.get("t0", 0.0))
+        return g
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cliffs_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state --------------------------------------------------------------
+    def set_stream(self, stream_ptr):
+        _chk(self.L.cliffs_gpu_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")
+
+    def set_initial(self, H, u=None, v=None):
+        s = (self.ny, self.nx)
+        _chk(self.L.cliffs_gpu_set_initial(self.h, _p(_f64(H, s)), _p(_f64(u, s)), _p(_f64(v, s))),
+             "set_initial")
+
+    def upload_state(self, cel, u=None, v=None):
+        s = (self.ny, self.nx)
+        _chk(self.L.cliffs_gpu_upload_state(self.h, _p(_f64(cel, s)), _p(_f64(u, s)), _p(_f64(v, s))),
+             "upload_state")
+
+    def download_state(self):
+        cel = np.empty((self.ny, self.nx))
+        u = np.empty((self.ny, self.nx))
+        v = np.empty((self.ny, self.nx))
+        _chk(self.L.cliffs_gpu_download_state(self.h, _p(cel), _p(u), _p(v)), "download_state")
+        return cel, u, v
+
+    def eta(self):
+        cel, _, _ = self.download_state()
+        H = cel * np.abs(cel) / GRAV
+        return np.where(cel > self.celmin, H - self.dep, np.nan)
+
+    # -- forcing --------------------------------------------------------------
+    def set_feed(self, tinput, west=None, east=None, south=None, north=None, irec=1, freeze=True):
+        arr = [_f64(a) for a in (tinput, west, east, south, north)]
+        self._feed = arr
+        t, w, e, s, n = arr
+        _chk(self.L.cliffs_gpu_set_feed(self.h, len(t), _p(t), _p(w), _p(e), _p(s), _p(n),
+                                        int(irec), int(bool(freeze))), "set_feed")
+
+    def feed_start(self, cuke):
+        return self.L.cliffs_gpu_feed_start(self.h, float(cuke))
+
+    def set_edges(self, edge1=None, edge2=None):
+        e1 = _f64(edge1)
+        e2 = _f64(edge2)
+        _chk(self.L.cliffs_gpu_set_edges(self.h, _p(e1), _p(e2)), "set_edges")
+
+    # -- stepping -------------------------------------------------------------
+    def step(self, nsteps=1):
+        done = ctypes.c_int32(0)
+        r = _chk(self.L.cliffs_gpu_step(self.h, int(nsteps), ctypes.byref(self.t), ctypes.byref(done)), "step")
+        return done.value, r == CLIFFS_FEED_ENDED
+
+    @property
+    def time(self):
+        return self.t.value
+
+    def sweep(self, iu):
+        _chk(self.L.cliffs_gpu_sweep(self.h, int(iu)), "sweep")
+
+    def maxwave_update(self):
+        _chk(self.L.cliffs_gpu_maxwave_update(self.h), "maxwave_update")
+
+    def sync(self):
+        _chk(self.L.cliffs_gpu_sync(self.h), "sync")
+
+    def status(self):
+        f = ctypes.c_uint32(0)
+        r = self.L.cliffs_gpu_status(self.h, ctypes.byref(f))
+        return r, f.value
+
+    # -- outputs ----------------------------------------------------------------
+    def maxwave(self):
+        me = np.empty((self.ny, self.nx), np.float32)
+        mv = np.empty((self.ny, self.nx), np.float32)
+        _chk(self.L.cliffs_gpu_get_maxwave(self.h, _p(me, _fp), _p(mv, _fp)), "get_maxwave")
+        return me, mv
+
+    def max_raw(self):
+        hm = np.empty((self.ny, self.nx))
+        vm = np.empty((self.ny, self.nx))
+        _chk(self.L.cliffs_gpu_get_max_raw(self.h, _p(hm), _p(vm)), "get_max_raw")
+        return hm, vm
+
+    def sea_state(self, lonsub=1, latsub=1):
+        nxs = (self.nx - 1) // lonsub + 1
+        nys = (self.ny - 1) // latsub + 1
+        h = np.empty((nys, nxs), np.float32)
+        u = np.empty((nys, nxs), np.float32)
+        v = np.empty((nys, nxs), np.float32)
+        _chk(self.L.cliffs_gpu_get_sea_state(self.h, lonsub, latsub, _p(h, _fp), _p(u, _fp), _p(v, _fp)),
+             "get_sea_state")
+        return h, u, v
+
+    def gauges(self, I, J):
+        I = np.ascontiguousarray(I, np.int32)
+        J = np.ascontiguousarray(J, np.int32)
+        n = len(I)
+        eta, u, v = np.empty(n), np.empty(n), np.empty(n)
+        _chk(self.L.cliffs_gpu_get_gauges(self.h, n, _p(I, _ip), _p(J, _ip), _p(eta), _p(u), _p(v)),
+             "get_gauges")
+        return eta, u, v
+
+    def runup(self):
+        r = Runup()
+        _chk(self.L.cliffs_gpu_runup(self.h, ctypes.byref(r)), "runup")
+        return dict(max_runup=r.max_runup, i=r.i, j=r.j, wetted_land=r.wetted_land, wet_now=r.wet_now)
+
+    # -- nesting ---------------------------------------------------------------
+    def nest_add(self, tables):
+        """tables: dict with the NestedGrid.f:104-119 fields (1-based)."""
+        WE_ny = np.ascontiguousarray(tables["WE_ny"], np.int32)
+        WE_cy = _f64(tables["WE_cy"])
+        SN_nx = np.ascontiguousarray(tables["SN_nx"], np.int32)
+        SN_cx = _f64(tables["SN_cx"])
+        d = NestDesc(mm=len(SN_nx), nn=len(WE_ny), W_nx=int(tables["W_nx"]), E_nx=int(tables["E_nx"]),
+                     S_ny=int(tables["S_ny"]), N_ny=int(tables["N_ny"]), W_cx=float(tables["W_cx"]),
+                     E_cx=float(tables["E_cx"]), S_cy=float(tables["S_cy"]), N_cy=float(tables["N_cy"]),
+                     WE_ny=_p(WE_ny, _ip), WE_cy=_p(WE_cy), SN_nx=_p(SN_nx, _ip), SN_cx=_p(SN_cx))
+        i = ctypes.c_int32(-1)
+        _chk(self.L.cliffs_gpu_nest_add(self.h, ctypes.byref(d), ctypes.byref(i)), "nest_add")
+        return i.value, (len(SN_nx), len(WE_ny))
+
+    def feed_child(self, nest, cuke, arrived):
+        nid, (mm, nn) = nest
+        a = ctypes.c_int32(int(bool(arrived)))
+        w, e = np.zeros((3, nn)), np.zeros((3, nn))
+        s, n = np.zeros((3, mm)), np.zeros((3, mm))
+        r = _chk(self.L.cliffs_gpu_feed_child(self.h, nid, float(cuke), ctypes.byref(a),
+                                              _p(w), _p(e), _p(s), _p(n)), "feed_child")
+        return bool(a.value), ((w, e, s, n) if r == 1 else None)
+
+    # -- profiling / tuning -------------------------------------------------------
+    def profile(self, enable=True):
+        _chk(self.L.cliffs_gpu_profile(self.h, int(bool(enable))), "profile")
+
+    def profile_read(self):
+        xm, ym = ctypes.c_double(), ctypes.c_double()
+        xn, yn = ctypes.c_int64(), ctypes.c_int64()
+        _chk(self.L.cliffs_gpu_profile_read(self.h, ctypes.byref(xm), ctypes.byref(xn),
+                                            ctypes.byref(ym), ctypes.byref(yn)), "profile_read")
+        return dict(x_ms=xm.value, x_n=xn.value, y_ms=ym.value, y_n=yn.value)
+
+    def set_tiling(self, seg_x=0, seg_y=0):
+        _chk(self.L.cliffs_gpu_set_tiling(self.h, int(seg_x), int(seg_y)), "set_tiling")

@@ -1,0 +1,1176 @@
+// cliffs_gpu.cu -- C ABI implementation (include/cliffs_gpu.h) and the
+// auxiliary kernels: state conversion, wetness bitmaps, output conversions,
+// gauges, runup, nested-grid feed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/cliffs_gpu.h"
+#include "kernels.cuh"
+
+using namespace cliffs;
+
+namespace {
+
+constexpr double kGrav = 9.800000190734863;   // (double)9.8f, global_modules.f:17
+constexpr double kPi = 3.1415927410125732;    // (double)3.1415926536f
+constexpr double kEarthR = 6371009.0;
+constexpr double kSqr2 = 1.4142135381698608;  // (double)1.41421356f, cliffs.f:34
+constexpr float kNan4 = -1.0e32f;             // global_modules.f:18
+
+#define CK(x)                                     \
+  do {                                            \
+    cudaError_t e_ = (x);                         \
+    if (e_ != cudaSuccess) return CLIFFS_ERR_CUDA; \
+  } while (0)
+
+struct Nest {
+  cliffs_nest_desc d;
+  int32_t *WE_ny = nullptr, *SN_nx = nullptr;
+  double *WE_cy = nullptr, *SN_cx = nullptr;
+};
+
+struct ProfPair {
+  cudaEvent_t a, b;
+  int dir;
+};
+
+}  // namespace
+
+struct cliffs_ctx {
+  int dev = 0;
+  int nx = 0, ny = 0, pitch = 0;
+  bool xrun = false, yrun = false;
+  int ii1 = 1, ii2 = 1, jj1 = 1, jj2 = 1;
+  double ground = 0, crough = 0, dt = 0, celmin = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  float* dep = nullptr;
+  float *eta[2] = {nullptr, nullptr}, *xu[2] = {nullptr, nullptr}, *yv[2] = {nullptr, nullptr};
+  float *hmax = nullptr, *velmax = nullptr;
+  int cur = 0;
+  uint32_t *bm_rows[2] = {nullptr, nullptr}, *bm_cols[2] = {nullptr, nullptr};
+  int cur_r = 0, cur_c = 0;
+  bool rows_valid = false, cols_valid = false;
+  int ldr = 0, ldc = 0;
+  float4 *geo_x = nullptr, *geo_y = nullptr;
+  float* scl_y = nullptr;
+  float2* lscale = nullptr;
+  float inv_dx1_x = 0, inv_dxn1_x = 0, inv_dx1_y = 0, inv_dxn1_y = 0;
+  // boundary forcing
+  int nt = 0;
+  std::vector<double> tinput;
+  double *fw = nullptr, *fe = nullptr, *fs = nullptr, *fn = nullptr;
+  int irec = 0;
+  bool feed_on = false, freeze = false;
+  // static edges for single sweeps (edge1/edge2 of module MASTER)
+  double *edge_s[2] = {nullptr, nullptr};
+  bool edges_static = false;
+  unsigned* status = nullptr;
+  double* red = nullptr;  // reduction scratch
+  int red_cap = 0;
+  std::vector<Nest> nests;
+  int* d_flag = nullptr;
+  bool have_state = false;
+  int seg_x = 64, seg_y = 64;
+  bool prof = false;
+  std::vector<ProfPair> prof_pending;
+  double prof_ms[2] = {0, 0};
+  int64_t prof_n[2] = {0, 0};
+};
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) return CLIFFS_ERR_NOMEM;
+  return CLIFFS_OK;
+}
+
+__global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict__ src,
+                             int src_is_celerity, const double* __restrict__ xv,
+                             const double* __restrict__ yvv, const float* __restrict__ dep,
+                             float* eta, float* xu, float* yv, double ground, double g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= pitch || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i;
+  if (i >= nx) {
+    eta[q] = 0.f;
+    xu[q] = 0.f;
+    yv[q] = 0.f;
+    return;
+  }
+  const size_t s = (size_t)j * nx + i;
+  const double d = (double)dep[q];
+  double H;
+  if (src_is_celerity) {
+    const double c = src[s];
+    H = c * fabs(c) / g;  // signed total depth keeps the sign of the celerity
+  } else {
+    // celerity transform of cliffs_main.f:218-227 expressed on H
+    H = src[s] <= ground ? 0.0 : src[s];
+  }
+  eta[q] = (float)(H - d);
+  xu[q] = xv ? (float)xv[s] : 0.f;
+  yv[q] = yvv ? (float)yvv[s] : 0.f;
+}
+
+__global__ void k_reset_max(int nx, int ny, int pitch, const float* __restrict__ dep, float* hmax,
+                            float* velmax) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= pitch || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i;
+  hmax[q] = i < nx ? -dep[q] : 0.f;  // hmax = 0 in celerity form
+  velmax[q] = 0.f;
+}
+
+// Both wetness bitmaps from the current state; one warp per 32x32 tile.
+__global__ void k_bitmaps(int nx, int ny, int pitch, const float* __restrict__ dep,
+                          const float* __restrict__ eta, float ground, uint32_t* rows, int ldr,
+                          uint32_t* cols, int ldc) {
+  const int lane = threadIdx.x & 31;
+  const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int tcx = (nx + 31) >> 5, tcy = (ny + 31) >> 5;
+  if (tile >= tcx * tcy) return;
+  const int bx = tile % tcx, by = tile / tcx;
+  const int i = (bx << 5) + lane;
+  uint32_t colbits = 0;
+  for (int r = 0; r < 32; ++r) {
+    const int j = (by << 5) + r;
+    bool w = false;
+    if (j < ny && i < nx) {
+      const size_t q = (size_t)j * pitch + i;
+      w = dep[q] + eta[q] > ground;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, w);
+    if (lane == 0 && j < ny) rows[(size_t)j * ldr + bx] = b;
+    colbits |= (w ? 1u : 0u) << r;
+  }
+  if (i < nx) cols[(size_t)i * ldc + by] = colbits;
+}
+
+__global__ void k_download(int nx, int ny, int pitch, const float* __restrict__ dep,
+                           const float* __restrict__ eta, const float* __restrict__ xu,
+                           const float* __restrict__ yv, double* cel, double* xo, double* yo,
+                           double g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i, s = (size_t)j * nx + i;
+  const double H = (double)dep[q] + (double)eta[q];
+  if (cel) cel[s] = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
+  if (xo) xo[s] = xu[q];
+  if (yo) yo[s] = yv[q];
+}
+
+__global__ void k_max_raw(int nx, int ny, int pitch, const float* __restrict__ dep,
+                          const float* __restrict__ hmax, const float* __restrict__ velmax,
+                          double* hout, double* vout, double g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i, s = (size_t)j * nx + i;
+  const double H = (double)dep[q] + (double)hmax[q];
+  if (hout) hout[s] = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
+  if (vout) vout[s] = velmax[q];
+}
+
+// output_maxwave.f:14-27
+__global__ void k_maxwave_out(int nx, int ny, int pitch, const float* __restrict__ dep,
+                              const float* __restrict__ hmax, const float* __restrict__ velmax,
+                              float ground, float* me, float* mv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i, s = (size_t)j * nx + i;
+  const float hm = hmax[q];
+  if (dep[q] + hm > ground) {
+    me[s] = hm;
+    mv[s] = sqrtf(velmax[q]);
+  } else {
+    me[s] = kNan4;
+    mv[s] = kNan4;
+  }
+}
+
+// output_sea_state.f:18-33
+__global__ void k_sea_state(int nxs, int nys, int pitch, int lonsub, int latsub,
+                            const float* __restrict__ dep, const float* __restrict__ eta,
+                            const float* __restrict__ xu, const float* __restrict__ yv,
+                            float ground, float* h, float* u, float* v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nxs || j >= nys) return;
+  const size_t q = (size_t)(latsub * j) * pitch + (size_t)(lonsub * i);
+  const size_t s = (size_t)j * nxs + i;
+  if (dep[q] + eta[q] > ground) {
+    h[s] = eta[q];
+    u[s] = xu[q];
+    v[s] = yv[q];
+  } else {
+    h[s] = kNan4;
+    u[s] = kNan4;
+    v[s] = kNan4;
+  }
+}
+
+// output_gages.f:18-29
+__global__ void k_gauges(int n, const int32_t* __restrict__ I, const int32_t* __restrict__ J,
+                         int pitch, const float* __restrict__ dep, const float* __restrict__ eta,
+                         const float* __restrict__ xu, const float* __restrict__ yv, float ground,
+                         double* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const size_t q = (size_t)(J[k] - 1) * pitch + (size_t)(I[k] - 1);
+  const float H = dep[q] + eta[q];
+  out[k] = H > ground ? (double)eta[q] : (double)kNan4;
+  out[n + k] = xu[q];
+  out[2 * n + k] = yv[q];
+}
+
+// Runup measures: per-block partials of (max runup, its index, wetted land
+// count, wet count) into scratch, finished on the host.
+__global__ void k_runup(int nx, int ny, int pitch, const float* __restrict__ dep,
+                        const float* __restrict__ eta, const float* __restrict__ hmax,
+                        float ground, double* part) {
+  __shared__ double s_best[256];
+  __shared__ long long s_idx[256], s_land[256], s_wet[256];
+  const int t = threadIdx.x;
+  double best = -1.0;
+  long long bidx = -1, nland = 0, nwet = 0;
+  const long long total = (long long)nx * ny;
+  for (long long c = (long long)blockIdx.x * blockDim.x + t; c < total;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(c / nx), i = (int)(c - (long long)j * nx);
+    const size_t q = (size_t)j * pitch + i;
+    const float d = dep[q];
+    if (d + eta[q] > ground) ++nwet;
+    if (d < 0.f && d + hmax[q] > ground) {
+      ++nland;
+      if (-d > best) {
+        best = -d;
+        bidx = c;
+      }
+    }
+  }
+  s_best[t] = best;
+  s_idx[t] = bidx;
+  s_land[t] = nland;
+  s_wet[t] = nwet;
+  __syncthreads();
+  for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+    if (t < w) {
+      if (s_best[t + w] > s_best[t] ||
+          (s_best[t + w] == s_best[t] && s_idx[t + w] >= 0 && (s_idx[t] < 0 || s_idx[t + w] < s_idx[t]))) {
+        s_best[t] = s_best[t + w];
+        s_idx[t] = s_idx[t + w];
+      }
+      s_land[t] += s_land[t + w];
+      s_wet[t] += s_wet[t + w];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    part[4 * blockIdx.x + 0] = s_best[0];
+    part[4 * blockIdx.x + 1] = (double)s_idx[0];
+    part[4 * blockIdx.x + 2] = (double)s_land[0];
+    part[4 * blockIdx.x + 3] = (double)s_wet[0];
+  }
+}
+
+// Arrival test of feed_children_grid.f:26-46 over parent columns ii1..ii2 and
+// rows kk1..kk2 (1-based).
+__global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
+                          const float* __restrict__ dep, const float* __restrict__ eta,
+                          const float* __restrict__ xu, const float* __restrict__ yv,
+                          double hmin, double cuke, double g, int* flag) {
+  const int ni = ii2 - ii1 + 1, nk = kk2 - kk1 + 1;
+  const long long total = (long long)ni * nk;
+  const double tenth = (double)0.1f;
+  bool hit = false;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total && !hit;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int k = kk1 + (int)(c / ni), i = ii1 + (int)(c % ni);
+    const size_t q = (size_t)(k - 1) * pitch + (size_t)(i - 1);
+    const double d = dep[q];
+    if (d > hmin) {
+      const double H = d + (double)eta[q];
+      const double c2g = fabs(H);  // cel**2/grav
+      if (fabs(c2g - d) > tenth * cuke) hit = true;
+      const double cel = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
+      if ((fabs((double)xu[q]) + fabs((double)yv[q])) * cel > cuke) hit = true;
+    }
+  }
+  if (hit) atomicOr(flag, 1);
+}
+
+// Edge records of feed_children_grid.f:197-325; one thread per child edge node.
+__device__ __forceinline__ void feed_clm(int i, int k, int pitch, const float* dep,
+                                         const float* eta, const float* xu, const float* yv,
+                                         double cc, double hmin, double g, double out[3]) {
+  const size_t q = (size_t)(k - 1) * pitch + (size_t)(i - 1);
+  const double d = dep[q];
+  if (d > hmin) {
+    const double H = d + (double)eta[q];
+    out[0] = cc * (double)xu[q];
+    out[1] = cc * (double)yv[q];
+    out[2] = cc * (fabs(H) - d);
+    (void)g;
+  } else {
+    out[0] = out[1] = out[2] = 0.0;
+  }
+}
+
+__global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N_ny, double W_cx,
+                             double E_cx, double S_cy, double N_cy, const int32_t* __restrict__ WE_ny,
+                             const double* __restrict__ WE_cy, const int32_t* __restrict__ SN_nx,
+                             const double* __restrict__ SN_cx, int pitch, const float* __restrict__ dep,
+                             const float* __restrict__ eta, const float* __restrict__ xu,
+                             const float* __restrict__ yv, double hmin, double g, double* w_out,
+                             double* e_out, double* s_out, double* n_out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * nn) {  // west / east: parent columns (ii, ii+1), rows kk, kk+1
+    const int side = t / nn, i = t % nn;
+    const int ii = side == 0 ? W_nx : E_nx;
+    const double cc = side == 0 ? W_cx : E_cx;
+    const int kk = WE_ny[i];
+    const double w = WE_cy[i];
+    double a0[3], a1[3], b0[3], b1[3];
+    feed_clm(ii, kk, pitch, dep, eta, xu, yv, cc, hmin, g, a0);
+    feed_clm(ii + 1, kk, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, a1);
+    feed_clm(ii, kk + 1, pitch, dep, eta, xu, yv, cc, hmin, g, b0);
+    feed_clm(ii + 1, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, b1);
+    double* o = side == 0 ? w_out : e_out;
+    for (int c = 0; c < 3; ++c) o[i + (size_t)c * nn] = (a0[c] + a1[c]) * w + (b0[c] + b1[c]) * (1 - w);
+  } else if (t < 2 * nn + 2 * mm) {  // south / north: parent rows (kk, kk+1)
+    const int u = t - 2 * nn;
+    const int side = u / mm, i = u % mm;
+    const int kk = side == 0 ? S_ny : N_ny;
+    const double cc = side == 0 ? S_cy : N_cy;
+    const int ii = SN_nx[i];
+    const double w = SN_cx[i];
+    double a0[3], a1[3], b0[3], b1[3];
+    feed_clm(ii, kk, pitch, dep, eta, xu, yv, cc, hmin, g, a0);
+    feed_clm(ii, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, a1);
+    feed_clm(ii + 1, kk, pitch, dep, eta, xu, yv, cc, hmin, g, b0);
+    feed_clm(ii + 1, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, b1);
+    double* o = side == 0 ? s_out : n_out;
+    for (int c = 0; c < 3; ++c) o[i + (size_t)c * mm] = (a0[c] + a1[c]) * w + (b0[c] + b1[c]) * (1 - w);
+  }
+}
+
+int check_device(int* dev) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CLIFFS_ERR_DEVICE;
+  if (cudaGetDevice(dev) != cudaSuccess) return CLIFFS_ERR_DEVICE;
+  cudaDeviceProp pr;
+  if (cudaGetDeviceProperties(&pr, *dev) != cudaSuccess) return CLIFFS_ERR_DEVICE;
+  if (pr.major < 10) return CLIFFS_ERR_DEVICE;
+  return CLIFFS_OK;
+}
+
+Phys<float> phys(const cliffs_ctx* c) {
+  Phys<float> p;
+  p.g = (float)kGrav;
+  p.ginv = (float)(1.0 / kGrav);
+  p.ground = (float)c->ground;
+  p.celmin = (float)c->celmin;
+  p.dt = (float)c->dt;
+  p.gcrough = (float)(kGrav * c->crough);
+  p.sqr2 = (float)kSqr2;
+  return p;
+}
+
+dim3 grid2(int nx, int ny, int bx = 128) { return dim3((nx + bx - 1) / bx, ny); }
+
+int refresh_bitmaps(cliffs_ctx* c) {
+  const int tiles = ((c->nx + 31) / 32) * ((c->ny + 31) / 32);
+  k_bitmaps<<<(tiles + 3) / 4, 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur],
+                                                    (float)c->ground, c->bm_rows[c->cur_r], c->ldr,
+                                                    c->bm_cols[c->cur_c], c->ldc);
+  CK(cudaGetLastError());
+  c->rows_valid = c->cols_valid = true;
+  return CLIFFS_OK;
+}
+
+// Launch one sweep.  fuse_max: update hmax/velmax on the way out.
+int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
+                 int flen, int irec, double cc) {
+  SweepParams P{};
+  const int s = c->cur, o = 1 - c->cur;
+  P.pitch = c->pitch;
+  P.dep = c->dep;
+  P.eta_in = c->eta[s];
+  P.xu_in = c->xu[s];
+  P.yv_in = c->yv[s];
+  P.eta_out = c->eta[o];
+  P.xu_out = c->xu[o];
+  P.yv_out = c->yv[o];
+  P.hmax = fuse_max ? c->hmax : nullptr;
+  P.velmax = fuse_max ? c->velmax : nullptr;
+  P.ph = phys(c);
+  P.status = c->status;
+  P.feedA = fA;
+  P.feedB = fB;
+  P.feed_len = flen;
+  P.irec = irec;
+  P.cc = cc;
+  // which sweep follows decides the bitmap layout this one writes
+  const bool next_is_x = (iu == 1) ? !c->yrun : true;
+  if (iu == 1) {
+    if (!c->rows_valid) {
+      int r = refresh_bitmaps(c);
+      if (r) return r;
+    }
+    P.n = c->nx;
+    P.nlines = c->ny;
+    P.lo = c->jj1;
+    P.hi = c->jj2;
+    P.seg = c->seg_x;
+    P.bm_in = c->bm_rows[c->cur_r];
+    P.ld_in = c->ldr;
+    P.geo = c->geo_x;
+    P.scl = nullptr;
+    P.lscale = c->lscale;
+    P.inv_dx1 = c->inv_dx1_x;
+    P.inv_dxn1 = c->inv_dxn1_x;
+    if (next_is_x) {  // 1-D along x: the next sweep reads rows again
+      P.bm_mode = 1;
+      P.bm_out = c->bm_rows[1 - c->cur_r];
+      P.ld_out = c->ldr;
+    } else {
+      P.bm_mode = 0;
+      P.bm_out = c->bm_cols[c->cur_c];
+      P.ld_out = c->ldc;
+    }
+  } else {
+    if (!c->cols_valid) {
+      int r = refresh_bitmaps(c);
+      if (r) return r;
+    }
+    P.n = c->ny;
+    P.nlines = c->nx;
+    P.lo = c->ii1;
+    P.hi = c->ii2;
+    P.seg = c->seg_y;
+    P.bm_in = c->bm_cols[c->cur_c];
+    P.ld_in = c->ldc;
+    P.geo = c->geo_y;
+    P.scl = c->scl_y;
+    P.lscale = nullptr;
+    P.inv_dx1 = c->inv_dx1_y;
+    P.inv_dxn1 = c->inv_dxn1_y;
+    const bool next_y = !c->xrun;
+    if (next_y) {
+      P.bm_mode = 1;
+      P.bm_out = c->bm_cols[1 - c->cur_c];
+      P.ld_out = c->ldc;
+    } else {
+      P.bm_mode = 0;
+      P.bm_out = c->bm_rows[c->cur_r];
+      P.ld_out = c->ldr;
+    }
+  }
+  const int nlb = (P.nlines + 31) / 32;
+  const int nseg = (P.n + P.seg - 1) / P.seg;
+  const int warps = nlb * nseg;
+  const int blocks = (warps + 3) / 4;
+  ProfPair pp{};
+  if (c->prof) {
+    CK(cudaEventCreate(&pp.a));
+    CK(cudaEventCreate(&pp.b));
+    pp.dir = iu - 1;
+    CK(cudaEventRecord(pp.a, c->stream));
+  }
+  if (iu == 1)
+    sweep_kernel<0><<<blocks, 128, 0, c->stream>>>(P);
+  else
+    sweep_kernel<1><<<blocks, 128, 0, c->stream>>>(P);
+  CK(cudaGetLastError());
+  if (c->prof) {
+    CK(cudaEventRecord(pp.b, c->stream));
+    c->prof_pending.push_back(pp);
+  }
+  c->cur = o;
+  // bitmap bookkeeping
+  if (iu == 1) {
+    if (P.bm_mode == 1) {
+      c->cur_r = 1 - c->cur_r;
+      c->rows_valid = true;
+      c->cols_valid = false;
+    } else {
+      c->cols_valid = true;
+      c->rows_valid = false;
+    }
+  } else {
+    if (P.bm_mode == 1) {
+      c->cur_c = 1 - c->cur_c;
+      c->cols_valid = true;
+      c->rows_valid = false;
+    } else {
+      c->rows_valid = true;
+      c->cols_valid = false;
+    }
+  }
+  return CLIFFS_OK;
+}
+
+__global__ void k_maxwave_update(int nx, int ny, int pitch, const float* __restrict__ eta,
+                                 const float* __restrict__ xu, const float* __restrict__ yv,
+                                 float* hmax, float* velmax) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t q = (size_t)j * pitch + i;
+  if (eta[q] > hmax[q]) hmax[q] = eta[q];
+  const float s = xu[q] * xu[q] + yv[q] * yv[q];
+  if (s > velmax[q]) velmax[q] = s;
+}
+
+int flush_profile(cliffs_ctx* c) {
+  if (c->prof_pending.empty()) return CLIFFS_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  for (auto& p : c->prof_pending) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b));
+    c->prof_ms[p.dir] += ms;
+    c->prof_n[p.dir] += 1;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  c->prof_pending.clear();
+  return CLIFFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cliffs_gpu_strerror(int code) {
+  switch (code) {
+    case CLIFFS_OK: return "ok";
+    case CLIFFS_FEED_ENDED: return "boundary forcing ended (freeze)";
+    case CLIFFS_ERR_ARG: return "invalid argument";
+    case CLIFFS_ERR_CUDA: return "CUDA runtime error";
+    case CLIFFS_ERR_NAN: return "non-finite value in the state";
+    case CLIFFS_ERR_NOMEM: return "device allocation failed";
+    case CLIFFS_ERR_STATE: return "call out of order";
+    case CLIFFS_ERR_DEVICE: return "no usable sm_103 device";
+    default: return "unknown status";
+  }
+}
+
+int cliffs_gpu_metrics(int32_t nx, int32_t ny, int32_t cartesian, const double* xcrd,
+                       const double* ycrd, double* dx, double* row_scale, double* dy, double* zeta) {
+  if (nx < 1 || ny < 1 || !xcrd || !ycrd) return CLIFFS_ERR_ARG;
+  const double beta = kPi * kEarthR / 180.;  // MasterGrid.f:237
+  if (nx > 2) {
+    if (dx)
+      for (int i = 0; i < nx - 1; ++i)
+        dx[i] = cartesian ? xcrd[i + 1] - xcrd[i] : beta * (xcrd[i + 1] - xcrd[i]);
+    if (row_scale)
+      for (int j = 0; j < ny; ++j) row_scale[j] = cartesian ? 1.0 : cos(kPi / 180. * ycrd[j]);
+  }
+  if (ny > 2) {
+    if (dy)
+      for (int j = 0; j < ny - 1; ++j)
+        dy[j] = cartesian ? ycrd[j + 1] - ycrd[j] : beta * (ycrd[j + 1] - ycrd[j]);
+    if (zeta)
+      for (int j = 0; j < ny; ++j)
+        zeta[j] = cartesian ? 0.0 : (0.125 / kEarthR) * tan(kPi / 180. * ycrd[j]);
+  }
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
+  if (!d || !out || !d->dep || d->nx < 1 || d->ny < 1) return CLIFFS_ERR_ARG;
+  if (d->nx <= 2 && d->ny <= 2) return CLIFFS_ERR_ARG;
+  if (d->nx > 2 && !d->dx) return CLIFFS_ERR_ARG;
+  if (d->ny > 2 && !d->dy) return CLIFFS_ERR_ARG;
+  if (!(d->dt > 0) || !(d->ground > 0) || d->crough < 0) return CLIFFS_ERR_ARG;
+  int dev = 0;
+  int r = check_device(&dev);
+  if (r) return r;
+  cliffs_ctx* c = new cliffs_ctx();
+  c->dev = dev;
+  c->nx = d->nx;
+  c->ny = d->ny;
+  c->pitch = (d->nx + 31) / 32 * 32;
+  c->ground = d->ground;
+  c->crough = d->crough;
+  c->dt = d->dt;
+  c->celmin = sqrt(kGrav * d->ground);  // cliffs_main.f:227
+  // 1-D / 2-D detection (cliffs_main.f:140-164)
+  c->xrun = d->nx > 2;
+  c->yrun = d->ny > 2;
+  c->ii1 = c->xrun ? 2 : 1;
+  c->ii2 = c->xrun ? d->nx - 1 : 1;
+  c->jj1 = c->yrun ? 2 : 1;
+  c->jj2 = c->yrun ? d->ny - 1 : 1;
+  c->ldr = (d->nx + 31) / 32;
+  c->ldc = (d->ny + 31) / 32;
+  const size_t cells = (size_t)c->pitch * c->ny;
+  auto fail = [&](int code) {
+    cliffs_gpu_destroy(c);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
+  c->stream = c->own;
+  if (dalloc(&c->dep, cells) || dalloc(&c->eta[0], cells) || dalloc(&c->eta[1], cells) ||
+      dalloc(&c->xu[0], cells) || dalloc(&c->xu[1], cells) || dalloc(&c->yv[0], cells) ||
+      dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
+      dalloc(&c->bm_rows[0], (size_t)c->ny * c->ldr) || dalloc(&c->bm_rows[1], (size_t)c->ny * c->ldr) ||
+      dalloc(&c->bm_cols[0], (size_t)c->nx * c->ldc) || dalloc(&c->bm_cols[1], (size_t)c->nx * c->ldc) ||
+      dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
+      dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
+      dalloc(&c->status, 1) || dalloc(&c->d_flag, 1))
+    return fail(CLIFFS_ERR_NOMEM);
+  // bathymetry, padded rows
+  std::vector<float> h((size_t)c->pitch * c->ny, 0.f);
+  for (int j = 0; j < c->ny; ++j)
+    for (int i = 0; i < c->nx; ++i) h[(size_t)j * c->pitch + i] = (float)d->dep[(size_t)j * c->nx + i];
+  if (cudaMemcpy(c->dep, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(CLIFFS_ERR_CUDA);
+  // geometry tables
+  auto build_geo = [&](int n, const double* s, std::vector<float4>& geo, float& i1, float& in1) {
+    geo.assign((size_t)n, make_float4(0, 0, 0, 0));
+    for (int m = 2; m <= n - 1; ++m) {
+      const double fm = s[m - 2], fp = s[m - 1];
+      geo[m - 1] = make_float4((float)(1.0 / fm), (float)(1.0 / fp), (float)(d->dt / (fm + fp)), (float)(fp - fm));
+    }
+    i1 = (float)(1.0 / s[0]);
+    in1 = (float)(1.0 / s[n - 2]);
+  };
+  std::vector<float4> gx, gy;
+  if (c->xrun) build_geo(c->nx, d->dx, gx, c->inv_dx1_x, c->inv_dxn1_x);
+  else gx.assign((size_t)c->nx, make_float4(0, 0, 0, 0));
+  if (c->yrun) build_geo(c->ny, d->dy, gy, c->inv_dx1_y, c->inv_dxn1_y);
+  else gy.assign((size_t)c->ny, make_float4(0, 0, 0, 0));
+  std::vector<float> sy((size_t)c->ny, 0.f);
+  if (d->zeta)
+    for (int j = 0; j < c->ny; ++j) sy[j] = (float)d->zeta[j];
+  std::vector<float2> ls((size_t)c->ny, make_float2(1.f, 1.f));
+  if (d->row_scale)
+    for (int j = 0; j < c->ny; ++j) ls[j] = make_float2((float)d->row_scale[j], (float)(1.0 / d->row_scale[j]));
+  if (cudaMemcpy(c->geo_x, gx.data(), gx.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->geo_y, gy.data(), gy.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->scl_y, sy.data(), sy.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->lscale, ls.data(), ls.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(c->status, 0, sizeof(unsigned)) != cudaSuccess)
+    return fail(CLIFFS_ERR_CUDA);
+  if (!d->row_scale) {
+    cudaFree(c->lscale);
+    c->lscale = nullptr;
+  }
+  if (!d->zeta) {
+    cudaFree(c->scl_y);
+    c->scl_y = nullptr;
+  }
+  *out = c;
+  return CLIFFS_OK;
+}
+
+void cliffs_gpu_destroy(cliffs_ctx* c) {
+  if (!c) return;
+  cudaStreamSynchronize(c->stream);
+  flush_profile(c);
+  void* ptrs[] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
+                  c->hmax, c->velmax, c->bm_rows[0], c->bm_rows[1], c->bm_cols[0], c->bm_cols[1],
+                  c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
+                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& n : c->nests) {
+    cudaFree(n.WE_ny);
+    cudaFree(n.WE_cy);
+    cudaFree(n.SN_nx);
+    cudaFree(n.SN_cx);
+  }
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+int cliffs_gpu_set_stream(cliffs_ctx* c, void* stream) {
+  if (!c) return CLIFFS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own;
+  return CLIFFS_OK;
+}
+
+static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const double* xv,
+                         const double* yv, bool reset_max) {
+  if (!c || !src) return CLIFFS_ERR_ARG;
+  const size_t n = (size_t)c->nx * c->ny;
+  double *dsrc = nullptr, *dx = nullptr, *dy = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&dsrc, n) || (xv && dalloc(&dx, n)) || (yv && dalloc(&dy, n))) r = CLIFFS_ERR_NOMEM;
+  if (!r && cudaMemcpyAsync(dsrc, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && xv && cudaMemcpyAsync(dx, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    c->cur = 0;
+    k_init_state<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(
+        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, c->eta[0], c->xu[0], c->yv[0], c->ground, kGrav);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && reset_max) {
+    k_reset_max<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r) r = refresh_bitmaps(c);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(dsrc);
+  if (dx) cudaFree(dx);
+  if (dy) cudaFree(dy);
+  if (!r) c->have_state = true;
+  return r;
+}
+
+int cliffs_gpu_set_initial(cliffs_ctx* c, const double* H, const double* xv, const double* yv) {
+  return upload_common(c, H, 0, xv, yv, true);
+}
+
+int cliffs_gpu_upload_state(cliffs_ctx* c, const double* cel, const double* xv, const double* yv) {
+  if (c && !c->have_state) {
+    int r = upload_common(c, cel, 1, xv, yv, true);
+    return r;
+  }
+  return upload_common(c, cel, 1, xv, yv, false);
+}
+
+int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv) {
+  if (!c) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const size_t n = (size_t)c->nx * c->ny;
+  double *a = nullptr, *b = nullptr, *e = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&a, n) || dalloc(&b, n) || dalloc(&e, n)) r = CLIFFS_ERR_NOMEM;
+  if (!r) {
+    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur],
+                                                          c->xu[c->cur], c->yv[c->cur], a, b, e, kGrav);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && cel && cudaMemcpyAsync(cel, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && xv && cudaMemcpyAsync(xv, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && yv && cudaMemcpyAsync(yv, e, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  if (e) cudaFree(e);
+  return r;
+}
+
+int cliffs_gpu_set_feed(cliffs_ctx* c, int32_t nt, const double* tinput, const double* west,
+                        const double* east, const double* south, const double* north, int32_t irec,
+                        int32_t freeze) {
+  if (!c) return CLIFFS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream));
+  double** bufs[] = {&c->fw, &c->fe, &c->fs, &c->fn};
+  for (double** b : bufs)
+    if (*b) {
+      cudaFree(*b);
+      *b = nullptr;
+    }
+  c->nt = 0;
+  c->feed_on = false;
+  c->tinput.clear();
+  if (nt == 0) return CLIFFS_OK;
+  if (nt < 2 || !tinput || irec < 1 || irec > nt) return CLIFFS_ERR_ARG;
+  if (c->xrun && (!west || !east)) return CLIFFS_ERR_ARG;
+  if (c->yrun && (!south || !north)) return CLIFFS_ERR_ARG;
+  c->tinput.assign(tinput, tinput + nt);
+  const size_t nxr = (size_t)c->ny * 3 * nt, nyr = (size_t)c->nx * 3 * nt;
+  if (c->xrun) {
+    if (dalloc(&c->fw, nxr) || dalloc(&c->fe, nxr)) return CLIFFS_ERR_NOMEM;
+    CK(cudaMemcpy(c->fw, west, nxr * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->fe, east, nxr * 8, cudaMemcpyHostToDevice));
+  }
+  if (c->yrun) {
+    if (dalloc(&c->fs, nyr) || dalloc(&c->fn, nyr)) return CLIFFS_ERR_NOMEM;
+    CK(cudaMemcpy(c->fs, south, nyr * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->fn, north, nyr * 8, cudaMemcpyHostToDevice));
+  }
+  c->nt = nt;
+  c->irec = irec;
+  c->freeze = freeze != 0;
+  c->feed_on = true;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_feed_start(cliffs_ctx* c, double cuke) {
+  // get_boundary_feed.f:473-496, on the host copy of the records
+  if (!c || c->nt < 2) return CLIFFS_ERR_ARG;
+  const int nt = c->nt;
+  std::vector<double> w, e, s, n;
+  const size_t nxr = (size_t)c->ny * 3 * nt, nyr = (size_t)c->nx * 3 * nt;
+  if (c->xrun) {
+    w.resize(nxr);
+    e.resize(nxr);
+    if (cudaMemcpy(w.data(), c->fw, nxr * 8, cudaMemcpyDeviceToHost) ||
+        cudaMemcpy(e.data(), c->fe, nxr * 8, cudaMemcpyDeviceToHost))
+      return CLIFFS_ERR_CUDA;
+  }
+  if (c->yrun) {
+    s.resize(nyr);
+    n.resize(nyr);
+    if (cudaMemcpy(s.data(), c->fs, nyr * 8, cudaMemcpyDeviceToHost) ||
+        cudaMemcpy(n.data(), c->fn, nyr * 8, cudaMemcpyDeviceToHost))
+      return CLIFFS_ERR_CUDA;
+  }
+  auto amp = [](const double* a, int len) {
+    double mx = a[0], mn = a[0];
+    for (int k = 1; k < len; ++k) {
+      mx = std::max(mx, a[k]);
+      mn = std::min(mn, a[k]);
+    }
+    return mx > -mn ? mx : -mn;
+  };
+  double w1 = 0, w2 = 0, w3 = 0, w4 = 0;
+  int it;
+  for (it = 1; it <= nt; ++it) {
+    if (c->xrun) {
+      const size_t o = (size_t)c->ny * 2 + (size_t)(it - 1) * c->ny * 3;
+      w1 = amp(w.data() + o, c->ny);
+      w2 = amp(e.data() + o, c->ny);
+    }
+    if (c->yrun) {
+      const size_t o = (size_t)c->nx * 2 + (size_t)(it - 1) * c->nx * 3;
+      w3 = amp(s.data() + o, c->nx);
+      w4 = amp(n.data() + o, c->nx);
+    }
+    const double wave = std::max(std::max(w1, w2), std::max(w3, w4));
+    if (wave >= cuke) break;
+  }
+  return it >= nt ? -1 : it;
+}
+
+int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_done) {
+  if (!c || !t || nsteps < 0) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if (steps_done) *steps_done = 0;
+  for (int s = 0; s < nsteps; ++s) {
+    *t = *t + c->dt;
+    // forcing record cursor (cliffs_main.f:305-315)
+    while (c->feed_on && *t >= c->tinput[c->irec - 1]) {
+      if (c->irec == c->nt) {
+        c->feed_on = false;
+        if (c->freeze) return CLIFFS_FEED_ENDED;
+      } else {
+        c->irec = c->irec + 1;
+      }
+    }
+    double cc = 0;
+    if (c->feed_on) cc = (c->tinput[c->irec - 1] - *t) / (c->tinput[c->irec - 1] - c->tinput[c->irec - 2]);
+    if (c->xrun) {
+      int r = launch_sweep(c, 1, !c->yrun, c->feed_on ? c->fw : nullptr, c->feed_on ? c->fe : nullptr, c->ny,
+                           c->irec, cc);
+      if (r) return r;
+    }
+    if (c->yrun) {
+      int r = launch_sweep(c, 2, true, c->feed_on ? c->fs : nullptr, c->feed_on ? c->fn : nullptr, c->nx,
+                           c->irec, cc);
+      if (r) return r;
+    }
+    if (steps_done) *steps_done = s + 1;
+    if (c->prof && c->prof_pending.size() > 4096) {
+      int r = flush_profile(c);
+      if (r) return r;
+    }
+  }
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_set_edges(cliffs_ctx* c, const double* edge1, const double* edge2);
+
+int cliffs_gpu_sweep(cliffs_ctx* c, int32_t iu) {
+  if (!c || (iu != 1 && iu != 2)) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if ((iu == 1 && !c->xrun) || (iu == 2 && !c->yrun)) return CLIFFS_ERR_ARG;
+  const int len = iu == 1 ? c->ny : c->nx;
+  if (c->edges_static) {
+    // static edge1/edge2, stored as two identical records: lerp weight 1
+    const int mx = std::max(c->xrun ? c->ny : 1, c->yrun ? c->nx : 1);
+    (void)len;
+    return launch_sweep(c, iu, false, c->edge_s[0], c->edge_s[1], mx, 2, 1.0);
+  }
+  return launch_sweep(c, iu, false, nullptr, nullptr, len, 2, 1.0);
+}
+
+int cliffs_gpu_set_edges(cliffs_ctx* c, const double* edge1, const double* edge2) {
+  if (!c) return CLIFFS_ERR_ARG;
+  const int mx = std::max(c->xrun ? c->ny : 1, c->yrun ? c->nx : 1);
+  if (!edge1 || !edge2) {
+    c->edges_static = false;
+    return CLIFFS_OK;
+  }
+  for (int k = 0; k < 2; ++k)
+    if (!c->edge_s[k] && dalloc(&c->edge_s[k], (size_t)mx * 3 * 2)) return CLIFFS_ERR_NOMEM;
+  for (int k = 0; k < 2; ++k) {
+    const double* src = k == 0 ? edge1 : edge2;
+    CK(cudaMemcpy(c->edge_s[k], src, (size_t)mx * 3 * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->edge_s[k] + (size_t)mx * 3, src, (size_t)mx * 3 * 8, cudaMemcpyHostToDevice));
+  }
+  c->edges_static = true;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_maxwave_update(cliffs_ctx* c) {
+  if (!c) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  k_maxwave_update<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->eta[c->cur],
+                                                              c->xu[c->cur], c->yv[c->cur], c->hmax, c->velmax);
+  CK(cudaGetLastError());
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
+  if (!c || !me || !mv) return CLIFFS_ERR_ARG;
+  const size_t n = (size_t)c->nx * c->ny;
+  float *a = nullptr, *b = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
+  if (!r) {
+    k_maxwave_out<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax,
+                                                             c->velmax, (float)c->ground, a, b);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && cudaMemcpyAsync(me, a, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && cudaMemcpyAsync(mv, b, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  return r;
+}
+
+int cliffs_gpu_get_max_raw(cliffs_ctx* c, double* hm, double* vm) {
+  if (!c) return CLIFFS_ERR_ARG;
+  const size_t n = (size_t)c->nx * c->ny;
+  double *a = nullptr, *b = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
+  if (!r) {
+    k_max_raw<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax,
+                                                         a, b, kGrav);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && hm && cudaMemcpyAsync(hm, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && vm && cudaMemcpyAsync(vm, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  return r;
+}
+
+int cliffs_gpu_get_sea_state(cliffs_ctx* c, int32_t lonsub, int32_t latsub, float* h, float* u, float* v) {
+  if (!c || lonsub < 1 || latsub < 1 || !h || !u || !v) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const int nxs = (c->nx - 1) / lonsub + 1, nys = (c->ny - 1) / latsub + 1;
+  const size_t n = (size_t)nxs * nys;
+  float* a = nullptr;
+  if (dalloc(&a, 3 * n)) return CLIFFS_ERR_NOMEM;
+  int r = CLIFFS_OK;
+  const int s = c->cur;
+  k_sea_state<<<grid2(nxs, nys), 128, 0, c->stream>>>(nxs, nys, c->pitch, lonsub, latsub, c->dep, c->eta[s],
+                                                      c->xu[s], c->yv[s], (float)c->ground, a, a + n, a + 2 * n);
+  if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  if (!r && (cudaMemcpyAsync(h, a, n * 4, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(u, a + n, n * 4, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(v, a + 2 * n, n * 4, cudaMemcpyDeviceToHost, c->stream)))
+    r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(a);
+  return r;
+}
+
+int cliffs_gpu_get_gauges(cliffs_ctx* c, int32_t n, const int32_t* I, const int32_t* J, double* eta, double* u,
+                          double* v) {
+  if (!c || n < 0 || (n > 0 && (!I || !J || !eta || !u || !v))) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if (n == 0) return CLIFFS_OK;
+  for (int k = 0; k < n; ++k)
+    if (I[k] < 1 || I[k] > c->nx || J[k] < 1 || J[k] > c->ny) return CLIFFS_ERR_ARG;
+  int32_t* dij = nullptr;
+  double* out = nullptr;
+  if (dalloc(&dij, 2 * (size_t)n) || dalloc(&out, 3 * (size_t)n)) {
+    if (dij) cudaFree(dij);
+    return CLIFFS_ERR_NOMEM;
+  }
+  int r = CLIFFS_OK;
+  if (cudaMemcpyAsync(dij, I, n * 4, cudaMemcpyHostToDevice, c->stream) ||
+      cudaMemcpyAsync(dij + n, J, n * 4, cudaMemcpyHostToDevice, c->stream))
+    r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    const int s = c->cur;
+    k_gauges<<<(n + 127) / 128, 128, 0, c->stream>>>(n, dij, dij + n, c->pitch, c->dep, c->eta[s], c->xu[s],
+                                                     c->yv[s], (float)c->ground, out);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && (cudaMemcpyAsync(eta, out, n * 8, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(u, out + n, n * 8, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(v, out + 2 * n, n * 8, cudaMemcpyDeviceToHost, c->stream)))
+    r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(dij);
+  cudaFree(out);
+  return r;
+}
+
+int cliffs_gpu_runup(cliffs_ctx* c, cliffs_runup* o) {
+  if (!c || !o) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const int blocks = 304;
+  if (c->red_cap < 4 * blocks) {
+    if (c->red) cudaFree(c->red);
+    c->red = nullptr;
+    if (dalloc(&c->red, 4 * (size_t)blocks)) return CLIFFS_ERR_NOMEM;
+    c->red_cap = 4 * blocks;
+  }
+  k_runup<<<blocks, 256, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur], c->hmax,
+                                         (float)c->ground, c->red);
+  CK(cudaGetLastError());
+  std::vector<double> h(4 * (size_t)blocks);
+  CK(cudaMemcpyAsync(h.data(), c->red, h.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double best = -1;
+  long long idx = -1, land = 0, wet = 0;
+  for (int b = 0; b < blocks; ++b) {
+    const double v = h[4 * b];
+    const long long id = (long long)h[4 * b + 1];
+    if (v > best || (v == best && id >= 0 && (idx < 0 || id < idx))) {
+      best = v;
+      idx = id;
+    }
+    land += (long long)h[4 * b + 2];
+    wet += (long long)h[4 * b + 3];
+  }
+  o->max_runup = idx >= 0 ? best : 0.0;
+  o->i = idx >= 0 ? (int32_t)(idx % c->nx) + 1 : 0;
+  o->j = idx >= 0 ? (int32_t)(idx / c->nx) + 1 : 0;
+  o->wetted_land = land;
+  o->wet_now = wet;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_nest_add(cliffs_ctx* c, const cliffs_nest_desc* d, int32_t* id) {
+  if (!c || !d || !id || d->mm < 1 || d->nn < 1 || !d->WE_ny || !d->WE_cy || !d->SN_nx || !d->SN_cx)
+    return CLIFFS_ERR_ARG;
+  if (!c->xrun || !c->yrun) return CLIFFS_ERR_ARG;  // allabout.f:35-39: no nesting in 1-D
+  auto inside_x = [&](int i) { return i >= 1 && i + 1 <= c->nx; };
+  auto inside_y = [&](int j) { return j >= 1 && j + 1 <= c->ny; };
+  if (!inside_x(d->W_nx) || !inside_x(d->E_nx) || !inside_y(d->S_ny) || !inside_y(d->N_ny)) return CLIFFS_ERR_ARG;
+  for (int k = 0; k < d->nn; ++k)
+    if (!inside_y(d->WE_ny[k])) return CLIFFS_ERR_ARG;
+  for (int k = 0; k < d->mm; ++k)
+    if (!inside_x(d->SN_nx[k])) return CLIFFS_ERR_ARG;
+  Nest n;
+  n.d = *d;
+  if (dalloc(&n.WE_ny, d->nn) || dalloc(&n.WE_cy, d->nn) || dalloc(&n.SN_nx, d->mm) || dalloc(&n.SN_cx, d->mm))
+    return CLIFFS_ERR_NOMEM;
+  CK(cudaMemcpy(n.WE_ny, d->WE_ny, d->nn * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(n.WE_cy, d->WE_cy, d->nn * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(n.SN_nx, d->SN_nx, d->mm * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(n.SN_cx, d->SN_cx, d->mm * 8, cudaMemcpyHostToDevice));
+  n.d.WE_ny = nullptr;
+  n.d.WE_cy = nullptr;
+  n.d.SN_nx = nullptr;
+  n.d.SN_cx = nullptr;
+  c->nests.push_back(n);
+  *id = (int32_t)c->nests.size() - 1;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arrived, double* w, double* e,
+                          double* s, double* nn_out) {
+  if (!c || !arrived || id < 0 || id >= (int32_t)c->nests.size()) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const Nest& n = c->nests[id];
+  const int st = c->cur;
+  if (!*arrived) {
+    // footprint: parent rows WE_ny(1)..WE_ny(nn)+1, columns SN_nx(1)..SN_nx(mm)+1
+    int32_t k1, k2, i1, i2;
+    CK(cudaMemcpy(&k1, n.WE_ny, 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&k2, n.WE_ny + n.d.nn - 1, 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&i1, n.SN_nx, 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&i2, n.SN_nx + n.d.mm - 1, 4, cudaMemcpyDeviceToHost));
+    k2 += 1;
+    i2 += 1;
+    CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+    k_arrival<<<152, 256, 0, c->stream>>>(i1, i2, k1, k2, c->pitch, c->dep, c->eta[st], c->xu[st], c->yv[st],
+                                          c->ground, cuke, kGrav, c->d_flag);
+    CK(cudaGetLastError());
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (f) *arrived = 1;
+  }
+  if (!*arrived) return 0;
+  if (!w || !e || !s || !nn_out) return CLIFFS_ERR_ARG;
+  const int mm = n.d.mm, nn = n.d.nn;
+  double* buf = nullptr;
+  if (dalloc(&buf, 6 * (size_t)(mm + nn))) return CLIFFS_ERR_NOMEM;
+  double *dw = buf, *de = buf + 3 * (size_t)nn, *ds = buf + 6 * (size_t)nn, *dn = ds + 3 * (size_t)mm;
+  const int threads = 2 * (mm + nn);
+  k_feed_child<<<(threads + 127) / 128, 128, 0, c->stream>>>(
+      mm, nn, n.d.W_nx, n.d.E_nx, n.d.S_ny, n.d.N_ny, n.d.W_cx, n.d.E_cx, n.d.S_cy, n.d.N_cy, n.WE_ny, n.WE_cy,
+      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->eta[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn);
+  int r = CLIFFS_OK;
+  if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  if (!r && (cudaMemcpyAsync(w, dw, 3 * nn * 8, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(e, de, 3 * nn * 8, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(s, ds, 3 * mm * 8, cudaMemcpyDeviceToHost, c->stream) ||
+             cudaMemcpyAsync(nn_out, dn, 3 * mm * 8, cudaMemcpyDeviceToHost, c->stream)))
+    r = CLIFFS_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(buf);
+  return r ? r : 1;
+}
+
+int cliffs_gpu_status(cliffs_ctx* c, uint32_t* flags) {
+  if (!c || !flags) return CLIFFS_ERR_ARG;
+  unsigned f = 0;
+  CK(cudaMemcpyAsync(&f, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *flags = f;
+  return (f & CLIFFS_ST_NAN) ? CLIFFS_ERR_NAN : CLIFFS_OK;
+}
+
+int cliffs_gpu_sync(cliffs_ctx* c) {
+  if (!c) return CLIFFS_ERR_ARG;
+  CK(cudaStreamSynchronize(c->stream));
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_profile(cliffs_ctx* c, int32_t enable) {
+  if (!c) return CLIFFS_ERR_ARG;
+  int r = flush_profile(c);
+  c->prof = enable != 0;
+  c->prof_ms[0] = c->prof_ms[1] = 0;
+  c->prof_n[0] = c->prof_n[1] = 0;
+  return r;
+}
+
+int cliffs_gpu_profile_read(cliffs_ctx* c, double* x_ms, int64_t* x_n, double* y_ms, int64_t* y_n) {
+  if (!c) return CLIFFS_ERR_ARG;
+  int r = flush_profile(c);
+  if (r) return r;
+  if (x_ms) *x_ms = c->prof_n[0] ? c->prof_ms[0] / c->prof_n[0] : 0.0;
+  if (x_n) *x_n = c->prof_n[0];
+  if (y_ms) *y_ms = c->prof_n[1] ? c->prof_ms[1] / c->prof_n[1] : 0.0;
+  if (y_n) *y_n = c->prof_n[1];
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t seg_x, int32_t seg_y) {
+  if (!c || seg_x < 0 || seg_y < 0 || seg_x % 32 || seg_y % 32) return CLIFFS_ERR_ARG;
+  if (seg_x) c->seg_x = seg_x;
+  if (seg_y) c->seg_y = seg_y;
+  return CLIFFS_OK;
+}
+
+}  // extern "C"

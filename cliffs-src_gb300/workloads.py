@@ -1,0 +1,123 @@
+"""Seeded synthetic inputs with the shapes of the Cliffs benchmark workloads.
+
+The reference ships no benchmark data (only two example archives), so these
+generators stand in for its inputs.  Every case is a dict with the fields a
+Cliffs run reads (cliffs_main.f, allabout.f):
+
+  xcrd, ycrd   grid coordinates (m, or degrees when cartesian is False)
+  cartesian    coordinate flag (allabout.f:23)
+  dep          still-water depth (ny, nx) after bottom deformation, >0 water,
+               rounded to float32 values so every arithmetic path starts from
+               identical bathymetry
+  H0           initial total water depth (ny, nx) before the celerity
+               transform of cliffs_main.f:218-227 (cel = dep, plus the surface
+               deformation, cliffs_main.f:193-212)
+  u0, v0       initial velocities (ny, nx)
+  ground, crough, dt, steps
+  gauges       (I, J) 1-based node indices (allabout.f:83-89)
+  gout, seaout output intervals in steps
+
+Sizes, depths and sources follow the benchmark configurations: a 1-D channel
+with a solitary wave running up a 1:20 beach, and a 2-D shelf/slope basin
+with an elliptical Gaussian uplift.
+"""
+import numpy as np
+
+GRAV = 9.800000190734863
+
+
+def _f32(a):
+    return np.asarray(a, np.float64).astype(np.float32).astype(np.float64)
+
+
+def channel_1d(seed=0, n=2000, dx=0.05, steps=5000):
+    """1-D Cartesian channel: flat 1 m depth over the offshore 60 %, then a
+    1:20 slope rising to +0.5 m of dry land (reached at x = 90 m), flat land
+    to the end.  A sech^2 hump of amplitude A ~ U[0.02, 0.05] m (seeded),
+    k = sqrt(3A/(4h^3)), centred 10 m offshore of the slope toe, u = 0.
+    CFL 0.8 on the 1 m depth.  The coast is on the high-x side."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(n, dtype=np.float64) * dx
+    h = 1.0
+    toe = 0.6 * n * dx
+    dep = np.where(x < toe, h, h - (x - toe) / 20.0)
+    dep = np.maximum(dep, -0.5)
+    dep = _f32(dep).reshape(1, n)
+    A = rng.uniform(0.02, 0.05)
+    k = np.sqrt(3 * A / (4 * h ** 3))
+    x0 = toe - 10.0
+    eta0 = A / np.cosh(k * (x - x0)) ** 2
+    H0 = dep + eta0.reshape(1, n)
+    dt = 0.8 * dx / np.sqrt(GRAV * h)
+    return dict(name="channel_1d", xcrd=x, ycrd=np.zeros(1), cartesian=True,
+                dep=dep, H0=H0, u0=np.zeros((1, n)), v0=np.zeros((1, n)),
+                ground=0.003, crough=0.0, dt=float(dt), steps=steps,
+                gauges=(np.array([], np.int32), np.array([], np.int32)),
+                gout=100, seaout=100, amplitude=float(A))
+
+
+def _powerlaw_field(rng, ny, nx):
+    """Random field with a k^-2 power spectrum, unit RMS."""
+    ky = np.fft.fftfreq(ny)[:, None]
+    kx = np.fft.rfftfreq(nx)[None, :]
+    kk = np.sqrt(kx * kx + ky * ky)
+    kk[0, 0] = 1.0
+    amp = 1.0 / kk  # power ~ k^-2
+    amp[0, 0] = 0.0
+    ph = rng.standard_normal((ny, nx // 2 + 1)) + 1j * rng.standard_normal((ny, nx // 2 + 1))
+    f = np.fft.irfft2(amp * ph, s=(ny, nx))
+    return f / (f.std() + 1e-30)
+
+
+def shelf_profile(xkm, length_km):
+    """Cross-shore depth profile (m, >0 water) over a basin of the given
+    length: 4000 m abyss, tanh shelf break to 200 m, 200 m shelf, then a
+    linear slope reaching +50 m of land at the last column."""
+    L = length_km
+    brk = L - 26.8     # shelf-break centre
+    s0 = L - 8.8       # start of the linear slope
+    d = 200.0 + 1900.0 * (1.0 - np.tanh((xkm - brk) / 2.0))
+    slope = 200.0 - 250.0 * (xkm - s0) / (L - s0)
+    return np.where(xkm < s0, d, slope)
+
+
+def shelf_2d(seed=0, nx=2048, ny=2048, dx=100.0, steps=3000, amp=2.0,
+             axes_km=(100.0, 50.0), ngauges=64, perturb=0.05, centre_km=None):
+    """2-D Cartesian basin, x cross-shore: 4000 m abyss, tanh shelf break to
+    200 m, linear slope to +50 m land at the last columns, plus a k^-2 random
+    perturbation of `perturb` x local |depth| (which also roughens the land).
+    Source: elliptical Gaussian bottom uplift (full axes axes_km, amplitude
+    amp, seeded orientation) applied instantaneously as in quake=1.
+    Gauges at seeded wet nodes; dt from CFL 0.8 on the maximum depth."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx, dtype=np.float64) * dx
+    y = np.arange(ny, dtype=np.float64) * dx
+    Lkm = nx * dx / 1000.0
+    d0 = shelf_profile(x / 1000.0, Lkm)[None, :].repeat(ny, 0)
+    if perturb:
+        d0 = d0 + perturb * np.abs(d0) * _powerlaw_field(rng, ny, nx)
+    d0 = _f32(d0)
+    theta = rng.uniform(0, np.pi)
+    if centre_km is None:
+        cx, cy = 0.45 * nx * dx, 0.5 * ny * dx
+    else:
+        cx, cy = centre_km[0] * 1000.0, centre_km[1] * 1000.0
+    a, b = axes_km[0] * 500.0, axes_km[1] * 500.0  # half-axes in m
+    X, Y = np.meshgrid(x - cx, y - cy)
+    xr = X * np.cos(theta) + Y * np.sin(theta)
+    yr = -X * np.sin(theta) + Y * np.cos(theta)
+    uplift = amp * np.exp(-(xr / a) ** 2 - (yr / b) ** 2)
+    # quake=1 (cliffs_main.f:193-207): cel = dep first, then dep -= uplift
+    H0 = d0.copy()
+    dep = _f32(d0 - uplift)
+    hmax = float(np.max(d0))
+    dt = 0.8 * dx / np.sqrt(GRAV * hmax)
+    wet = np.argwhere(d0 > 10.0)
+    pick = wet[rng.choice(len(wet), ngauges, replace=False)] if ngauges else np.zeros((0, 2), int)
+    J = (pick[:, 0] + 1).astype(np.int32)
+    I = (pick[:, 1] + 1).astype(np.int32)
+    return dict(name=f"shelf_2d_{nx}x{ny}", xcrd=x, ycrd=y, cartesian=True,
+                dep=dep, H0=H0, u0=np.zeros((ny, nx)), v0=np.zeros((ny, nx)),
+                ground=0.01, crough=0.0, dt=float(dt), steps=steps,
+                gauges=(I, J), gout=10, seaout=steps + 1, amplitude=float(amp),
+                theta=float(theta))

@@ -1,0 +1,196 @@
+/*
+ * cliffs_gpu.h -- C ABI of the GB300 (sm_103a) Cliffs time-stepping library.
+ *
+ * Drop-in for the hot path of the Cliffs tsunami model: the loop body of
+ * cliffs_main.f:303-378 (x- and y-sweeps of subroutine cliffs, cliffs.f:17-346;
+ * the max-wave update; the nested-grid feed; gauge and screenshot sampling).
+ * The Fortran driver keeps its setup and NetCDF I/O and calls these entry
+ * points through ISO_C_BINDING; fields stay resident on one GPU between
+ * output intervals.
+ *
+ * Conventions
+ *  - Every 2-D array is column-major (x fastest) exactly like the Fortran
+ *    module arrays: element (i,j), 1-based, at [(i-1) + (j-1)*nx].
+ *  - Grid indices passed in (gauges, nest tables, records) are 1-based.
+ *  - Every call returns an int status: CLIFFS_OK (0) on success, a positive
+ *    informational code, or a negative error code; nothing in the library
+ *    calls exit().  cliffs_gpu_strerror() names a code.
+ *  - One context is driven by one host thread at a time; calls on a context
+ *    are ordered on its CUDA stream.  Independent contexts (ensembles,
+ *    parent/child grids) may share a device.
+ */
+#ifndef CLIFFS_GPU_H
+#define CLIFFS_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  CLIFFS_OK = 0,
+  CLIFFS_FEED_ENDED = 1,      /* forcing ended with freeze set (cliffs_main.f:305-311) */
+  CLIFFS_ERR_ARG = -1,        /* bad argument or grid description */
+  CLIFFS_ERR_CUDA = -2,       /* CUDA runtime error */
+  CLIFFS_ERR_NAN = -3,        /* a non-finite eta/u/v appeared */
+  CLIFFS_ERR_NOMEM = -4,      /* device allocation failed */
+  CLIFFS_ERR_STATE = -5,      /* call out of order (e.g. no state uploaded) */
+  CLIFFS_ERR_DEVICE = -6      /* no usable sm_103 device */
+};
+
+/* status bits reported by cliffs_gpu_status() */
+enum {
+  CLIFFS_ST_NAN = 1u          /* a sweep produced a non-finite value */
+};
+
+typedef struct cliffs_ctx cliffs_ctx;
+
+/* Grid and physical parameters of one Cliffs grid (modules MASTER and
+ * PARAMETERS, global_modules.f:16-55, as filled by allabout.f and
+ * MasterGrid.f).  x spacing is passed in the separable form MasterGrid.f
+ * builds it: s1(i,j) = row_scale(j) * dx(i). */
+typedef struct cliffs_grid_desc {
+  int32_t nx, ny;          /* nXn, nYn; at least one must exceed 2 */
+  const double *dep;       /* (nx,ny) depth, >0 water, after wall/deformation */
+  const double *dx;        /* (nx-1) x-spacing factor; may be NULL if nx <= 2 */
+  const double *row_scale; /* (ny) cos(lat) factor, NULL for all ones */
+  const double *dy;        /* (ny-1) s2; may be NULL if ny <= 2 */
+  const double *zeta;      /* (ny) metric term or channel width; NULL = 0 */
+  double ground;           /* minimal flow depth (allabout.f:44) */
+  double crough;           /* Manning n**2 (allabout.f:46) */
+  double dt;               /* time step (allabout.f:55) */
+} cliffs_grid_desc;
+
+/* Interpolation tables of one nested child grid, as NestedGrid.f:104-119
+ * builds them with pinpoint (NestedGrid.f:129-148).  Indices 1-based. */
+typedef struct cliffs_nest_desc {
+  int32_t mm, nn;               /* child nXnst, nYnst */
+  int32_t W_nx, E_nx, S_ny, N_ny;
+  double W_cx, E_cx, S_cy, N_cy;
+  const int32_t *WE_ny;         /* (nn) */
+  const double *WE_cy;          /* (nn) */
+  const int32_t *SN_nx;         /* (mm) */
+  const double *SN_cx;          /* (mm) */
+} cliffs_nest_desc;
+
+/* Derived runup measures over the max-wave fields. */
+typedef struct cliffs_runup {
+  double max_runup;      /* max(-dep) over land cells (dep<0) ever wetted */
+  int32_t i, j;          /* 1-based node of max_runup (0 if none) */
+  int64_t wetted_land;   /* land cells ever wetted */
+  int64_t wet_now;       /* cells currently wet */
+} cliffs_runup;
+
+/* MasterGrid.f:237-268 restated: the spacing factors of cliffs_grid_desc from
+ * grid coordinates.  Replaces the s1/s2/zeta computation of MasterGrid; the
+ * optional zeta override of MasterGrid.f:270-273 (channel width) is the
+ * caller's.  Outputs may be NULL when the grid shape does not use them. */
+int cliffs_gpu_metrics(int32_t nx, int32_t ny, int32_t cartesian,
+                       const double *xcrd, const double *ycrd, double *dx,
+                       double *row_scale, double *dy, double *zeta);
+
+/* Allocate device state for one grid (replaces the allocate() calls of
+ * cliffs_main.f:191-197 and 288).  hmax/velmax start at zero and edges at
+ * still water, as in the reference. */
+int cliffs_gpu_create(const cliffs_grid_desc *desc, cliffs_ctx **out);
+void cliffs_gpu_destroy(cliffs_ctx *ctx);
+
+/* Use the caller's cudaStream_t (passed as void*) instead of the context's
+ * own stream.  NULL restores the context stream. */
+int cliffs_gpu_set_stream(cliffs_ctx *ctx, void *stream);
+
+/* Initial state from total depth H = cel after apply_initial_conditions
+ * (before the celerity transform of cliffs_main.f:218-227, which this call
+ * applies) and velocities xvel, yvel (NULL = 0).  Resets hmax/velmax. */
+int cliffs_gpu_set_initial(cliffs_ctx *ctx, const double *H,
+                           const double *xvel, const double *yvel);
+
+/* State in the reference's own form: celerity cel (= sqrt(g*H)), xvel, yvel
+ * (module MASTER).  Upload does not touch hmax/velmax. */
+int cliffs_gpu_upload_state(cliffs_ctx *ctx, const double *cel,
+                            const double *xvel, const double *yvel);
+int cliffs_gpu_download_state(cliffs_ctx *ctx, double *cel, double *xvel,
+                              double *yvel);
+
+/* Boundary forcing (get_boundary_feed.f): nt records at times tinput(nt);
+ * west/east (ny,3,nt) and south/north (nx,3,nt) hold (u, v, eta) per edge
+ * node, either pair may be NULL when that sweep does not run.  irec is the
+ * 1-based start record (get_boundary_feed.f:473-496), freeze the stop flag of
+ * allabout.f:65.  The time-loop cursor of cliffs_main.f:305-315 is kept by the
+ * library.  nt = 0 removes the forcing. */
+int cliffs_gpu_set_feed(cliffs_ctx *ctx, int32_t nt, const double *tinput,
+                        const double *west, const double *east,
+                        const double *south, const double *north,
+                        int32_t irec, int32_t freeze);
+/* First record whose edge elevation reaches cuke (get_boundary_feed.f:473-496);
+ * -1 when the signal stays below it.  Uses the records of cliffs_gpu_set_feed. */
+int cliffs_gpu_feed_start(cliffs_ctx *ctx, double cuke);
+
+/* Advance nsteps time steps (cliffs_main.f:304-355): t += dt, forcing record
+ * and edge interpolation, x-sweep over rows 2..ny-1 (or row 1 in 1-D),
+ * y-sweep over columns 2..nx-1 (or column 1), max-wave update.  *t is the
+ * model time (tinput(irec) at start).  Returns CLIFFS_FEED_ENDED with
+ * *steps_done < nsteps when the forcing ended and freeze is set.  Does not
+ * synchronise the stream. */
+int cliffs_gpu_step(cliffs_ctx *ctx, int32_t nsteps, double *t,
+                    int32_t *steps_done);
+/* One sweep only: the OpenMP loop over call cliffs(iu, j, n) of
+ * cliffs_main.f:325-329 (iu=1) or 340-344 (iu=2), with the edges currently
+ * set; no max-wave update. */
+int cliffs_gpu_sweep(cliffs_ctx *ctx, int32_t iu);
+/* edge1/edge2 of module MASTER, (mx,3) each with mx = max(ny if the x-sweep
+ * runs, nx if the y-sweep runs), as filled by cliffs_main.f:318-339; used by
+ * cliffs_gpu_sweep only.  NULL clears them (still-water open boundary). */
+int cliffs_gpu_set_edges(cliffs_ctx *ctx, const double *edge1,
+                         const double *edge2);
+/* Max-wave update alone (cliffs_main.f:347-355). */
+int cliffs_gpu_maxwave_update(cliffs_ctx *ctx);
+
+/* Output conversions (real*4 like the reference writers):
+ *   maxwave   output_maxwave.f:14-27  (MaxE, MaxV; -1e32 where never wet)
+ *   sea state output_sea_state.f:18-33 (subsampled eta/u/v; -1e32 where dry)
+ * hmax/velmax in the reference's raw form (max celerity, max u^2+v^2). */
+int cliffs_gpu_get_maxwave(cliffs_ctx *ctx, float *maxe, float *maxv);
+int cliffs_gpu_get_max_raw(cliffs_ctx *ctx, double *hmax, double *velmax);
+int cliffs_gpu_get_sea_state(cliffs_ctx *ctx, int32_t lonsub, int32_t latsub,
+                             float *hsub, float *usub, float *vsub);
+/* output_gages.f:18-29: eta (-1e32 where dry), u, v at 1-based (I,J). */
+int cliffs_gpu_get_gauges(cliffs_ctx *ctx, int32_t n, const int32_t *I,
+                          const int32_t *J, double *eta, double *u, double *v);
+/* Runup measures from the max-wave fields (no reference counterpart). */
+int cliffs_gpu_runup(cliffs_ctx *ctx, cliffs_runup *out);
+
+/* Nested-grid feed (feed_children_grid.f:10-179).  nest_add copies the
+ * child's tables to the device and returns its id. */
+int cliffs_gpu_nest_add(cliffs_ctx *ctx, const cliffs_nest_desc *nest,
+                        int32_t *id);
+/* Arrival test and, once arrived, the (u, v, eta) records of the child's
+ * west/east (nn,3) and south/north (mm,3) edges.  *arrived is the sticky
+ * iarv flag (in/out).  Returns 1 when records were produced, 0 before
+ * arrival. */
+int cliffs_gpu_feed_child(cliffs_ctx *ctx, int32_t id, double cuke,
+                          int32_t *arrived, double *uvq_w, double *uvq_e,
+                          double *uvq_s, double *uvq_n);
+
+/* Sticky status bits (CLIFFS_ST_*) since the last call; synchronises. */
+int cliffs_gpu_status(cliffs_ctx *ctx, uint32_t *flags);
+/* Block until queued work on the context's stream is done. */
+int cliffs_gpu_sync(cliffs_ctx *ctx);
+
+/* Kernel timing: when enabled, step() brackets every sweep launch with CUDA
+ * events; read returns the mean duration (ms) of x- and y-sweep launches and
+ * their counts since the last reset. */
+int cliffs_gpu_profile(cliffs_ctx *ctx, int32_t enable);
+int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
+                            double *y_ms, int64_t *y_count);
+
+/* Tuning: line segment length (cells per warp work item) of each sweep;
+ * multiples of 32.  0 keeps the current value. */
+int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t seg_x, int32_t seg_y);
+
+const char *cliffs_gpu_strerror(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

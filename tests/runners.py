@@ -1,0 +1,53 @@
+"""Shared helpers: run one case on the GPU library and on the oracle, compare."""
+import importlib
+
+import numpy as np
+
+import oracle
+
+pkg = importlib.import_module("cliffs-src_gb300")
+GRAV = oracle.GRAV
+
+
+def oracle_model(case):
+    s1, s2, zeta = oracle.metrics(case["xcrd"], case["ycrd"], case["cartesian"])
+    if case.get("zeta") is not None:
+        zeta = case["zeta"]
+    return oracle.Model(case["dep"], s1, s2, zeta, ground=case["ground"], crough=case["crough"],
+                        dt=case["dt"], cel=case["H0"], xvel=case.get("u0"), yvel=case.get("v0"),
+                        t0=case.get("t0", 0.0))
+
+
+def gpu_grid(case):
+    return pkg.GpuGrid.from_case(case)
+
+
+def compare_state(m, cel, u, v, scale):
+    """Differences between oracle model m and a GPU state (cel, u, v).
+
+    Returns a dict: wet/dry mismatch count and the max |difference| of eta, u,
+    v over cells wet in both, eta relative to `scale`.
+    """
+    wo = m.cel > m.celmin
+    wg = cel > m.celmin
+    both = wo & wg
+    eo = m.cel ** 2 / GRAV - m.dep
+    eg = cel * np.abs(cel) / GRAV - m.dep
+    res = dict(mismatch=int((wo != wg).sum()), wet=int(wo.sum()))
+    if both.any():
+        res["eta"] = float(np.abs(eo - eg)[both].max() / scale)
+        res["u"] = float(np.abs(m.xvel - u)[both].max())
+        res["v"] = float(np.abs(m.yvel - v)[both].max())
+    else:
+        res["eta"] = res["u"] = res["v"] = 0.0
+    return res
+
+
+def compare_maxwave(mo, vo, mg, vg, scale):
+    so = mo > -1e30
+    sg = mg > -1e30
+    both = so & sg
+    r = dict(mismatch=int((so != sg).sum()))
+    r["maxe"] = float(np.abs(mo - mg)[both].max() / scale) if both.any() else 0.0
+    r["maxv"] = float(np.abs(vo - vg)[both].max()) if both.any() else 0.0
+    return r
