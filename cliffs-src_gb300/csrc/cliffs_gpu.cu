@@ -1,6 +1,8 @@
 // cliffs_gpu.cu -- C ABI implementation (include/cliffs_gpu.h) and the
 // auxiliary kernels: state conversion, wetness bitmaps, output conversions,
 // gauges, runup, nested-grid feed.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -75,6 +77,12 @@ struct cliffs_ctx {
   int* d_flag = nullptr;
   bool have_state = false;
   int seg_x = 64, seg_y = 64;
+  // TMA descriptors: [0] dep, [1..2] eta, [3..4] xvel, [5..6] yvel,
+  // [7] hmax, [8] velmax; boxes of 8 cells x 32 rows (x-sweep) and 32 columns
+  // x 8 rows (y-sweep)
+  CUtensorMap tmx[9], tmy[9];
+  bool geo_uni_x = false, geo_uni_y = false;
+  float4 geo0_x = {0, 0, 0, 0}, geo0_y = {0, 0, 0, 0};
   bool prof = false;
   std::vector<ProfPair> prof_pending;
   double prof_ms[2] = {0, 0};
@@ -364,6 +372,32 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
   }
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encoder() {
+  if (g_encode) return CLIFFS_OK;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return CLIFFS_ERR_CUDA;
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return CLIFFS_OK;
+}
+
+// 2-D FP32 map over an (nx, ny) field with a row pitch of `pitch` floats.
+int make_map(CUtensorMap* m, float* base, int nx, int ny, int pitch, int bx, int by) {
+  cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+}
+
 int check_device(int* dev) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CLIFFS_ERR_DEVICE;
@@ -381,6 +415,7 @@ Phys<float> phys(const cliffs_ctx* c) {
   p.ground = (float)c->ground;
   p.celmin = (float)c->celmin;
   p.dt = (float)c->dt;
+  p.idt = (float)(1.0 / c->dt);
   p.gcrough = (float)(kGrav * c->crough);
   p.sqr2 = (float)kSqr2;
   return p;
@@ -404,10 +439,16 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   SweepParams P{};
   const int s = c->cur, o = 1 - c->cur;
   P.pitch = c->pitch;
-  P.dep = c->dep;
-  P.eta_in = c->eta[s];
-  P.xu_in = c->xu[s];
-  P.yv_in = c->yv[s];
+  const CUtensorMap* tm = iu == 1 ? c->tmx : c->tmy;
+  P.tm_in[0] = tm[0];
+  P.tm_in[1] = tm[1 + s];
+  P.tm_in[2] = tm[3 + s];
+  P.tm_in[3] = tm[5 + s];
+  P.tm_in[4] = tm[7];
+  P.tm_in[5] = tm[8];
+  P.tm_out[0] = c->tmx[1 + o];
+  P.tm_out[1] = c->tmx[3 + o];
+  P.tm_out[2] = c->tmx[5 + o];
   P.eta_out = c->eta[o];
   P.xu_out = c->xu[o];
   P.yv_out = c->yv[o];
@@ -435,6 +476,8 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     P.bm_in = c->bm_rows[c->cur_r];
     P.ld_in = c->ldr;
     P.geo = c->geo_x;
+    P.geo_uniform = c->geo_uni_x;
+    P.geo0 = c->geo0_x;
     P.scl = nullptr;
     P.lscale = c->lscale;
     P.inv_dx1 = c->inv_dx1_x;
@@ -461,6 +504,8 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     P.bm_in = c->bm_cols[c->cur_c];
     P.ld_in = c->ldc;
     P.geo = c->geo_y;
+    P.geo_uniform = c->geo_uni_y;
+    P.geo0 = c->geo0_y;
     P.scl = c->scl_y;
     P.lscale = nullptr;
     P.inv_dx1 = c->inv_dx1_y;
@@ -479,7 +524,7 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   const int nlb = (P.nlines + 31) / 32;
   const int nseg = (P.n + P.seg - 1) / P.seg;
   const int warps = nlb * nseg;
-  const int blocks = (warps + 3) / 4;
+  const int blocks = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
   ProfPair pp{};
   if (c->prof) {
     CK(cudaEventCreate(&pp.a));
@@ -488,9 +533,9 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     CK(cudaEventRecord(pp.a, c->stream));
   }
   if (iu == 1)
-    sweep_kernel<0><<<blocks, 128, 0, c->stream>>>(P);
+    sweep_kernel<0><<<blocks, 32 * kWarpsPerCta, kWarpsPerCta * warp_smem_bytes<0>(), c->stream>>>(P);
   else
-    sweep_kernel<1><<<blocks, 128, 0, c->stream>>>(P);
+    sweep_kernel<1><<<blocks, 32 * kWarpsPerCta, kWarpsPerCta * warp_smem_bytes<1>(), c->stream>>>(P);
   CK(cudaGetLastError());
   if (c->prof) {
     CK(cudaEventRecord(pp.b, c->stream));
@@ -651,9 +696,24 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   else gx.assign((size_t)c->nx, make_float4(0, 0, 0, 0));
   if (c->yrun) build_geo(c->ny, d->dy, gy, c->inv_dx1_y, c->inv_dxn1_y);
   else gy.assign((size_t)c->ny, make_float4(0, 0, 0, 0));
+  auto uniform = [](const std::vector<float4>& g, int n, float4& g0) {
+    if (n < 3) return false;
+    g0 = g[1];
+    for (int m = 2; m <= n - 1; ++m) {
+      const float4& a = g[m - 1];
+      if (a.x != g0.x || a.y != g0.y || a.z != g0.z || a.w != g0.w) return false;
+    }
+    return true;
+  };
+  if (c->xrun) c->geo_uni_x = uniform(gx, c->nx, c->geo0_x);
+  if (c->yrun) c->geo_uni_y = uniform(gy, c->ny, c->geo0_y);
   std::vector<float> sy((size_t)c->ny, 0.f);
+  bool zeta_nonzero = false;
   if (d->zeta)
-    for (int j = 0; j < c->ny; ++j) sy[j] = (float)d->zeta[j];
+    for (int j = 0; j < c->ny; ++j) {
+      sy[j] = (float)d->zeta[j];
+      zeta_nonzero |= sy[j] != 0.f;
+    }
   std::vector<float2> ls((size_t)c->ny, make_float2(1.f, 1.f));
   if (d->row_scale)
     for (int j = 0; j < c->ny; ++j) ls[j] = make_float2((float)d->row_scale[j], (float)(1.0 / d->row_scale[j]));
@@ -663,11 +723,25 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       cudaMemcpy(c->lscale, ls.data(), ls.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(c->status, 0, sizeof(unsigned)) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
+  if (get_encoder()) return fail(CLIFFS_ERR_CUDA);
+  {
+    float* f[9] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1], c->hmax, c->velmax};
+    for (int k = 0; k < 9; ++k) {
+      if (make_map(&c->tmx[k], f[k], c->nx, c->ny, c->pitch, kChunk, 32) ||
+          make_map(&c->tmy[k], f[k], c->nx, c->ny, c->pitch, 32, kChunk))
+        return fail(CLIFFS_ERR_CUDA);
+    }
+  }
+  if (cudaFuncSetAttribute(sweep_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerCta * warp_smem_bytes<0>()) != cudaSuccess ||
+      cudaFuncSetAttribute(sweep_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kWarpsPerCta * warp_smem_bytes<1>()) != cudaSuccess)
+    return fail(CLIFFS_ERR_CUDA);
   if (!d->row_scale) {
     cudaFree(c->lscale);
     c->lscale = nullptr;
   }
-  if (!d->zeta) {
+  if (!zeta_nonzero) {
     cudaFree(c->scl_y);
     c->scl_y = nullptr;
   }

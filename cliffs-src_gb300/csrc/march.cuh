@@ -45,6 +45,37 @@ CL_HD R csqrt(R x) {
 #endif
 }
 
+// sqrt(x) for x > 0 where ~1 ulp is enough (celerity and friction
+// coefficients; the state itself is carried in eta): one MUFU op on the GPU.
+CL_HD float fsqrt_pos(float x) {
+#ifdef __CUDA_ARCH__
+  return x * rsqrtf(x);
+#else
+  return std::sqrt(x);
+#endif
+}
+CL_HD double fsqrt_pos(double x) { return csqrt(x); }
+
+// sqrt(x) for x >= 0 (0 maps to 0).
+CL_HD float fsqrt0(float x) {
+#ifdef __CUDA_ARCH__
+  return x * rsqrtf(fmaxf(x, 1e-30f));
+#else
+  return std::sqrt(x);
+#endif
+}
+CL_HD double fsqrt0(double x) { return csqrt(x); }
+
+// 1/sqrt(x), x > 0
+CL_HD float frsqrt(float x) {
+#ifdef __CUDA_ARCH__
+  return rsqrtf(x);
+#else
+  return 1.0f / std::sqrt(x);
+#endif
+}
+CL_HD double frsqrt(double x) { return 1.0 / csqrt(x); }
+
 // Physical constants of one sweep (module PARAMETERS, global_modules.f:46-55).
 template <typename R>
 struct Phys {
@@ -53,6 +84,7 @@ struct Phys {
   R ground;   // minimal flow depth
   R celmin;   // sqrt(g*ground)
   R dt;
+  R idt;      // 1/dt
   R gcrough;  // g*crough
   R sqr2;     // (double)1.41421356f
 };
@@ -189,7 +221,7 @@ struct LineMarch {
         B.vf = A.v;
         B.fl |= F_EW;
       } else if (!(B.fl & F_LAND)) {
-        B.c = csqrt(p.g * B.H);
+        B.c = fsqrt_pos(p.g * B.H);
         B.ef = B.eta;
         B.uf = B.u;
         B.vf = B.v;
@@ -234,7 +266,8 @@ struct LineMarch {
       const R Hj = (C.fl & F_LAND) ? p.ground : C.H;  // h^2/g
       R cc = R(0);
       if (p.gcrough != R(0)) {  // "almost Manning" friction (cliffs.f:204)
-        cc = p.gcrough * uj * csqrt((uj * uj + vj * vj) / Hj) / Hj;
+        const R r = frsqrt(Hj);  // sqrt((u^2+v^2)/H)/H = |u,v| / H^1.5
+        cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
       }
       const R sphr = R(8) * cj * uj * geo_m.scl;  // (P-Q)(P+Q)*scl
       const bool water = (dj > p.ground) && (da > p.ground) && (db > p.ground);
@@ -242,7 +275,7 @@ struct LineMarch {
       const bool sonP = water && (ua + ca < R(0)) && (ub + cb > R(0));
       const bool sonQ = water && (ua - ca < R(0)) && (ub - cb > R(0));
       if (sonP || sonQ) sdiff = R(2) * p.g * (csqrt(dj * db) - csqrt(dj * da));
-      const R isum = dtx / p.dt;  // 1/(fm+fp)
+      const R isum = dtx * p.idt;  // 1/(fm+fp)
       // P equation (cliffs.f:223-234)
       R QpP = FPr * inv_fp, QmP = FPl * inv_fm, QsP;
       const R ejP = uj + cj;  // e_j/4
@@ -343,6 +376,77 @@ struct LineMarch {
     }
     (void)o;
     return true;
+  }
+
+  // push() for a stretch where cells k-3..k are all wet (H > ground) and
+  // interior (2 <= k-3, k <= n-1): no flooding, no shoreline ghost, no
+  // limiter, no edge.  Leaves the ring exactly as push() would.
+  CL_HD OutCell<R> push_fast(R d, R eta, R u, R v, const Geo<R>& geo_m) {
+    re = rd;
+    rd = rc;
+    rc = rb;
+    rb = ra;
+    RCell<R>& A = ra;
+    RCell<R>& B = rb;
+    RCell<R>& C = rc;
+    RCell<R>& D = rd;
+    A.d = d;
+    A.eta = eta;
+    A.u = u;
+    A.v = v;
+    A.H = d + eta;
+    A.fl = F_PRESENT;
+    B.c = fsqrt_pos(p.g * B.H);
+    B.ef = B.eta;
+    B.uf = B.u;
+    B.vf = B.v;
+    B.fl = F_PRESENT | F_EW;
+    // interior VTCS-2 update of C with real neighbours D (left), B (right)
+    const R uj = C.uf, cj = C.c, vj = C.vf, dj = C.d;
+    const R ua = D.uf, ca = D.c, da = D.d, va = D.vf;
+    const R ub = B.uf, cb = B.c, db = B.d, vb = B.vf;
+    R FPl, FQl, FPr, FQr;
+    if (fpr_ok) {
+      FPl = fpr_P;
+      FQl = fpr_Q;
+    } else {
+      face_flux(ua, ca, D.ef, uj, cj, C.ef, p, FPl, FQl);
+    }
+    face_flux(uj, cj, C.ef, ub, cb, B.ef, p, FPr, FQr);
+    fpr_ok = true;
+    fpr_P = FPr;
+    fpr_Q = FQr;
+    const R inv_fm = geo_m.inv_fm, inv_fp = geo_m.inv_fp, dtx = geo_m.dtx;
+    R cc = R(0);
+    if (p.gcrough != R(0)) {
+      const R r = frsqrt(C.H);
+      cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
+    }
+    const R sphr = R(8) * cj * uj * geo_m.scl;
+    const R ejP = uj + cj, ejQ = uj - cj;
+    const R QpP = FPr * inv_fp, QmP = FPl * inv_fm;
+    const R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm;
+    R QsP = R(0.5) * (QpP + QmP);
+    R QsQ = R(0.5) * (QpQ + QmQ);
+    const bool sonP = (ua + ca < R(0)) && (ub + cb > R(0));
+    const bool sonQ = (ua - ca < R(0)) && (ub - cb > R(0));
+    if ((sonP || sonQ) && (dj > p.ground) && (da > p.ground) && (db > p.ground)) {
+      const R isum = dtx * p.idt;
+      const R sdiff = R(2) * p.g * (csqrt(dj * db) - csqrt(dj * da));
+      if (sonP) QsP = (ejP * ((ub - ua) + R(2) * (cb - ca)) - sdiff) * isum;
+      if (sonQ) QsQ = (ejQ * ((ub - ua) - R(2) * (cb - ca)) - sdiff) * isum;
+    }
+    QsP = QsP + ejP * dtx * (QmP - QpP);
+    QsQ = QsQ + ejQ * dtx * (QmQ - QpQ);
+    const R dP = -p.dt * (QsP + cc - sphr);
+    const R dQ = -p.dt * (QsQ + cc + sphr);
+    const R Qv = (vb - vj) * inv_fp - (vj - va) * inv_fm;
+    C.vn = vj - uj * dtx * ((vb - va) - Qv * (uj * p.dt + geo_m.dfpm));
+    const R dc = R(0.25) * (dP - dQ);
+    C.cn = cj + dc;
+    C.un = uj + R(0.5) * (dP + dQ);
+    C.en = eta_step(cj, C.ef, dc, dj, p);
+    return OutCell<R>{D.en, D.un, D.vn};
   }
 };
 

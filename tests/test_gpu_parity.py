@@ -13,7 +13,7 @@ import pytest
 
 import oracle
 from tests.lines import random_grid, random_spacing
-from tests.runners import GRAV, compare_maxwave, compare_state, gpu_grid, oracle_model
+from tests.runners import GRAV, compare_maxwave, compare_state, gpu_grid, maxwave_ties, oracle_model
 
 pytestmark = pytest.mark.gpu
 pkg = importlib.import_module("cliffs-src_gb300")
@@ -52,8 +52,7 @@ def test_single_sweep_adversarial_lines(iu, n):
     g.sweep(iu)
     cel, u, v = g.download_state()
     r = compare_state(m, cel, u, v, 1.0)
-    cells = m.cel.size
-    assert r["mismatch"] <= max(2, cells // 2000), r
+    assert r["mismatch"] <= 2, r
     assert r["eta"] <= 2e-5, r          # m, values up to ~2 m
     wet = (m.cel > m.celmin) & (cel > m.celmin)
     du = np.abs(m.xvel - u)[wet]
@@ -64,17 +63,16 @@ def test_single_sweep_adversarial_lines(iu, n):
 
 
 def test_fully_dry_lines_untouched():
+    """cliffs.f:113: a line without a wet cell is left exactly as it was."""
     rng = np.random.default_rng(9)
     m, g = _line_models(rng, 40, 64, 1)
-    # make every line dry but with residual state
-    cel = np.full_like(m.cel, 0.5 * m.celmin)
-    m.cel[...] = cel
+    cel = np.full_like(m.cel, 0.5 * m.celmin)  # dry, with residual celerity
     g.upload_state(cel, m.xvel, m.yvel)
-    m.sweep(1)
+    before = g.download_state()
     g.sweep(1)
-    c2, u2, v2 = g.download_state()
-    assert np.allclose(c2, m.cel, rtol=1e-6, atol=1e-7)
-    assert np.allclose(u2, m.xvel, rtol=1e-6, atol=1e-7)
+    after = g.download_state()
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
     g.close()
 
 
@@ -95,7 +93,7 @@ def test_channel_1d_runup():
         assert r["u"] <= 2e-4, (blk, r)
     mo, vo = m.maxwave()
     mg, vg = g.maxwave()
-    rm = compare_maxwave(mo, vo, mg, vg, A)
+    rm = compare_maxwave(mo, vo, mg, vg, A, maxwave_ties(m))
     assert rm["mismatch"] <= 2 and rm["maxe"] <= 1e-4, rm
     # runup: highest land elevation reached
     ro = g.runup()
@@ -130,7 +128,7 @@ def test_shelf_2d(nx, ny, steps):
     assert r["u"] <= 2e-4 and r["v"] <= 2e-4, r
     mo, vo = m.maxwave()
     mg, vg = g.maxwave()
-    rm = compare_maxwave(mo, vo, mg, vg, A)
+    rm = compare_maxwave(mo, vo, mg, vg, A, maxwave_ties(m))
     assert rm["mismatch"] <= nx * ny // 20000 + 2 and rm["maxe"] <= 1e-4, rm
     # screenshots (output_sea_state.f)
     ho, uo, _ = m.sea_state(3, 2)
