@@ -239,9 +239,9 @@ def run_ours(args):
     peak, peak_kind = _peaks()
     kx, ky = prof["x_ms"], prof["y_ms"]
     if ky >= kx:
-        kname, kms, bpc = "sweep_kernel<1> (y-sweep + max-wave)", ky, B_Y
+        kname, kms, bpc = "y-sweep + max-wave (fast_kernel<1> + general_kernel<1>)", ky, B_Y
     else:
-        kname, kms, bpc = "sweep_kernel<0> (x-sweep)", kx, B_X
+        kname, kms, bpc = "x-sweep (fast_kernel<0> + general_kernel<0>)", kx, B_X
     achieved = bpc * cells / (kms / 1e3) / 1e9 if kms > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
@@ -266,7 +266,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": config_dict(case, "CUDA sm_103a, include/cliffs_gpu.h"),
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
-                "gpu_launches": int(prof["x_n"] + prof["y_n"]),
+                "gpu_launches": int(2 * (prof["x_n"] + prof["y_n"])),
                 "hbm_frac_step": round(B_STEP * cells * args.steps / (ms / 1e3) / 1e9 / peak, 4)}
         print(json.dumps(line), flush=True)
     if dist is not None:

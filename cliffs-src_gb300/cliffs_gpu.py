@@ -335,5 +335,5 @@ class GpuGrid:
                                             ctypes.byref(ym), ctypes.byref(yn)), "profile_read")
         return dict(x_ms=xm.value, x_n=xn.value, y_ms=ym.value, y_n=yn.value)
 
-    def set_tiling(self, seg_x=0, seg_y=0):
-        _chk(self.L.cliffs_gpu_set_tiling(self.h, int(seg_x), int(seg_y)), "set_tiling")
+    def set_tiling(self, block_x=0, warps_y=0):
+        _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")

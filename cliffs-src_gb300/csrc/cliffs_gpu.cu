@@ -1,8 +1,6 @@
 // cliffs_gpu.cu -- C ABI implementation (include/cliffs_gpu.h) and the
 // auxiliary kernels: state conversion, wetness bitmaps, output conversions,
 // gauges, runup, nested-grid feed.
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -11,7 +9,7 @@
 #include <vector>
 
 #include "../../include/cliffs_gpu.h"
-#include "kernels.cuh"
+#include "sweep.cuh"
 
 using namespace cliffs;
 
@@ -53,10 +51,10 @@ struct cliffs_ctx {
   float *eta[2] = {nullptr, nullptr}, *xu[2] = {nullptr, nullptr}, *yv[2] = {nullptr, nullptr};
   float *hmax = nullptr, *velmax = nullptr;
   int cur = 0;
-  uint32_t *bm_rows[2] = {nullptr, nullptr}, *bm_cols[2] = {nullptr, nullptr};
-  int cur_r = 0, cur_c = 0;
-  bool rows_valid = false, cols_valid = false;
-  int ldr = 0, ldc = 0;
+  // worklist of cells for the general kernel and one counter per sweep parity
+  uint32_t* list = nullptr;
+  uint32_t* cnt = nullptr;
+  unsigned sweeps = 0;
   float4 *geo_x = nullptr, *geo_y = nullptr;
   float* scl_y = nullptr;
   float2* lscale = nullptr;
@@ -76,11 +74,7 @@ struct cliffs_ctx {
   std::vector<Nest> nests;
   int* d_flag = nullptr;
   bool have_state = false;
-  int seg_x = 64, seg_y = 64;
-  // TMA descriptors: [0] dep, [1..2] eta, [3..4] xvel, [5..6] yvel,
-  // [7] hmax, [8] velmax; boxes of 8 cells x 32 rows (x-sweep) and 32 columns
-  // x 8 rows (y-sweep)
-  CUtensorMap tmx[9], tmy[9];
+  int blk_x = 128, warps_y = 8;  // fast-kernel block shapes (cliffs_gpu_set_tiling)
   bool geo_uni_x = false, geo_uni_y = false;
   float4 geo0_x = {0, 0, 0, 0}, geo0_y = {0, 0, 0, 0};
   bool prof = false;
@@ -135,31 +129,6 @@ __global__ void k_reset_max(int nx, int ny, int pitch, const float* __restrict__
   const size_t q = (size_t)j * pitch + i;
   hmax[q] = i < nx ? -dep[q] : 0.f;  // hmax = 0 in celerity form
   velmax[q] = 0.f;
-}
-
-// Both wetness bitmaps from the current state; one warp per 32x32 tile.
-__global__ void k_bitmaps(int nx, int ny, int pitch, const float* __restrict__ dep,
-                          const float* __restrict__ eta, float ground, uint32_t* rows, int ldr,
-                          uint32_t* cols, int ldc) {
-  const int lane = threadIdx.x & 31;
-  const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int tcx = (nx + 31) >> 5, tcy = (ny + 31) >> 5;
-  if (tile >= tcx * tcy) return;
-  const int bx = tile % tcx, by = tile / tcx;
-  const int i = (bx << 5) + lane;
-  uint32_t colbits = 0;
-  for (int r = 0; r < 32; ++r) {
-    const int j = (by << 5) + r;
-    bool w = false;
-    if (j < ny && i < nx) {
-      const size_t q = (size_t)j * pitch + i;
-      w = dep[q] + eta[q] > ground;
-    }
-    const unsigned b = __ballot_sync(0xffffffffu, w);
-    if (lane == 0 && j < ny) rows[(size_t)j * ldr + bx] = b;
-    colbits |= (w ? 1u : 0u) << r;
-  }
-  if (i < nx) cols[(size_t)i * ldc + by] = colbits;
 }
 
 __global__ void k_download(int nx, int ny, int pitch, const float* __restrict__ dep,
@@ -372,32 +341,6 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-
-int get_encoder() {
-  if (g_encode) return CLIFFS_OK;
-  cudaDriverEntryPointQueryResult q;
-  void* fn = nullptr;
-  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-          cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !fn)
-    return CLIFFS_ERR_CUDA;
-  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-  return CLIFFS_OK;
-}
-
-// 2-D FP32 map over an (nx, ny) field with a row pitch of `pitch` floats.
-int make_map(CUtensorMap* m, float* base, int nx, int ny, int pitch, int bx, int by) {
-  cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
-  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
-  cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? CLIFFS_OK : CLIFFS_ERR_CUDA;
-}
-
 int check_device(int* dev) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CLIFFS_ERR_DEVICE;
@@ -423,108 +366,59 @@ Phys<float> phys(const cliffs_ctx* c) {
 
 dim3 grid2(int nx, int ny, int bx = 128) { return dim3((nx + bx - 1) / bx, ny); }
 
-int refresh_bitmaps(cliffs_ctx* c) {
-  const int tiles = ((c->nx + 31) / 32) * ((c->ny + 31) / 32);
-  k_bitmaps<<<(tiles + 3) / 4, 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur],
-                                                    (float)c->ground, c->bm_rows[c->cur_r], c->ldr,
-                                                    c->bm_cols[c->cur_c], c->ldc);
-  CK(cudaGetLastError());
-  c->rows_valid = c->cols_valid = true;
-  return CLIFFS_OK;
-}
+constexpr int kGeneralBlocks = 304;
 
-// Launch one sweep.  fuse_max: update hmax/velmax on the way out.
+// Launch one sweep: the fast kernel, then the general kernel over the cells it
+// listed.  fuse_max: update hmax/velmax on the way out.
 int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
                  int flen, int irec, double cc) {
-  SweepParams P{};
+  SweepArgs A{};
   const int s = c->cur, o = 1 - c->cur;
-  P.pitch = c->pitch;
-  const CUtensorMap* tm = iu == 1 ? c->tmx : c->tmy;
-  P.tm_in[0] = tm[0];
-  P.tm_in[1] = tm[1 + s];
-  P.tm_in[2] = tm[3 + s];
-  P.tm_in[3] = tm[5 + s];
-  P.tm_in[4] = tm[7];
-  P.tm_in[5] = tm[8];
-  P.tm_out[0] = c->tmx[1 + o];
-  P.tm_out[1] = c->tmx[3 + o];
-  P.tm_out[2] = c->tmx[5 + o];
-  P.eta_out = c->eta[o];
-  P.xu_out = c->xu[o];
-  P.yv_out = c->yv[o];
-  P.hmax = fuse_max ? c->hmax : nullptr;
-  P.velmax = fuse_max ? c->velmax : nullptr;
-  P.ph = phys(c);
-  P.status = c->status;
-  P.feedA = fA;
-  P.feedB = fB;
-  P.feed_len = flen;
-  P.irec = irec;
-  P.cc = cc;
-  // which sweep follows decides the bitmap layout this one writes
-  const bool next_is_x = (iu == 1) ? !c->yrun : true;
+  A.pitch = c->pitch;
+  A.dep = c->dep;
+  A.eta = c->eta[s];
+  A.xu = c->xu[s];
+  A.yv = c->yv[s];
+  A.eta_o = c->eta[o];
+  A.xu_o = c->xu[o];
+  A.yv_o = c->yv[o];
+  A.hmax = fuse_max ? c->hmax : nullptr;
+  A.velmax = fuse_max ? c->velmax : nullptr;
+  A.ph = phys(c);
+  A.status = c->status;
+  A.feedA = fA;
+  A.feedB = fB;
+  A.feed_len = flen;
+  A.irec = irec;
+  A.cc = cc;
+  A.list = c->list;
+  A.count = c->cnt + (c->sweeps & 1u);
+  A.count_next = c->cnt + ((c->sweeps + 1u) & 1u);
   if (iu == 1) {
-    if (!c->rows_valid) {
-      int r = refresh_bitmaps(c);
-      if (r) return r;
-    }
-    P.n = c->nx;
-    P.nlines = c->ny;
-    P.lo = c->jj1;
-    P.hi = c->jj2;
-    P.seg = c->seg_x;
-    P.bm_in = c->bm_rows[c->cur_r];
-    P.ld_in = c->ldr;
-    P.geo = c->geo_x;
-    P.geo_uniform = c->geo_uni_x;
-    P.geo0 = c->geo0_x;
-    P.scl = nullptr;
-    P.lscale = c->lscale;
-    P.inv_dx1 = c->inv_dx1_x;
-    P.inv_dxn1 = c->inv_dxn1_x;
-    if (next_is_x) {  // 1-D along x: the next sweep reads rows again
-      P.bm_mode = 1;
-      P.bm_out = c->bm_rows[1 - c->cur_r];
-      P.ld_out = c->ldr;
-    } else {
-      P.bm_mode = 0;
-      P.bm_out = c->bm_cols[c->cur_c];
-      P.ld_out = c->ldc;
-    }
+    A.n = c->nx;
+    A.nlines = c->ny;
+    A.lo = c->jj1;
+    A.hi = c->jj2;
+    A.geo = c->geo_x;
+    A.geo_uniform = c->geo_uni_x;
+    A.geo0 = c->geo0_x;
+    A.scl = nullptr;
+    A.lscale = c->lscale;
+    A.inv_dx1 = c->inv_dx1_x;
+    A.inv_dxn1 = c->inv_dxn1_x;
   } else {
-    if (!c->cols_valid) {
-      int r = refresh_bitmaps(c);
-      if (r) return r;
-    }
-    P.n = c->ny;
-    P.nlines = c->nx;
-    P.lo = c->ii1;
-    P.hi = c->ii2;
-    P.seg = c->seg_y;
-    P.bm_in = c->bm_cols[c->cur_c];
-    P.ld_in = c->ldc;
-    P.geo = c->geo_y;
-    P.geo_uniform = c->geo_uni_y;
-    P.geo0 = c->geo0_y;
-    P.scl = c->scl_y;
-    P.lscale = nullptr;
-    P.inv_dx1 = c->inv_dx1_y;
-    P.inv_dxn1 = c->inv_dxn1_y;
-    const bool next_y = !c->xrun;
-    if (next_y) {
-      P.bm_mode = 1;
-      P.bm_out = c->bm_cols[1 - c->cur_c];
-      P.ld_out = c->ldc;
-    } else {
-      P.bm_mode = 0;
-      P.bm_out = c->bm_rows[c->cur_r];
-      P.ld_out = c->ldr;
-    }
+    A.n = c->ny;
+    A.nlines = c->nx;
+    A.lo = c->ii1;
+    A.hi = c->ii2;
+    A.geo = c->geo_y;
+    A.geo_uniform = c->geo_uni_y;
+    A.geo0 = c->geo0_y;
+    A.scl = c->scl_y;
+    A.lscale = nullptr;
+    A.inv_dx1 = c->inv_dx1_y;
+    A.inv_dxn1 = c->inv_dxn1_y;
   }
-  const int nlb = (P.nlines + 31) / 32;
-  const int nseg = (P.n + P.seg - 1) / P.seg;
-  const int warps = nlb * nseg;
-  const int blocks = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
   ProfPair pp{};
   if (c->prof) {
     CK(cudaEventCreate(&pp.a));
@@ -532,36 +426,26 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     pp.dir = iu - 1;
     CK(cudaEventRecord(pp.a, c->stream));
   }
-  if (iu == 1)
-    sweep_kernel<0><<<blocks, 32 * kWarpsPerCta, kWarpsPerCta * warp_smem_bytes<0>(), c->stream>>>(P);
-  else
-    sweep_kernel<1><<<blocks, 32 * kWarpsPerCta, kWarpsPerCta * warp_smem_bytes<1>(), c->stream>>>(P);
+  if (iu == 1) {
+    const int cells = c->blk_x * kCellsPerThread;
+    const dim3 grid((A.n + cells - 1) / cells, A.nlines);
+    fast_kernel<0><<<grid, c->blk_x, 0, c->stream>>>(A);
+    CK(cudaGetLastError());
+    general_kernel<0><<<kGeneralBlocks, 128, 0, c->stream>>>(A);
+  } else {
+    const int rows = c->warps_y * kCellsPerThread;
+    const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
+    fast_kernel<1><<<grid, 32 * c->warps_y, 0, c->stream>>>(A);
+    CK(cudaGetLastError());
+    general_kernel<1><<<kGeneralBlocks, 128, 0, c->stream>>>(A);
+  }
   CK(cudaGetLastError());
   if (c->prof) {
     CK(cudaEventRecord(pp.b, c->stream));
     c->prof_pending.push_back(pp);
   }
   c->cur = o;
-  // bitmap bookkeeping
-  if (iu == 1) {
-    if (P.bm_mode == 1) {
-      c->cur_r = 1 - c->cur_r;
-      c->rows_valid = true;
-      c->cols_valid = false;
-    } else {
-      c->cols_valid = true;
-      c->rows_valid = false;
-    }
-  } else {
-    if (P.bm_mode == 1) {
-      c->cur_c = 1 - c->cur_c;
-      c->cols_valid = true;
-      c->rows_valid = false;
-    } else {
-      c->rows_valid = true;
-      c->cols_valid = false;
-    }
-  }
+  c->sweeps += 1u;
   return CLIFFS_OK;
 }
 
@@ -657,8 +541,6 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   c->ii2 = c->xrun ? d->nx - 1 : 1;
   c->jj1 = c->yrun ? 2 : 1;
   c->jj2 = c->yrun ? d->ny - 1 : 1;
-  c->ldr = (d->nx + 31) / 32;
-  c->ldc = (d->ny + 31) / 32;
   const size_t cells = (size_t)c->pitch * c->ny;
   auto fail = [&](int code) {
     cliffs_gpu_destroy(c);
@@ -669,8 +551,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   if (dalloc(&c->dep, cells) || dalloc(&c->eta[0], cells) || dalloc(&c->eta[1], cells) ||
       dalloc(&c->xu[0], cells) || dalloc(&c->xu[1], cells) || dalloc(&c->yv[0], cells) ||
       dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
-      dalloc(&c->bm_rows[0], (size_t)c->ny * c->ldr) || dalloc(&c->bm_rows[1], (size_t)c->ny * c->ldr) ||
-      dalloc(&c->bm_cols[0], (size_t)c->nx * c->ldc) || dalloc(&c->bm_cols[1], (size_t)c->nx * c->ldc) ||
+      dalloc(&c->list, (size_t)c->nx * c->ny) || dalloc(&c->cnt, 2) ||
       dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
       dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
       dalloc(&c->status, 1) || dalloc(&c->d_flag, 1))
@@ -721,21 +602,8 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       cudaMemcpy(c->geo_y, gy.data(), gy.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->scl_y, sy.data(), sy.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->lscale, ls.data(), ls.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(c->status, 0, sizeof(unsigned)) != cudaSuccess)
-    return fail(CLIFFS_ERR_CUDA);
-  if (get_encoder()) return fail(CLIFFS_ERR_CUDA);
-  {
-    float* f[9] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1], c->hmax, c->velmax};
-    for (int k = 0; k < 9; ++k) {
-      if (make_map(&c->tmx[k], f[k], c->nx, c->ny, c->pitch, kChunk, 32) ||
-          make_map(&c->tmy[k], f[k], c->nx, c->ny, c->pitch, 32, kChunk))
-        return fail(CLIFFS_ERR_CUDA);
-    }
-  }
-  if (cudaFuncSetAttribute(sweep_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kWarpsPerCta * warp_smem_bytes<0>()) != cudaSuccess ||
-      cudaFuncSetAttribute(sweep_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           kWarpsPerCta * warp_smem_bytes<1>()) != cudaSuccess)
+      cudaMemset(c->status, 0, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(c->cnt, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
   if (!d->row_scale) {
     cudaFree(c->lscale);
@@ -754,7 +622,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   cudaStreamSynchronize(c->stream);
   flush_profile(c);
   void* ptrs[] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
-                  c->hmax, c->velmax, c->bm_rows[0], c->bm_rows[1], c->bm_cols[0], c->bm_cols[1],
+                  c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
                   c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag};
   for (void* p : ptrs)
@@ -796,7 +664,6 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
     k_reset_max<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
-  if (!r) r = refresh_bitmaps(c);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   cudaFree(dsrc);
   if (dx) cudaFree(dx);
@@ -1240,10 +1107,10 @@ int cliffs_gpu_profile_read(cliffs_ctx* c, double* x_ms, int64_t* x_n, double* y
   return CLIFFS_OK;
 }
 
-int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t seg_x, int32_t seg_y) {
-  if (!c || seg_x < 0 || seg_y < 0 || seg_x % 32 || seg_y % 32) return CLIFFS_ERR_ARG;
-  if (seg_x) c->seg_x = seg_x;
-  if (seg_y) c->seg_y = seg_y;
+int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t block_x, int32_t warps_y) {
+  if (!c || block_x < 0 || warps_y < 0 || block_x % 32 || block_x > 256 || warps_y > 8) return CLIFFS_ERR_ARG;
+  if (block_x) c->blk_x = block_x;
+  if (warps_y) c->warps_y = warps_y;
   return CLIFFS_OK;
 }
 

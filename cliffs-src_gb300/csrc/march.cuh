@@ -152,6 +152,55 @@ CL_HD R eta_step(R c0, R e0, R dc, R d, const Phys<R>& p) {
   return eta_from_c(c1, d, p);
 }
 
+// State of one cell as the interior update sees it (after flooding).
+template <typename R>
+struct CellState {
+  R u, c, e, d, v, H;  // normal velocity, celerity, eta, depth, tangential, H
+};
+
+struct NoFlux {};
+
+// VTCS-2 interior update of cell j between real neighbours a (left) and b
+// (right), cliffs.f:200-262, in the eta form.  FPl/FQl, FPr/FQr are the face
+// fluxes (a,j) and (j,b).  Returns the new (eta, u, v); *cn gets the new
+// celerity.
+template <typename R>
+CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, const CellState<R>& b,
+                                 R FPl, R FQl, R FPr, R FQr, const Geo<R>& geo, const Phys<R>& p,
+                                 R* cn_out) {
+  const R uj = j.u, cj = j.c, vj = j.v, dj = j.d;
+  const R inv_fm = geo.inv_fm, inv_fp = geo.inv_fp, dtx = geo.dtx;
+  const R r = frsqrt(j.H);  // sqrt((u^2+v^2)/H)/H = |u,v| / H^1.5 (cliffs.f:204)
+  const R cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
+  const R sphr = R(8) * cj * uj * geo.scl;  // (P-Q)(P+Q)*scl
+  const R ejP = uj + cj, ejQ = uj - cj;
+  const R QpP = FPr * inv_fp, QmP = FPl * inv_fm;
+  const R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm;
+  R QsP = R(0.5) * (QpP + QmP);
+  R QsQ = R(0.5) * (QpQ + QmQ);
+  const bool sonP = (a.u + a.c < R(0)) && (b.u + b.c > R(0));
+  const bool sonQ = (a.u - a.c < R(0)) && (b.u - b.c > R(0));
+  if ((sonP || sonQ) && (dj > p.ground) && (a.d > p.ground) && (b.d > p.ground)) {
+    // transcritical point (cliffs.f:228-232, 241-245)
+    const R isum = dtx * p.idt;
+    const R sdiff = R(2) * p.g * (csqrt(dj * b.d) - csqrt(dj * a.d));
+    if (sonP) QsP = (ejP * ((b.u - a.u) + R(2) * (b.c - a.c)) - sdiff) * isum;
+    if (sonQ) QsQ = (ejQ * ((b.u - a.u) - R(2) * (b.c - a.c)) - sdiff) * isum;
+  }
+  QsP = QsP + ejP * dtx * (QmP - QpP);
+  QsQ = QsQ + ejQ * dtx * (QmQ - QpQ);
+  const R dP = -p.dt * (QsP + cc - sphr);
+  const R dQ = -p.dt * (QsQ + cc + sphr);
+  const R Qv = (b.v - vj) * inv_fp - (vj - a.v) * inv_fm;
+  OutCell<R> o;
+  o.v = vj - uj * dtx * ((b.v - a.v) - Qv * (uj * p.dt + geo.dfpm));
+  const R dc = R(0.25) * (dP - dQ);
+  *cn_out = cj + dc;
+  o.u = uj + R(0.5) * (dP + dQ);
+  o.eta = eta_step(cj, j.e, dc, dj, p);
+  return o;
+}
+
 template <typename R>
 struct LineMarch {
   Phys<R> p;
@@ -402,50 +451,24 @@ struct LineMarch {
     B.vf = B.v;
     B.fl = F_PRESENT | F_EW;
     // interior VTCS-2 update of C with real neighbours D (left), B (right)
-    const R uj = C.uf, cj = C.c, vj = C.vf, dj = C.d;
-    const R ua = D.uf, ca = D.c, da = D.d, va = D.vf;
-    const R ub = B.uf, cb = B.c, db = B.d, vb = B.vf;
     R FPl, FQl, FPr, FQr;
     if (fpr_ok) {
       FPl = fpr_P;
       FQl = fpr_Q;
     } else {
-      face_flux(ua, ca, D.ef, uj, cj, C.ef, p, FPl, FQl);
+      face_flux(D.uf, D.c, D.ef, C.uf, C.c, C.ef, p, FPl, FQl);
     }
-    face_flux(uj, cj, C.ef, ub, cb, B.ef, p, FPr, FQr);
+    face_flux(C.uf, C.c, C.ef, B.uf, B.c, B.ef, p, FPr, FQr);
     fpr_ok = true;
     fpr_P = FPr;
     fpr_Q = FQr;
-    const R inv_fm = geo_m.inv_fm, inv_fp = geo_m.inv_fp, dtx = geo_m.dtx;
-    R cc = R(0);
-    if (p.gcrough != R(0)) {
-      const R r = frsqrt(C.H);
-      cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
-    }
-    const R sphr = R(8) * cj * uj * geo_m.scl;
-    const R ejP = uj + cj, ejQ = uj - cj;
-    const R QpP = FPr * inv_fp, QmP = FPl * inv_fm;
-    const R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm;
-    R QsP = R(0.5) * (QpP + QmP);
-    R QsQ = R(0.5) * (QpQ + QmQ);
-    const bool sonP = (ua + ca < R(0)) && (ub + cb > R(0));
-    const bool sonQ = (ua - ca < R(0)) && (ub - cb > R(0));
-    if ((sonP || sonQ) && (dj > p.ground) && (da > p.ground) && (db > p.ground)) {
-      const R isum = dtx * p.idt;
-      const R sdiff = R(2) * p.g * (csqrt(dj * db) - csqrt(dj * da));
-      if (sonP) QsP = (ejP * ((ub - ua) + R(2) * (cb - ca)) - sdiff) * isum;
-      if (sonQ) QsQ = (ejQ * ((ub - ua) - R(2) * (cb - ca)) - sdiff) * isum;
-    }
-    QsP = QsP + ejP * dtx * (QmP - QpP);
-    QsQ = QsQ + ejQ * dtx * (QmQ - QpQ);
-    const R dP = -p.dt * (QsP + cc - sphr);
-    const R dQ = -p.dt * (QsQ + cc + sphr);
-    const R Qv = (vb - vj) * inv_fp - (vj - va) * inv_fm;
-    C.vn = vj - uj * dtx * ((vb - va) - Qv * (uj * p.dt + geo_m.dfpm));
-    const R dc = R(0.25) * (dP - dQ);
-    C.cn = cj + dc;
-    C.un = uj + R(0.5) * (dP + dQ);
-    C.en = eta_step(cj, C.ef, dc, dj, p);
+    const CellState<R> a{D.uf, D.c, D.ef, D.d, D.vf, D.H};
+    const CellState<R> j{C.uf, C.c, C.ef, C.d, C.vf, C.H};
+    const CellState<R> b{B.uf, B.c, B.ef, B.d, B.vf, B.H};
+    const OutCell<R> r = interior_update(a, j, b, FPl, FQl, FPr, FQr, geo_m, p, &C.cn);
+    C.en = r.eta;
+    C.un = r.u;
+    C.vn = r.v;
     return OutCell<R>{D.en, D.un, D.vn};
   }
 };

@@ -177,16 +177,17 @@ int cliffs_gpu_status(cliffs_ctx *ctx, uint32_t *flags);
 /* Block until queued work on the context's stream is done. */
 int cliffs_gpu_sync(cliffs_ctx *ctx);
 
-/* Kernel timing: when enabled, step() brackets every sweep launch with CUDA
- * events; read returns the mean duration (ms) of x- and y-sweep launches and
- * their counts since the last reset. */
+/* Kernel timing: when enabled, step() brackets every sweep (its two kernel
+ * launches) with CUDA events; read returns the mean duration (ms) of x- and
+ * y-sweeps and their counts since the last reset. */
 int cliffs_gpu_profile(cliffs_ctx *ctx, int32_t enable);
 int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
                             double *y_ms, int64_t *y_count);
 
-/* Tuning: line segment length (cells per warp work item) of each sweep;
- * multiples of 32.  0 keeps the current value. */
-int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t seg_x, int32_t seg_y);
+/* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
+ * and warps per block of the y-sweep kernel (<= 8).  0 keeps the current
+ * value.  Results do not depend on the tiling. */
+int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
 
 const char *cliffs_gpu_strerror(int code);
 
