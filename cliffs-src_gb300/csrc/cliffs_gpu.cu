@@ -51,10 +51,6 @@ struct cliffs_ctx {
   float *eta[2] = {nullptr, nullptr}, *xu[2] = {nullptr, nullptr}, *yv[2] = {nullptr, nullptr};
   float *hmax = nullptr, *velmax = nullptr;
   int cur = 0;
-  // worklist of cells for the general kernel and one counter per sweep parity
-  uint32_t* list = nullptr;
-  uint32_t* cnt = nullptr;
-  unsigned sweeps = 0;
   float4 *geo_x = nullptr, *geo_y = nullptr;
   float* scl_y = nullptr;
   float2* lscale = nullptr;
@@ -74,7 +70,11 @@ struct cliffs_ctx {
   std::vector<Nest> nests;
   int* d_flag = nullptr;
   bool have_state = false;
-  int blk_x = 128, warps_y = 8;  // fast-kernel block shapes (cliffs_gpu_set_tiling)
+  int blk_x = 128, warps_y = 8;
+  // worklist of cells for the general kernel and one counter per sweep parity
+  uint32_t* list = nullptr;
+  uint32_t* cnt = nullptr;
+  unsigned sweeps = 0;  // fast-kernel block shapes (cliffs_gpu_set_tiling)
   bool geo_uni_x = false, geo_uni_y = false;
   float4 geo0_x = {0, 0, 0, 0}, geo0_y = {0, 0, 0, 0};
   bool prof = false;
@@ -386,14 +386,14 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   A.velmax = fuse_max ? c->velmax : nullptr;
   A.ph = phys(c);
   A.status = c->status;
+  A.list = c->list;
+  A.count = c->cnt + (c->sweeps & 1u);
+  A.count_next = c->cnt + ((c->sweeps + 1u) & 1u);
   A.feedA = fA;
   A.feedB = fB;
   A.feed_len = flen;
   A.irec = irec;
   A.cc = cc;
-  A.list = c->list;
-  A.count = c->cnt + (c->sweeps & 1u);
-  A.count_next = c->cnt + ((c->sweeps + 1u) & 1u);
   if (iu == 1) {
     A.n = c->nx;
     A.nlines = c->ny;
@@ -551,10 +551,10 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   if (dalloc(&c->dep, cells) || dalloc(&c->eta[0], cells) || dalloc(&c->eta[1], cells) ||
       dalloc(&c->xu[0], cells) || dalloc(&c->xu[1], cells) || dalloc(&c->yv[0], cells) ||
       dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
-      dalloc(&c->list, (size_t)c->nx * c->ny) || dalloc(&c->cnt, 2) ||
       dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
       dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
-      dalloc(&c->status, 1) || dalloc(&c->d_flag, 1))
+      dalloc(&c->status, 1) || dalloc(&c->d_flag, 1) || dalloc(&c->list, (size_t)c->nx * c->ny) ||
+      dalloc(&c->cnt, 2))
     return fail(CLIFFS_ERR_NOMEM);
   // bathymetry, padded rows
   std::vector<float> h((size_t)c->pitch * c->ny, 0.f);

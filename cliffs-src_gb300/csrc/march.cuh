@@ -201,6 +201,178 @@ CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, c
   return o;
 }
 
+// Open / forced edge update of line cell 1 (cliffs.f:288-308): C is cell 1
+// and B cell 2 (flood-modified), both wet or flooded.
+template <typename R>
+CL_HD void edge_left(const CellState<R>& C, const CellState<R>& B, const EdgeVals<R>& e, R inv_dx1, R scl1,
+                     const Phys<R>& p, R& cn, R& un, R& vn, R& en) {
+  R FP, FQ;
+  face_flux(C.u, C.c, C.e, B.u, B.c, B.e, p, FP, FQ);
+  const R sphr = R(8) * C.c * C.u * scl1;
+  const R dQ = -p.dt * (FQ * inv_dx1 + sphr);
+  const R cbnd = csqrt(p.g * (C.d + e.eta));
+  const R dP = (e.un - C.u) + R(2) * p.g * (e.eta - C.e) / (cbnd + C.c);
+  vn = (C.u < R(0)) ? C.v - p.dt * (B.v - C.v) * C.u * inv_dx1 : e.vt;
+  const R dc = R(0.25) * (dP - dQ);
+  cn = C.c + dc;
+  un = C.u + R(0.5) * (dP + dQ);
+  en = eta_step(C.c, C.e, dc, C.d, p);
+}
+
+// Open / forced edge update of line cell n (cliffs.f:309-329): D is cell n-1,
+// C cell n.
+template <typename R>
+CL_HD void edge_right(const CellState<R>& D, const CellState<R>& C, const EdgeVals<R>& e, R inv_dxn1, R scln,
+                      const Phys<R>& p, R& cn, R& un, R& vn, R& en) {
+  R FP, FQ;
+  face_flux(D.u, D.c, D.e, C.u, C.c, C.e, p, FP, FQ);
+  const R sphr = R(8) * C.c * C.u * scln;
+  const R dP = -p.dt * (FP * inv_dxn1 - sphr);
+  const R cbnd = csqrt(p.g * (C.d + e.eta));
+  const R dQ = (e.un - C.u) - R(2) * p.g * (e.eta - C.e) / (cbnd + C.c);
+  vn = (C.u > R(0)) ? C.v - p.dt * (C.v - D.v) * C.u * inv_dxn1 : e.vt;
+  const R dc = R(0.25) * (dP - dQ);
+  cn = C.c + dc;
+  un = C.u + R(0.5) * (dP + dQ);
+  en = eta_step(C.c, C.e, dc, C.d, p);
+}
+
+// Raw input of one line cell; present iff 1 <= position <= n.
+template <typename R>
+struct RawCell {
+  R d, e, u, v;
+  bool present;
+};
+
+// Per-line constants the wet/dry rules need.
+template <typename R>
+struct LineCtx {
+  int n;
+  bool wet;            // the line holds a wet cell (else it is left untouched)
+  EdgeVals<R> eL, eR;  // forcing at cells 1 and n
+  R inv_dx1, inv_dxn1, scl1, scln;
+};
+
+// Final value of line cell o from the raw cells o-3..o+3 (w[3] is cell o):
+// the whole of cliffs.f:56-329 evaluated for one cell with the per-cell rules
+//   R(k) = land(k) & !land(k-1) & u(k-1) >= 0 & flood from k-1  (cliffs.f:76-82)
+//   L(k) = land(k) & !R(k) & !land(k+1) & u(k+1) <= 0 & flood from k+1 (89-98)
+//   wet-or-flooded(k) = !land(k) | R(k) | L(k)
+// an interior neighbour outside the cell's run is the mirror ghost of the cell
+// (cliffs.f:137-152); the angle limiter applies to a cell flooded from the left
+// (right) whose other side is newland (cliffs.f:264-285).  geo[t] is the
+// geometry of positions o-1, o, o+1 (t = 0, 1, 2).
+template <typename R>
+CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L, const Geo<R> geo[3],
+                              const Phys<R>& p) {
+  bool land[7], Rf[7], Lf[7], ew[7];
+  R H[7];
+#pragma unroll
+  for (int t = 0; t < 7; ++t) {
+    H[t] = w[t].d + w[t].e;
+    land[t] = !w[t].present || H[t] <= p.ground;
+    Rf[t] = Lf[t] = false;
+  }
+#pragma unroll
+  for (int t = 1; t <= 5; ++t) {
+    if (w[t].present && land[t]) {
+      Rf[t] = w[t - 1].present && !land[t - 1] && w[t - 1].u >= R(0) && (w[t - 1].e + w[t].d > p.ground);
+      Lf[t] = !Rf[t] && w[t + 1].present && !land[t + 1] && w[t + 1].u <= R(0) &&
+              (w[t + 1].e + w[t].d > p.ground);
+    }
+  }
+  CellState<R> fm[7];
+#pragma unroll
+  for (int t = 0; t < 7; ++t) {
+    ew[t] = w[t].present && (!land[t] || Rf[t] || Lf[t]);
+    if (Rf[t] || Lf[t]) {
+      const int s = Rf[t] ? t - 1 : t + 1;
+      fm[t] = CellState<R>{w[s].u, p.celmin, p.ground - w[t].d, w[t].d, w[s].v, p.ground};
+    } else {
+      fm[t] = CellState<R>{w[t].u, fsqrt_pos(p.g * (H[t] > p.ground ? H[t] : p.ground)), w[t].e, w[t].d, w[t].v,
+                           H[t]};
+    }
+  }
+  OutCell<R> out;
+  if (!ew[3]) {
+    if (L.wet) {  // newland in a line with water: h=u=v=0 (cliffs.f:118-122)
+      out.eta = -w[3].d;
+      out.u = R(0);
+      out.v = R(0);
+    } else {  // a line without water is left untouched (cliffs.f:113)
+      out.eta = w[3].e;
+      out.u = w[3].u;
+      out.v = w[3].v;
+    }
+    return out;
+  }
+  const int n = L.n;
+  if (o == 1 || o == n) {
+    // flood-modified value unless the edge condition holds
+    out.eta = fm[3].e;
+    out.u = fm[3].u;
+    out.v = fm[3].v;
+    R cn, un, vn, en;
+    if (o == 1 && n >= 2 && ew[4] && (L.eL.eta + w[3].d > p.ground)) {
+      edge_left(fm[3], fm[4], L.eL, L.inv_dx1, L.scl1, p, cn, un, vn, en);
+      out.eta = en;
+      out.u = un;
+      out.v = vn;
+    } else if (o == n && n >= 2 && ew[2] && (L.eR.eta + w[3].d > p.ground)) {
+      edge_right(fm[2], fm[3], L.eR, L.inv_dxn1, L.scln, p, cn, un, vn, en);
+      out.eta = en;
+      out.u = un;
+      out.v = vn;
+    }
+    return out;
+  }
+  // interior update of cell t with real or mirror neighbours
+  auto update = [&](int t, const Geo<R>& g, R& cn) -> OutCell<R> {
+    const CellState<R>& j = fm[t];
+    const CellState<R> mir{-j.u, j.c, j.e, j.d, j.v, j.H};
+    const CellState<R>& a = ew[t - 1] ? fm[t - 1] : mir;
+    const CellState<R>& b = ew[t + 1] ? fm[t + 1] : mir;
+    R FPl, FQl, FPr, FQr;
+    face_flux(a.u, a.c, a.e, j.u, j.c, j.e, p, FPl, FQl);
+    face_flux(j.u, j.c, j.e, b.u, b.c, b.e, p, FPr, FQr);
+    return interior_update(a, j, b, FPl, FQl, FPr, FQr, g, p, &cn);
+  };
+  R cO;
+  out = update(3, geo[1], cO);
+  if (Lf[3] && !ew[2]) {
+    // newly wetted cell on a left shoreline: limit against cell o+1
+    R hj, uj;
+    if (o + 1 <= n - 1) {
+      const OutCell<R> nb = update(4, geo[2], hj);
+      uj = nb.u;
+    } else {
+      hj = fm[4].c;
+      uj = fm[4].u;
+    }
+    if (p.sqr2 * cO > hj) {
+      cO = hj / p.sqr2;
+      out.eta = eta_from_c(cO, w[3].d, p);
+    }
+    if (out.u < uj) out.u = uj;
+  } else if (Rf[3] && !ew[4]) {
+    // newly wetted cell on a right shoreline: limit against cell o-1
+    R hj, uj;
+    if (o - 1 >= 2) {
+      const OutCell<R> nb = update(2, geo[0], hj);
+      uj = nb.u;
+    } else {
+      hj = fm[2].c;
+      uj = fm[2].u;
+    }
+    if (p.sqr2 * cO > hj) {
+      cO = hj / p.sqr2;
+      out.eta = eta_from_c(cO, w[3].d, p);
+    }
+    if (out.u > uj) out.u = uj;
+  }
+  return out;
+}
+
 template <typename R>
 struct LineMarch {
   Phys<R> p;

@@ -1,25 +1,24 @@
-// sweep.cuh -- the two kernels of one dimensional sweep (cliffs.f:17-346 over
-// every line of the grid, cliffs_main.f:325-344).
+// sweep.cuh -- the two kernels of one dimensional sweep: subroutine cliffs
+// (cliffs.f:17-346) over every line of the grid (cliffs_main.f:325-344).
 //
-// fast kernel: one thread per 4 consecutive cells of a line.  It loads the
-//   6-cell window (the 4 cells and one neighbour on each side) into registers
-//   (x-sweep: float4 loads along the row plus two shuffled halo cells;
-//   y-sweep: 6 coalesced row loads of its column), and finishes every cell
-//   whose own update needs no wet/dry logic:
-//     - a cell with both neighbours wet (all three H > ground) gets the plain
-//       VTCS-2 interior update (no flooding, no shoreline ghost, no limiter);
-//     - a dry cell between dry neighbours that already holds the zero state
-//       stays as it is (the reference zeroes it, or leaves the whole line
-//       untouched: both give the same values).
-//   Every other cell (shoreline, line ends, dried cells with residual state)
-//   goes to a worklist.
-// general kernel: one thread per worklist cell replays the full line update
-//   (LineMarch: flooding, mirror ghosts, angle limiter, open/forced edges) over
-//   the cell's window of +-3 neighbours and writes that one cell.
+// fast kernel: one thread owns 4 consecutive cells of a line and loads the
+//   6-cell window (the 4 cells and one neighbour on each side) into registers:
+//   the x-sweep (lines are rows) with float4 loads along the row plus two
+//   shuffled halo cells, the y-sweep (lines are columns) with 6 row loads that
+//   are coalesced across the warp (lanes are neighbouring columns).  It
+//   finishes every cell whose update needs no wet/dry logic:
+//     - both neighbours wet (all three H > ground): the plain VTCS-2 interior
+//       update (the open ocean, almost every cell);
+//     - dry between dry neighbours and already at the zero state: unchanged
+//       (the reference zeroes it, or leaves the whole line untouched: same
+//       values);
+//   and lists every other cell (shorelines, line ends, drying cells).
+// general kernel: one thread per listed cell evaluates general_cell, the full
+//   wet/dry rule set, on the raw cells o-3..o+3 and overwrites that cell.
 //
-// The worklist is the only scratch memory: (line, position) pairs and a
-// counter per sweep parity.  A fast kernel zeroes the counter of the other
-// parity, which the previous sweep's general kernel has finished with.
+// The worklist is the sweep's only scratch memory: (line, position) entries
+// and one counter per sweep parity; the fast kernel zeroes the counter of the
+// other parity, which the previous sweep's general kernel has finished with.
 #pragma once
 #include <cstdint>
 
@@ -54,9 +53,9 @@ struct SweepArgs {
   int irec;
   double cc;
   Phys<float> ph;
-  uint32_t* list;       // worklist: (line-1)*n + (position-1)
-  uint32_t* count;      // worklist length of this sweep
-  uint32_t* count_next; // the other parity's counter, zeroed by the fast kernel
+  uint32_t* list;        // worklist: (line-1)*n + (position-1)
+  uint32_t* count;       // worklist length of this sweep
+  uint32_t* count_next;  // the other parity's counter, zeroed by the fast kernel
   unsigned* status;
 };
 
@@ -70,8 +69,9 @@ __device__ __forceinline__ size_t cidx(int L, int k, int pitch) {
 }
 
 __device__ __forceinline__ Geo<float> geo_at(const SweepArgs& A, int m, float alpha, float ialpha) {
-  float4 g = A.geo_uniform ? A.geo0 : __ldg(A.geo + (m - 1));
-  Geo<float> r;
+  Geo<float> r{0.f, 0.f, 0.f, 0.f, 0.f};
+  if (m < 2 || m > A.n - 1) return r;
+  const float4 g = A.geo_uniform ? A.geo0 : __ldg(A.geo + (m - 1));
   r.inv_fm = g.x * ialpha;
   r.inv_fp = g.y * ialpha;
   r.dtx = g.z * ialpha;
@@ -80,23 +80,64 @@ __device__ __forceinline__ Geo<float> geo_at(const SweepArgs& A, int m, float al
   return r;
 }
 
+// edge1/edge2 of line L = lerp of the forcing records (cliffs_main.f:318-339).
 template <int DIR>
-__device__ __forceinline__ void store_out(const SweepArgs& A, size_t q, float eo, float uo, float vo,
-                                          bool& bad) {
-  const float xo = DIR == 0 ? uo : vo;
-  const float yo = DIR == 0 ? vo : uo;
-  A.eta_o[q] = eo;
-  A.xu_o[q] = xo;
-  A.yv_o[q] = yo;
-  if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
-    if (eo > A.hmax[q]) A.hmax[q] = eo;
-    const float s2 = xo * xo + yo * yo;
-    if (s2 > A.velmax[q]) A.velmax[q] = s2;
-  }
-  bad |= !isfinite(eo + xo + yo);
+__device__ __forceinline__ EdgeVals<float> edge_vals(const SweepArgs& A, const double* F, int L) {
+  if (!F) return EdgeVals<float>{0.f, 0.f, 0.f};
+  const int len = A.feed_len;
+  const size_t r0 = (size_t)(A.irec - 2) * 3 * (size_t)len;
+  const size_t r1 = (size_t)(A.irec - 1) * 3 * (size_t)len;
+  const double cc = A.cc;
+  const int cn = DIR == 0 ? 0 : 1;  // normal velocity component (iu)
+  const int ct = DIR == 0 ? 1 : 0;  // tangential component (3-iu)
+  auto val = [&](int comp) -> float {
+    const size_t b = (size_t)(L - 1) + (size_t)comp * (size_t)len;
+    return (float)(F[b + r0] * cc + F[b + r1] * (1.0 - cc));
+  };
+  return EdgeVals<float>{val(cn), val(ct), val(2)};
 }
 
-// Warp-aggregated append to the worklist.
+// The cell's value through the full wet/dry rules (cliffs.f:56-329).
+template <int DIR>
+__device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L, int o, float alpha, float ialpha) {
+  const int n = A.n;
+  const Phys<float>& p = A.ph;
+  RawCell<float> w[7];
+  bool anywet = false;
+#pragma unroll
+  for (int t = 0; t < 7; ++t) {
+    const int k = o - 3 + t;
+    w[t] = RawCell<float>{0.f, 0.f, 0.f, 0.f, false};
+    if (k >= 1 && k <= n) {
+      const size_t q = cidx<DIR>(L, k, A.pitch);
+      const float xu = __ldg(A.xu + q), yv = __ldg(A.yv + q);
+      w[t] = RawCell<float>{__ldg(A.dep + q), __ldg(A.eta + q), DIR == 0 ? xu : yv, DIR == 0 ? yv : xu, true};
+      anywet |= w[t].d + w[t].e > p.ground;
+    }
+  }
+  LineCtx<float> C;
+  C.n = n;
+  C.wet = anywet;
+  if (!anywet && !(w[3].d + w[3].e == 0.f && w[3].u == 0.f && w[3].v == 0.f)) {
+    // does the line hold a wet cell anywhere (cliffs.f:113)?
+    for (int k = 1; k <= n && !C.wet; ++k) {
+      const size_t q = cidx<DIR>(L, k, A.pitch);
+      C.wet = __ldg(A.dep + q) + __ldg(A.eta + q) > p.ground;
+    }
+  }
+  C.eL = o == 1 ? edge_vals<DIR>(A, A.feedA, L) : EdgeVals<float>{0.f, 0.f, 0.f};
+  C.eR = o == n ? edge_vals<DIR>(A, A.feedB, L) : EdgeVals<float>{0.f, 0.f, 0.f};
+  C.inv_dx1 = A.inv_dx1 * ialpha;
+  C.inv_dxn1 = A.inv_dxn1 * ialpha;
+  C.scl1 = A.scl ? A.scl[0] : 0.f;
+  C.scln = A.scl ? A.scl[n - 1] : 0.f;
+  Geo<float> g[3];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) g[t] = geo_at(A, o - 1 + t, alpha, ialpha);
+  return general_cell(w, o, C, g, p);
+}
+
+// Warp-aggregated append to the worklist; every lane of the warp calls it.
 __device__ __forceinline__ void enqueue(const SweepArgs& A, bool want, uint32_t entry) {
   const unsigned m = __ballot_sync(0xffffffffu, want);
   if (!m) return;
@@ -123,24 +164,32 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     L = blockIdx.y * 32 + lane + 1;
     i0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kCellsPerThread + 1;
   }
-  const bool active = L <= A.nlines && i0 <= n;  // x-sweep: warp-uniform in L
+  const bool active = L <= A.nlines && i0 <= n;
   const bool swept = active && L >= A.lo && L <= A.hi;
-  // window w[0..5] = positions i0-1 .. i0+4
+  const Phys<float>& p = A.ph;
+  // window w[0..5] = positions i0-1 .. i0+4 (u normal, v tangential)
   float d[6], e[6], u[6], v[6];
+  float hm[kCellsPerThread], vm[kCellsPerThread];
+  size_t q0 = 0;
   if (DIR == 0) {
-    // float4 along the row: positions i0..i0+3; halo cells from the neighbours
-    const size_t q0 = cidx<0>(min(L, A.nlines), i0, A.pitch);
-    float4 D4 = make_float4(0, 0, 0, 0), E4 = D4, X4 = D4, Y4 = D4;
+    q0 = cidx<0>(min(L, A.nlines), i0, A.pitch);
+    float4 D4 = make_float4(0, 0, 0, 0), E4 = D4, X4 = D4, Y4 = D4, H4 = D4, V4 = D4;
     if (active) {
       D4 = __ldg(reinterpret_cast<const float4*>(A.dep + q0));
       E4 = __ldg(reinterpret_cast<const float4*>(A.eta + q0));
       X4 = __ldg(reinterpret_cast<const float4*>(A.xu + q0));
       Y4 = __ldg(reinterpret_cast<const float4*>(A.yv + q0));
+      if (A.hmax) {
+        H4 = *reinterpret_cast<const float4*>(A.hmax + q0);
+        V4 = *reinterpret_cast<const float4*>(A.velmax + q0);
+      }
     }
     d[1] = D4.x; d[2] = D4.y; d[3] = D4.z; d[4] = D4.w;
     e[1] = E4.x; e[2] = E4.y; e[3] = E4.z; e[4] = E4.w;
     u[1] = X4.x; u[2] = X4.y; u[3] = X4.z; u[4] = X4.w;
     v[1] = Y4.x; v[2] = Y4.y; v[3] = Y4.z; v[4] = Y4.w;
+    hm[0] = H4.x; hm[1] = H4.y; hm[2] = H4.z; hm[3] = H4.w;
+    vm[0] = V4.x; vm[1] = V4.y; vm[2] = V4.z; vm[3] = V4.w;
     d[0] = __shfl_up_sync(0xffffffffu, D4.w, 1);
     e[0] = __shfl_up_sync(0xffffffffu, E4.w, 1);
     u[0] = __shfl_up_sync(0xffffffffu, X4.w, 1);
@@ -164,27 +213,37 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
   } else {
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
-      const int k = i0 - 1 + w;
+      const int k = min(max(i0 - 1 + w, 1), n);
+      const size_t q = cidx<1>(min(L, A.nlines), k, A.pitch);
       d[w] = e[w] = u[w] = v[w] = 0.f;
-      if (active && k >= 1 && k <= n) {
-        const size_t q = cidx<1>(L, k, A.pitch);
+      if (active) {
         d[w] = __ldg(A.dep + q);
         e[w] = __ldg(A.eta + q);
         v[w] = __ldg(A.xu + q);  // tangential in the y-sweep
         u[w] = __ldg(A.yv + q);  // normal
       }
     }
-  }
-  bool bad = false;
-  unsigned need = 0u;  // bit r: cell i0+r goes to the general kernel
-  if (active && !swept) {  // lines not swept are copied through
 #pragma unroll
     for (int r = 0; r < kCellsPerThread; ++r) {
-      const int k = i0 + r;
-      if (k <= n) store_out<DIR>(A, cidx<DIR>(L, k, A.pitch), e[r + 1], u[r + 1], v[r + 1], bad);
+      hm[r] = vm[r] = 0.f;
+      const int k = min(i0 + r, n);
+      if (active && A.hmax) {
+        const size_t q = cidx<1>(L, k, A.pitch);
+        hm[r] = A.hmax[q];
+        vm[r] = A.velmax[q];
+      }
+    }
+  }
+  float oe[kCellsPerThread], ou[kCellsPerThread], ov[kCellsPerThread];
+  unsigned need = 0u;  // bit r: cell i0+r goes to the general kernel
+  if (!swept) {  // lines not swept are copied through
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r) {
+      oe[r] = e[r + 1];
+      ou[r] = u[r + 1];
+      ov[r] = v[r + 1];
     }
   } else if (active) {
-    const Phys<float>& p = A.ph;
     float alpha = 1.f, ialpha = 1.f;
     if (DIR == 0 && A.lscale != nullptr) {
       const float2 s = A.lscale[L - 1];
@@ -207,31 +266,71 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     for (int r = 0; r < kCellsPerThread; ++r) {
       const int k = i0 + r;
       const int w = r + 1;
-      if (k <= n) {
-        const size_t q = cidx<DIR>(L, k, A.pitch);
-        if (k >= 2 && k <= n - 1 && wet[w - 1] && wet[w] && wet[w + 1]) {
-          const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
-          const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
-          const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
-          float cn;
-          const OutCell<float> o =
-              interior_update(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], geo_at(A, k, alpha, ialpha), p, &cn);
-          store_out<DIR>(A, q, o.eta, o.u, o.v, bad);
-        } else if (!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f) {
-          store_out<DIR>(A, q, e[w], u[w], v[w], bad);  // dry, zero state: unchanged either way
-        } else {
-          need |= 1u << r;
-        }
+      oe[r] = e[w];
+      ou[r] = u[w];
+      ov[r] = v[w];
+      if (k > n) continue;
+      if (k >= 2 && k <= n - 1 && wet[w - 1] && wet[w] && wet[w + 1]) {
+        const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
+        const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
+        const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
+        float cn;
+        const OutCell<float> o =
+            interior_update(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], geo_at(A, k, alpha, ialpha), p, &cn);
+        oe[r] = o.eta;
+        ou[r] = o.u;
+        ov[r] = o.v;
+      } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
+        need |= 1u << r;
       }
+      // else: dry, zero state: unchanged whether or not the line holds water
     }
   }
 #pragma unroll
   for (int r = 0; r < kCellsPerThread; ++r)
-    enqueue(A, (need >> r) & 1u, (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1));
+    enqueue(A, active && ((need >> r) & 1u), (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1));
+  if (!active) return;
+  bool bad = false;
+  float xo[kCellsPerThread], yo[kCellsPerThread];
+#pragma unroll
+  for (int r = 0; r < kCellsPerThread; ++r) {
+    xo[r] = DIR == 0 ? ou[r] : ov[r];
+    yo[r] = DIR == 0 ? ov[r] : ou[r];
+    const bool done = i0 + r <= n && !((need >> r) & 1u);
+    if (done) bad |= !isfinite(oe[r] + xo[r] + yo[r]);
+    if (A.hmax && done) {  // max-wave update (cliffs_main.f:347-355)
+      hm[r] = fmaxf(hm[r], oe[r]);
+      vm[r] = fmaxf(vm[r], xo[r] * xo[r] + yo[r] * yo[r]);
+    }
+  }
+  if (DIR == 0) {
+    // whole float4s: the row padding beyond nx takes the values of no cell
+    *reinterpret_cast<float4*>(A.eta_o + q0) = make_float4(oe[0], oe[1], oe[2], oe[3]);
+    *reinterpret_cast<float4*>(A.xu_o + q0) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+    *reinterpret_cast<float4*>(A.yv_o + q0) = make_float4(yo[0], yo[1], yo[2], yo[3]);
+    if (A.hmax) {
+      *reinterpret_cast<float4*>(A.hmax + q0) = make_float4(hm[0], hm[1], hm[2], hm[3]);
+      *reinterpret_cast<float4*>(A.velmax + q0) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r) {
+      const int k = i0 + r;
+      if (k > n) break;
+      const size_t q = cidx<1>(L, k, A.pitch);
+      A.eta_o[q] = oe[r];
+      A.xu_o[q] = xo[r];
+      A.yv_o[q] = yo[r];
+      if (A.hmax) {
+        A.hmax[q] = hm[r];
+        A.velmax[q] = vm[r];
+      }
+    }
+  }
   if (bad) atomicOr(A.status, ST_NAN);
 }
 
-// One thread per worklist cell: the full line update over its +-3 window.
+// One thread per listed cell: the full wet/dry rules over its +-3 window.
 template <int DIR>
 __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {
   const uint32_t cnt = *A.count;
@@ -240,72 +339,24 @@ __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {
     const uint32_t ent = A.list[t];
     const int L = (int)(ent / (uint32_t)n) + 1;
     const int o = (int)(ent % (uint32_t)n) + 1;
-    const Phys<float>& p = A.ph;
-    // Does the line hold a wet cell (cliffs.f:113)?  The +-3 window usually
-    // answers; a cell whose window is all dry needs the answer only when it
-    // holds a non-zero residual state, and then the whole line is scanned.
-    bool wet = false, need = false;
-    for (int k = max(1, o - 3); k <= min(n, o + 3); ++k) {
-      const size_t q = cidx<DIR>(L, k, A.pitch);
-      wet |= __ldg(A.dep + q) + __ldg(A.eta + q) > p.ground;
-    }
-    if (!wet) {
-      const size_t q = cidx<DIR>(L, o, A.pitch);
-      need = (__ldg(A.dep + q) + __ldg(A.eta + q)) != 0.f || __ldg(A.xu + q) != 0.f || __ldg(A.yv + q) != 0.f;
-      for (int k = 1; need && !wet && k <= n; ++k) {
-        const size_t q2 = cidx<DIR>(L, k, A.pitch);
-        wet |= __ldg(A.dep + q2) + __ldg(A.eta + q2) > p.ground;
-      }
-    }
     float alpha = 1.f, ialpha = 1.f;
     if (DIR == 0 && A.lscale != nullptr) {
       const float2 s = A.lscale[L - 1];
       alpha = s.x;
       ialpha = s.y;
     }
-    LineMarch<float> M;
-    M.init(p, n, wet);
-    M.inv_dx1 = A.inv_dx1 * ialpha;
-    M.inv_dxn1 = A.inv_dxn1 * ialpha;
-    M.scl1 = A.scl ? A.scl[0] : 0.f;
-    M.scln = A.scl ? A.scl[n - 1] : 0.f;
-    M.eL = EdgeVals<float>{0.f, 0.f, 0.f};
-    M.eR = EdgeVals<float>{0.f, 0.f, 0.f};
-    if ((o <= 4 || o >= n - 3) && (A.feedA || A.feedB)) {
-      // edge1/edge2 = lerp of the forcing records (cliffs_main.f:318-339)
-      const int len = A.feed_len;
-      const size_t r0 = (size_t)(A.irec - 2) * 3 * (size_t)len;
-      const size_t r1 = (size_t)(A.irec - 1) * 3 * (size_t)len;
-      const double cc = A.cc;
-      const int cn = DIR == 0 ? 0 : 1;  // normal velocity component (iu)
-      const int ct = DIR == 0 ? 1 : 0;  // tangential component (3-iu)
-      auto val = [&](const double* F, int comp) -> float {
-        const size_t b = (size_t)(L - 1) + (size_t)comp * (size_t)len;
-        return (float)(F[b + r0] * cc + F[b + r1] * (1.0 - cc));
-      };
-      if (A.feedA) M.eL = EdgeVals<float>{val(A.feedA, cn), val(A.feedA, ct), val(A.feedA, 2)};
-      if (A.feedB) M.eR = EdgeVals<float>{val(A.feedB, cn), val(A.feedB, ct), val(A.feedB, 2)};
+    const OutCell<float> r = general_path<DIR>(A, L, o, alpha, ialpha);
+    const size_t q = cidx<DIR>(L, o, A.pitch);
+    const float xo = DIR == 0 ? r.u : r.v;
+    const float yo = DIR == 0 ? r.v : r.u;
+    A.eta_o[q] = r.eta;
+    A.xu_o[q] = xo;
+    A.yv_o[q] = yo;
+    if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
+      A.hmax[q] = fmaxf(A.hmax[q], r.eta);
+      A.velmax[q] = fmaxf(A.velmax[q], xo * xo + yo * yo);
     }
-    OutCell<float> res{0.f, 0.f, 0.f};
-    for (int k = max(1, o - 3); k <= o + 3; ++k) {
-      float dd = 0.f, ee = 0.f, uu = 0.f, vv = 0.f;
-      if (k <= n) {
-        const size_t q = cidx<DIR>(L, k, A.pitch);
-        dd = __ldg(A.dep + q);
-        ee = __ldg(A.eta + q);
-        const float xu = __ldg(A.xu + q), yv = __ldg(A.yv + q);
-        uu = DIR == 0 ? xu : yv;
-        vv = DIR == 0 ? yv : xu;
-      }
-      const int m = k - 2;
-      Geo<float> g{0.f, 0.f, 0.f, 0.f, 0.f};
-      if (m >= 2 && m <= n - 1) g = geo_at(A, m, alpha, ialpha);
-      OutCell<float> oc;
-      if (M.push(k, dd, ee, uu, vv, g, oc) && k - 3 == o) res = oc;
-    }
-    bool bad = false;
-    store_out<DIR>(A, cidx<DIR>(L, o, A.pitch), res.eta, res.u, res.v, bad);
-    if (bad) atomicOr(A.status, ST_NAN);
+    if (!isfinite(r.eta + xo + yo)) atomicOr(A.status, ST_NAN);
   }
 }
 
