@@ -1114,4 +1114,128 @@ int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t block_x, int32_t warps_y) {
   return CLIFFS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Sweep without device allocation.
+//
+// Callers that cannot allocate device memory use this entry point, e.g. a host
+// application that hands the solver a fixed memory budget up front and
+// forbids cudaMalloc afterwards, or a time loop that must not pay
+// cudaMalloc's implicit device synchronisation on every call.  The sweep's
+// only scratch, the worklist of cells that need the full wet/dry rules (and
+// its counters), lives in the fixed-size arrays below instead of memory the
+// library allocates.  Every GPU that loads this library holds them until the
+// process exits: kNoAllocCells * 4 bytes plus a few words.
+// ---------------------------------------------------------------------------
+
+static constexpr int kNoAllocCells = 1 << 20;  // largest nx*ny accepted
+static __device__ __align__(256) uint32_t g_noalloc_list[kNoAllocCells];
+static __device__ __align__(256) uint32_t g_noalloc_count[2];
+static __device__ __align__(256) unsigned g_noalloc_status[1];
+
+struct NoAllocScratch {
+  uint32_t* list = nullptr;
+  uint32_t* count = nullptr;
+  unsigned* status = nullptr;
+};
+
+// Device addresses of the scratch arrays, resolved once per device with that
+// device current.  In host code the array names are host-side stand-ins, never
+// device addresses.
+static int noalloc_scratch(NoAllocScratch* out) {
+  constexpr int kMaxDevices = 64;
+  static NoAllocScratch cache[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CLIFFS_ERR_DEVICE;
+  NoAllocScratch& s = cache[dev];
+  if (!s.list) {
+    void *a = nullptr, *b = nullptr, *c = nullptr;
+    if (cudaGetSymbolAddress(&a, g_noalloc_list) != cudaSuccess ||
+        cudaGetSymbolAddress(&b, g_noalloc_count) != cudaSuccess ||
+        cudaGetSymbolAddress(&c, g_noalloc_status) != cudaSuccess)
+      return CLIFFS_ERR_CUDA;
+    s.count = (uint32_t*)b;
+    s.status = (unsigned*)c;
+    s.list = (uint32_t*)a;
+  }
+  *out = s;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, const float* dep,
+                             const float* eta, const float* xvel, const float* yvel, float* eta_out,
+                             float* xvel_out, float* yvel_out, double dx, double dy, double ground,
+                             double crough, double dt, void* stream) {
+  if (iu != 1 && iu != 2) return CLIFFS_ERR_ARG;
+  if (nx < 1 || ny < 1 || (nx <= 2 && ny <= 2)) return CLIFFS_ERR_ARG;
+  if ((iu == 1 && nx <= 2) || (iu == 2 && ny <= 2)) return CLIFFS_ERR_ARG;
+  if ((int64_t)nx * (int64_t)ny > kNoAllocCells) return CLIFFS_ERR_ARG;
+  if (pitch < nx || pitch % 4 != 0) return CLIFFS_ERR_ARG;
+  const void* ptrs[] = {dep, eta, xvel, yvel, eta_out, xvel_out, yvel_out};
+  for (const void* q : ptrs)
+    if (!q || ((uintptr_t)q % 16) != 0) return CLIFFS_ERR_ARG;
+  if (!(dt > 0) || !(ground > 0) || crough < 0) return CLIFFS_ERR_ARG;
+  if ((iu == 1 && !(dx > 0)) || (iu == 2 && !(dy > 0))) return CLIFFS_ERR_ARG;
+  NoAllocScratch sc;
+  int r = noalloc_scratch(&sc);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  SweepArgs A{};
+  A.pitch = pitch;
+  A.dep = dep;
+  A.eta = eta;
+  A.xu = xvel;
+  A.yv = yvel;
+  A.eta_o = eta_out;
+  A.xu_o = xvel_out;
+  A.yv_o = yvel_out;
+  A.hmax = nullptr;
+  A.velmax = nullptr;
+  A.ph.g = (float)kGrav;
+  A.ph.ginv = (float)(1.0 / kGrav);
+  A.ph.ground = (float)ground;
+  A.ph.celmin = (float)sqrt(kGrav * ground);
+  A.ph.dt = (float)dt;
+  A.ph.idt = (float)(1.0 / dt);
+  A.ph.gcrough = (float)(kGrav * crough);
+  A.ph.sqr2 = (float)kSqr2;
+  const double h = iu == 1 ? dx : dy;  // uniform spacing along the line
+  A.geo = nullptr;
+  A.geo_uniform = 1;
+  A.geo0 = make_float4((float)(1.0 / h), (float)(1.0 / h), (float)(dt / (2.0 * h)), 0.f);
+  A.scl = nullptr;
+  A.lscale = nullptr;
+  A.inv_dx1 = A.inv_dxn1 = (float)(1.0 / h);
+  A.feedA = A.feedB = nullptr;
+  A.feed_len = 0;
+  A.irec = 2;
+  A.cc = 1.0;
+  A.list = sc.list;
+  A.count = sc.count;
+  A.count_next = sc.count + 1;
+  A.status = sc.status;
+  // the shared counter keeps the previous call's value: start from zero
+  CK(cudaMemsetAsync(sc.count, 0, sizeof(uint32_t), st));
+  if (iu == 1) {
+    A.n = nx;
+    A.nlines = ny;
+    A.lo = ny > 2 ? 2 : 1;
+    A.hi = ny > 2 ? ny - 1 : 1;
+    const dim3 grid((nx + 128 * kCellsPerThread - 1) / (128 * kCellsPerThread), ny);
+    fast_kernel<0><<<grid, 128, 0, st>>>(A);
+    CK(cudaGetLastError());
+    general_kernel<0><<<kGeneralBlocks, 128, 0, st>>>(A);
+  } else {
+    A.n = ny;
+    A.nlines = nx;
+    A.lo = nx > 2 ? 2 : 1;
+    A.hi = nx > 2 ? nx - 1 : 1;
+    const dim3 grid((ny + 8 * kCellsPerThread - 1) / (8 * kCellsPerThread), (nx + 31) / 32);
+    fast_kernel<1><<<grid, 256, 0, st>>>(A);
+    CK(cudaGetLastError());
+    general_kernel<1><<<kGeneralBlocks, 128, 0, st>>>(A);
+  }
+  CK(cudaGetLastError());
+  return CLIFFS_OK;
+}
+
 }  // extern "C"

@@ -189,6 +189,36 @@ int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
  * value.  Results do not depend on the tiling. */
 int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
 
+/* One sweep without any device allocation, for callers that cannot allocate
+ * device memory: an application that gives the solver a fixed memory budget
+ * and forbids cudaMalloc afterwards, or a time loop that must not pay the
+ * implicit device synchronisation of cudaMalloc.  This entry point has no
+ * counterpart in the reference; it is the x-sweep (iu=1) or y-sweep (iu=2)
+ * of cliffs_gpu_sweep on arrays the caller owns.
+ *
+ * Arrays are device FP32 in the library's own state form: dep (depth, >0
+ * water), eta (surface elevation = H - dep; a drying cell keeps H = c|c|/g),
+ * xvel, yvel, ny rows of `pitch` floats (pitch >= nx, a multiple of 4, every
+ * pointer 16-byte aligned).  Output rows are written whole, so columns
+ * nx..pitch-1 of the outputs may change.  The grid is Cartesian with uniform
+ * spacing dx (x-sweep) or dy (y-sweep), still-water open edges, no max-wave.
+ * Rows (iu=1) 2..ny-1 or columns (iu=2) 2..nx-1 are swept (row/column 1 on a
+ * 1-D grid); the other lines are copied.  The work is queued on `stream`
+ * (NULL: the default stream); nothing is synchronised.
+ *
+ * Limit: nx*ny <= 1048576 cells (CLIFFS_ERR_ARG beyond).  The scratch is a
+ * fixed 4 MiB device array inside the library that every GPU loading it keeps
+ * until the process exits; all calls share it, so calls that overlap on the
+ * GPU (different streams, or devices sharing a process without ordering) race
+ * on it.  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. */
+int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch,
+                             const float *dep, const float *eta,
+                             const float *xvel, const float *yvel,
+                             float *eta_out, float *xvel_out, float *yvel_out,
+                             double dx, double dy, double ground, double crough,
+                             double dt, void *stream);
+
 const char *cliffs_gpu_strerror(int code);
 
 #ifdef __cplusplus
