@@ -64,6 +64,9 @@ struct cliffs_ctx {
   // static edges for single sweeps (edge1/edge2 of module MASTER)
   double *edge_s[2] = {nullptr, nullptr};
   bool edges_static = false;
+  // per-step forcing at the line ends, 6 floats per line, for each sweep
+  float* edge_x = nullptr;
+  float* edge_y = nullptr;
   unsigned* status = nullptr;
   double* red = nullptr;  // reduction scratch
   int red_cap = 0;
@@ -389,11 +392,15 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   A.list = c->list;
   A.count = c->cnt + (c->sweeps & 1u);
   A.count_next = c->cnt + ((c->sweeps + 1u) & 1u);
-  A.feedA = fA;
-  A.feedB = fB;
-  A.feed_len = flen;
-  A.irec = irec;
-  A.cc = cc;
+  A.edges = nullptr;
+  if (fA || fB) {
+    float* eb = iu == 1 ? c->edge_x : c->edge_y;
+    const int nl = iu == 1 ? c->ny : c->nx;
+    edges_kernel<<<(nl + 127) / 128, 128, 0, c->stream>>>(nl, flen, fA, fB, irec, cc, iu == 1 ? 0 : 1,
+                                                          iu == 1 ? 1 : 0, eb);
+    CK(cudaGetLastError());
+    A.edges = eb;
+  }
   if (iu == 1) {
     A.n = c->nx;
     A.nlines = c->ny;
@@ -429,15 +436,11 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   if (iu == 1) {
     const int cells = c->blk_x * kCellsPerThread;
     const dim3 grid((A.n + cells - 1) / cells, A.nlines);
-    fast_kernel<0><<<grid, c->blk_x, 0, c->stream>>>(A);
-    CK(cudaGetLastError());
-    general_kernel<0><<<kGeneralBlocks, 128, 0, c->stream>>>(A);
+    fast_kernel<0, true><<<grid, c->blk_x, 0, c->stream>>>(A);
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
-    fast_kernel<1><<<grid, 32 * c->warps_y, 0, c->stream>>>(A);
-    CK(cudaGetLastError());
-    general_kernel<1><<<kGeneralBlocks, 128, 0, c->stream>>>(A);
+    fast_kernel<1, true><<<grid, 32 * c->warps_y, 0, c->stream>>>(A);
   }
   CK(cudaGetLastError());
   if (c->prof) {
@@ -554,6 +557,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
       dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
       dalloc(&c->status, 1) || dalloc(&c->d_flag, 1) || dalloc(&c->list, (size_t)c->nx * c->ny) ||
+      dalloc(&c->edge_x, (size_t)c->ny * 6) || dalloc(&c->edge_y, (size_t)c->nx * 6) ||
       dalloc(&c->cnt, 2))
     return fail(CLIFFS_ERR_NOMEM);
   // bathymetry, padded rows
@@ -624,7 +628,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   void* ptrs[] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
                   c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
-                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag};
+                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& n : c->nests) {
@@ -1205,10 +1209,7 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
   A.scl = nullptr;
   A.lscale = nullptr;
   A.inv_dx1 = A.inv_dxn1 = (float)(1.0 / h);
-  A.feedA = A.feedB = nullptr;
-  A.feed_len = 0;
-  A.irec = 2;
-  A.cc = 1.0;
+  A.edges = nullptr;
   A.list = sc.list;
   A.count = sc.count;
   A.count_next = sc.count + 1;
@@ -1221,7 +1222,7 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
     A.lo = ny > 2 ? 2 : 1;
     A.hi = ny > 2 ? ny - 1 : 1;
     const dim3 grid((nx + 128 * kCellsPerThread - 1) / (128 * kCellsPerThread), ny);
-    fast_kernel<0><<<grid, 128, 0, st>>>(A);
+    fast_kernel<0, false><<<grid, 128, 0, st>>>(A);
     CK(cudaGetLastError());
     general_kernel<0><<<kGeneralBlocks, 128, 0, st>>>(A);
   } else {
@@ -1230,7 +1231,7 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
     A.lo = nx > 2 ? 2 : 1;
     A.hi = nx > 2 ? nx - 1 : 1;
     const dim3 grid((ny + 8 * kCellsPerThread - 1) / (8 * kCellsPerThread), (nx + 31) / 32);
-    fast_kernel<1><<<grid, 256, 0, st>>>(A);
+    fast_kernel<1, false><<<grid, 256, 0, st>>>(A);
     CK(cudaGetLastError());
     general_kernel<1><<<kGeneralBlocks, 128, 0, st>>>(A);
   }

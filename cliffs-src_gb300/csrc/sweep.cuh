@@ -46,12 +46,10 @@ struct SweepArgs {
   const float* scl;      // per position metric term (y-sweep), nullptr = 0
   const float2* lscale;  // per line (alpha, 1/alpha) (x-sweep), nullptr = 1
   float inv_dx1, inv_dxn1;
-  // boundary forcing: records A (low edge) and B (high edge), (len,3,nt) FP64
-  const double* feedA;
-  const double* feedB;
-  int feed_len;
-  int irec;
-  double cc;
+  // forcing at the line ends for this step, 6 floats per line: normal
+  // velocity, tangential velocity, eta at cell 1, then at cell n; nullptr =
+  // still-water open edges
+  const float* edges;
   Phys<float> ph;
   uint32_t* list;        // worklist: (line-1)*n + (position-1)
   uint32_t* count;       // worklist length of this sweep
@@ -80,26 +78,17 @@ __device__ __forceinline__ Geo<float> geo_at(const SweepArgs& A, int m, float al
   return r;
 }
 
-// edge1/edge2 of line L = lerp of the forcing records (cliffs_main.f:318-339).
-template <int DIR>
-__device__ __forceinline__ EdgeVals<float> edge_vals(const SweepArgs& A, const double* F, int L) {
-  if (!F) return EdgeVals<float>{0.f, 0.f, 0.f};
-  const int len = A.feed_len;
-  const size_t r0 = (size_t)(A.irec - 2) * 3 * (size_t)len;
-  const size_t r1 = (size_t)(A.irec - 1) * 3 * (size_t)len;
-  const double cc = A.cc;
-  const int cn = DIR == 0 ? 0 : 1;  // normal velocity component (iu)
-  const int ct = DIR == 0 ? 1 : 0;  // tangential component (3-iu)
-  auto val = [&](int comp) -> float {
-    const size_t b = (size_t)(L - 1) + (size_t)comp * (size_t)len;
-    return (float)(F[b + r0] * cc + F[b + r1] * (1.0 - cc));
-  };
-  return EdgeVals<float>{val(cn), val(ct), val(2)};
+// edge1 (cell 1, side 0) or edge2 (cell n, side 1) of line L.
+__device__ __forceinline__ EdgeVals<float> edge_vals(const SweepArgs& A, int L, int side) {
+  if (!A.edges) return EdgeVals<float>{0.f, 0.f, 0.f};
+  const float* e = A.edges + (size_t)(L - 1) * 6 + side * 3;
+  return EdgeVals<float>{e[0], e[1], e[2]};
 }
 
 // The cell's value through the full wet/dry rules (cliffs.f:56-329).
 template <int DIR>
-__device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L, int o, float alpha, float ialpha) {
+__device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L, int o, float alpha, float ialpha,
+                                                       const EdgeVals<float>& eL, const EdgeVals<float>& eR) {
   const int n = A.n;
   const Phys<float>& p = A.ph;
   RawCell<float> w[7];
@@ -125,8 +114,8 @@ __device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L
       C.wet = __ldg(A.dep + q) + __ldg(A.eta + q) > p.ground;
     }
   }
-  C.eL = o == 1 ? edge_vals<DIR>(A, A.feedA, L) : EdgeVals<float>{0.f, 0.f, 0.f};
-  C.eR = o == n ? edge_vals<DIR>(A, A.feedB, L) : EdgeVals<float>{0.f, 0.f, 0.f};
+  C.eL = eL;
+  C.eR = eR;
   C.inv_dx1 = A.inv_dx1 * ialpha;
   C.inv_dxn1 = A.inv_dxn1 * ialpha;
   C.scl1 = A.scl ? A.scl[0] : 0.f;
@@ -151,9 +140,53 @@ __device__ __forceinline__ void enqueue(const SweepArgs& A, bool want, uint32_t 
 
 constexpr int kCellsPerThread = 4;
 
+// One listed cell through the full rules, written with its max-wave update.
 template <int DIR>
+__device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
+  const int n = A.n;
+  const int L = (int)(ent / (uint32_t)n) + 1;
+  const int o = (int)(ent % (uint32_t)n) + 1;
+  float alpha = 1.f, ialpha = 1.f;
+  if (DIR == 0 && A.lscale != nullptr) {
+    const float2 s = A.lscale[L - 1];
+    alpha = s.x;
+    ialpha = s.y;
+  }
+  const size_t q = cidx<DIR>(L, o, A.pitch);
+  // every global read this cell needs goes out before the compute
+  float hm = 0.f, vm = 0.f;
+  if (A.hmax) {
+    hm = A.hmax[q];
+    vm = A.velmax[q];
+  }
+  const EdgeVals<float> eL = o == 1 ? edge_vals(A, L, 0) : EdgeVals<float>{0.f, 0.f, 0.f};
+  const EdgeVals<float> eR = o == n ? edge_vals(A, L, 1) : EdgeVals<float>{0.f, 0.f, 0.f};
+  const OutCell<float> r = general_path<DIR>(A, L, o, alpha, ialpha, eL, eR);
+  const float xo = DIR == 0 ? r.u : r.v;
+  const float yo = DIR == 0 ? r.v : r.u;
+  A.eta_o[q] = r.eta;
+  A.xu_o[q] = xo;
+  A.yv_o[q] = yo;
+  if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
+    A.hmax[q] = fmaxf(hm, r.eta);
+    A.velmax[q] = fmaxf(vm, xo * xo + yo * yo);
+  }
+  if (!isfinite(r.eta + xo + yo)) atomicOr(A.status, ST_NAN);
+}
+
+// LOCAL: the block finishes its own listed cells after its fast cells (a
+// block-local list in shared memory); otherwise they go to the global
+// worklist for general_kernel.
+template <int DIR, bool LOCAL>
 __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *A.count_next = 0u;
+  __shared__ uint32_t s_list[LOCAL ? 256 * 4 : 1];
+  __shared__ unsigned s_n;
+  if (LOCAL) {
+    if (threadIdx.x == 0) s_n = 0u;
+    __syncthreads();
+  } else if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    *A.count_next = 0u;
+  }
   const int lane = threadIdx.x & 31;
   const int n = A.n;
   int L, i0;  // line, first position (1-based)
@@ -280,20 +313,42 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
         oe[r] = o.eta;
         ou[r] = o.u;
         ov[r] = o.v;
+      } else if ((k == 1 && wet[w] && wet[w + 1]) || (k == n && wet[w - 1] && wet[w])) {
+        // line end next to a wet cell: no flooding reaches it; the open or
+        // forced edge update (cliffs.f:287-329), or the cell as it is
+        const EdgeVals<float> ev = edge_vals(A, L, k == 1 ? 0 : 1);
+        if (ev.eta + d[w] > p.ground) {
+          const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
+          float cn;
+          if (k == 1) {
+            const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
+            edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], oe[r]);
+          } else {
+            const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
+            edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r], oe[r]);
+          }
+        }
       } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
         need |= 1u << r;
       }
       // else: dry, zero state: unchanged whether or not the line holds water
     }
   }
+  if (LOCAL) {
 #pragma unroll
-  for (int r = 0; r < kCellsPerThread; ++r)
-    enqueue(A, active && ((need >> r) & 1u), (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1));
-  if (!active) return;
+    for (int r = 0; r < kCellsPerThread; ++r)
+      if (active && ((need >> r) & 1u))
+        s_list[atomicAdd(&s_n, 1u)] = (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1);
+  } else {
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r)
+      enqueue(A, active && ((need >> r) & 1u), (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1));
+  }
   bool bad = false;
   float xo[kCellsPerThread], yo[kCellsPerThread];
 #pragma unroll
   for (int r = 0; r < kCellsPerThread; ++r) {
+    if (!active) break;
     xo[r] = DIR == 0 ? ou[r] : ov[r];
     yo[r] = DIR == 0 ? ov[r] : ou[r];
     const bool done = i0 + r <= n && !((need >> r) & 1u);
@@ -303,7 +358,9 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
       vm[r] = fmaxf(vm[r], xo[r] * xo[r] + yo[r] * yo[r]);
     }
   }
-  if (DIR == 0) {
+  if (!active) {
+    // nothing to store
+  } else if (DIR == 0) {
     // whole float4s: the row padding beyond nx takes the values of no cell
     *reinterpret_cast<float4*>(A.eta_o + q0) = make_float4(oe[0], oe[1], oe[2], oe[3]);
     *reinterpret_cast<float4*>(A.xu_o + q0) = make_float4(xo[0], xo[1], xo[2], xo[3]);
@@ -328,35 +385,47 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     }
   }
   if (bad) atomicOr(A.status, ST_NAN);
+  if (LOCAL) {
+    __syncthreads();  // the block's fast values are stored; its listed cells overwrite theirs
+    const unsigned cnt = s_n;
+    for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) general_store<DIR>(A, s_list[t]);
+  }
 }
 
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
 template <int DIR>
 __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {
   const uint32_t cnt = *A.count;
-  const int n = A.n;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
-    const uint32_t ent = A.list[t];
-    const int L = (int)(ent / (uint32_t)n) + 1;
-    const int o = (int)(ent % (uint32_t)n) + 1;
-    float alpha = 1.f, ialpha = 1.f;
-    if (DIR == 0 && A.lscale != nullptr) {
-      const float2 s = A.lscale[L - 1];
-      alpha = s.x;
-      ialpha = s.y;
+    general_store<DIR>(A, A.list[t]);
+  }
+}
+
+// Forcing at the line ends of one sweep for the current step: edge1/edge2
+// lerped from the boundary records in FP64 (cliffs_main.f:318-324 for the
+// x-sweep, 333-339 for the y-sweep), stored as 6 floats per line.  recA/recB
+// are the records of the low and high edge, (len,3,nt); irec is 1-based with
+// tinput(irec-1) <= t < tinput(irec); cc the weight of record irec-1.  cn is
+// the normal velocity component (iu-1 in the reference), ct the tangential.
+__global__ void edges_kernel(int nlines, int len, const double* __restrict__ recA, const double* __restrict__ recB,
+                             int irec, double cc, int cn, int ct, float* out) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nlines) return;
+  const size_t r0 = (size_t)(irec - 2) * 3 * (size_t)len;
+  const size_t r1 = (size_t)(irec - 1) * 3 * (size_t)len;
+  const int comp[3] = {cn, ct, 2};
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const double* F = side == 0 ? recA : recB;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float v = 0.f;
+      if (F) {
+        const size_t b = (size_t)L + (size_t)comp[k] * (size_t)len;
+        v = (float)(F[b + r0] * cc + F[b + r1] * (1.0 - cc));
+      }
+      out[(size_t)L * 6 + side * 3 + k] = v;
     }
-    const OutCell<float> r = general_path<DIR>(A, L, o, alpha, ialpha);
-    const size_t q = cidx<DIR>(L, o, A.pitch);
-    const float xo = DIR == 0 ? r.u : r.v;
-    const float yo = DIR == 0 ? r.v : r.u;
-    A.eta_o[q] = r.eta;
-    A.xu_o[q] = xo;
-    A.yv_o[q] = yo;
-    if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
-      A.hmax[q] = fmaxf(A.hmax[q], r.eta);
-      A.velmax[q] = fmaxf(A.velmax[q], xo * xo + yo * yo);
-    }
-    if (!isfinite(r.eta + xo + yo)) atomicOr(A.status, ST_NAN);
   }
 }
 
