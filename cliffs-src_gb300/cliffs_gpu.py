@@ -82,6 +82,7 @@ SIGNATURES = {
     "cliffs_gpu_profile": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_profile_read": ([_V, _dp, ctypes.POINTER(ctypes.c_int64), _dp,
                                  ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
     "cliffs_gpu_sweep_noalloc": ([_I, _I, _I, _I] + [_V] * 7 + [_D] * 5 + [_V], ctypes.c_int),
@@ -335,6 +336,12 @@ class GpuGrid:
         _chk(self.L.cliffs_gpu_profile_read(self.h, ctypes.byref(xm), ctypes.byref(xn),
                                             ctypes.byref(ym), ctypes.byref(yn)), "profile_read")
         return dict(x_ms=xm.value, x_n=xn.value, y_ms=ym.value, y_n=yn.value)
+
+    def launches(self):
+        """Kernels this context has launched so far."""
+        n = ctypes.c_int64()
+        _chk(self.L.cliffs_gpu_launch_count(self.h, ctypes.byref(n)), "launch_count")
+        return int(n.value)
 
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")

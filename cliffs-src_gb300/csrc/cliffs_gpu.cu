@@ -48,9 +48,11 @@ struct cliffs_ctx {
   double ground = 0, crough = 0, dt = 0, celmin = 0;
   cudaStream_t own = nullptr, stream = nullptr;
   float* dep = nullptr;
-  float *eta[2] = {nullptr, nullptr}, *xu[2] = {nullptr, nullptr}, *yv[2] = {nullptr, nullptr};
+  // surface state (eta where dep >= 0, water depth where dep < 0), u, v; ping-pong
+  float *srf[2] = {nullptr, nullptr}, *xu[2] = {nullptr, nullptr}, *yv[2] = {nullptr, nullptr};
   float *hmax = nullptr, *velmax = nullptr;
   int cur = 0;
+  int64_t launches = 0;  // kernels this context has launched
   float4 *geo_x = nullptr, *geo_y = nullptr;
   float* scl_y = nullptr;
   float2* lscale = nullptr;
@@ -98,13 +100,13 @@ int dalloc(T** p, size_t n) {
 __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict__ src,
                              int src_is_celerity, const double* __restrict__ xv,
                              const double* __restrict__ yvv, const float* __restrict__ dep,
-                             float* eta, float* xu, float* yv, double ground, double g) {
+                             float* srf, float* xu, float* yv, double ground, double g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= pitch || j >= ny) return;
   const size_t q = (size_t)j * pitch + i;
   if (i >= nx) {
-    eta[q] = 0.f;
+    srf[q] = 0.f;
     xu[q] = 0.f;
     yv[q] = 0.f;
     return;
@@ -119,7 +121,7 @@ __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict
     // celerity transform of cliffs_main.f:218-227 expressed on H
     H = src[s] <= ground ? 0.0 : src[s];
   }
-  eta[q] = (float)(H - d);
+  srf[q] = (float)(d < 0 ? H : H - d);  // surface state: H on land, eta at sea
   xu[q] = xv ? (float)xv[s] : 0.f;
   yv[q] = yvv ? (float)yvv[s] : 0.f;
 }
@@ -135,14 +137,14 @@ __global__ void k_reset_max(int nx, int ny, int pitch, const float* __restrict__
 }
 
 __global__ void k_download(int nx, int ny, int pitch, const float* __restrict__ dep,
-                           const float* __restrict__ eta, const float* __restrict__ xu,
+                           const float* __restrict__ srf, const float* __restrict__ xu,
                            const float* __restrict__ yv, double* cel, double* xo, double* yo,
                            double g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= nx || j >= ny) return;
   const size_t q = (size_t)j * pitch + i, s = (size_t)j * nx + i;
-  const double H = (double)dep[q] + (double)eta[q];
+  const double H = depth_of((double)srf[q], (double)dep[q]);
   if (cel) cel[s] = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
   if (xo) xo[s] = xu[q];
   if (yo) yo[s] = yv[q];
@@ -180,7 +182,7 @@ __global__ void k_maxwave_out(int nx, int ny, int pitch, const float* __restrict
 
 // output_sea_state.f:18-33
 __global__ void k_sea_state(int nxs, int nys, int pitch, int lonsub, int latsub,
-                            const float* __restrict__ dep, const float* __restrict__ eta,
+                            const float* __restrict__ dep, const float* __restrict__ srf,
                             const float* __restrict__ xu, const float* __restrict__ yv,
                             float ground, float* h, float* u, float* v) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -188,8 +190,8 @@ __global__ void k_sea_state(int nxs, int nys, int pitch, int lonsub, int latsub,
   if (i >= nxs || j >= nys) return;
   const size_t q = (size_t)(latsub * j) * pitch + (size_t)(lonsub * i);
   const size_t s = (size_t)j * nxs + i;
-  if (dep[q] + eta[q] > ground) {
-    h[s] = eta[q];
+  if (depth_of(srf[q], dep[q]) > ground) {
+    h[s] = eta_of(srf[q], dep[q]);
     u[s] = xu[q];
     v[s] = yv[q];
   } else {
@@ -201,14 +203,14 @@ __global__ void k_sea_state(int nxs, int nys, int pitch, int lonsub, int latsub,
 
 // output_gages.f:18-29
 __global__ void k_gauges(int n, const int32_t* __restrict__ I, const int32_t* __restrict__ J,
-                         int pitch, const float* __restrict__ dep, const float* __restrict__ eta,
+                         int pitch, const float* __restrict__ dep, const float* __restrict__ srf,
                          const float* __restrict__ xu, const float* __restrict__ yv, float ground,
                          double* out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const size_t q = (size_t)(J[k] - 1) * pitch + (size_t)(I[k] - 1);
-  const float H = dep[q] + eta[q];
-  out[k] = H > ground ? (double)eta[q] : (double)kNan4;
+  const float H = depth_of(srf[q], dep[q]);
+  out[k] = H > ground ? (double)eta_of(srf[q], dep[q]) : (double)kNan4;
   out[n + k] = xu[q];
   out[2 * n + k] = yv[q];
 }
@@ -216,7 +218,7 @@ __global__ void k_gauges(int n, const int32_t* __restrict__ I, const int32_t* __
 // Runup measures: per-block partials of (max runup, its index, wetted land
 // count, wet count) into scratch, finished on the host.
 __global__ void k_runup(int nx, int ny, int pitch, const float* __restrict__ dep,
-                        const float* __restrict__ eta, const float* __restrict__ hmax,
+                        const float* __restrict__ srf, const float* __restrict__ hmax,
                         float ground, double* part) {
   __shared__ double s_best[256];
   __shared__ long long s_idx[256], s_land[256], s_wet[256];
@@ -229,7 +231,7 @@ __global__ void k_runup(int nx, int ny, int pitch, const float* __restrict__ dep
     const int j = (int)(c / nx), i = (int)(c - (long long)j * nx);
     const size_t q = (size_t)j * pitch + i;
     const float d = dep[q];
-    if (d + eta[q] > ground) ++nwet;
+    if (depth_of(srf[q], d) > ground) ++nwet;
     if (d < 0.f && d + hmax[q] > ground) {
       ++nland;
       if (-d > best) {
@@ -266,7 +268,7 @@ __global__ void k_runup(int nx, int ny, int pitch, const float* __restrict__ dep
 // Arrival test of feed_children_grid.f:26-46 over parent columns ii1..ii2 and
 // rows kk1..kk2 (1-based).
 __global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
-                          const float* __restrict__ dep, const float* __restrict__ eta,
+                          const float* __restrict__ dep, const float* __restrict__ srf,
                           const float* __restrict__ xu, const float* __restrict__ yv,
                           double hmin, double cuke, double g, int* flag) {
   const int ni = ii2 - ii1 + 1, nk = kk2 - kk1 + 1;
@@ -279,7 +281,7 @@ __global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
     const size_t q = (size_t)(k - 1) * pitch + (size_t)(i - 1);
     const double d = dep[q];
     if (d > hmin) {
-      const double H = d + (double)eta[q];
+      const double H = depth_of((double)srf[q], d);
       const double c2g = fabs(H);  // cel**2/grav
       if (fabs(c2g - d) > tenth * cuke) hit = true;
       const double cel = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
@@ -291,12 +293,12 @@ __global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
 
 // Edge records of feed_children_grid.f:197-325; one thread per child edge node.
 __device__ __forceinline__ void feed_clm(int i, int k, int pitch, const float* dep,
-                                         const float* eta, const float* xu, const float* yv,
+                                         const float* srf, const float* xu, const float* yv,
                                          double cc, double hmin, double g, double out[3]) {
   const size_t q = (size_t)(k - 1) * pitch + (size_t)(i - 1);
   const double d = dep[q];
   if (d > hmin) {
-    const double H = d + (double)eta[q];
+    const double H = depth_of((double)srf[q], d);
     out[0] = cc * (double)xu[q];
     out[1] = cc * (double)yv[q];
     out[2] = cc * (fabs(H) - d);
@@ -310,7 +312,7 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
                              double E_cx, double S_cy, double N_cy, const int32_t* __restrict__ WE_ny,
                              const double* __restrict__ WE_cy, const int32_t* __restrict__ SN_nx,
                              const double* __restrict__ SN_cx, int pitch, const float* __restrict__ dep,
-                             const float* __restrict__ eta, const float* __restrict__ xu,
+                             const float* __restrict__ srf, const float* __restrict__ xu,
                              const float* __restrict__ yv, double hmin, double g, double* w_out,
                              double* e_out, double* s_out, double* n_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -321,10 +323,10 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
     const int kk = WE_ny[i];
     const double w = WE_cy[i];
     double a0[3], a1[3], b0[3], b1[3];
-    feed_clm(ii, kk, pitch, dep, eta, xu, yv, cc, hmin, g, a0);
-    feed_clm(ii + 1, kk, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, a1);
-    feed_clm(ii, kk + 1, pitch, dep, eta, xu, yv, cc, hmin, g, b0);
-    feed_clm(ii + 1, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, b1);
+    feed_clm(ii, kk, pitch, dep, srf, xu, yv, cc, hmin, g, a0);
+    feed_clm(ii + 1, kk, pitch, dep, srf, xu, yv, 1 - cc, hmin, g, a1);
+    feed_clm(ii, kk + 1, pitch, dep, srf, xu, yv, cc, hmin, g, b0);
+    feed_clm(ii + 1, kk + 1, pitch, dep, srf, xu, yv, 1 - cc, hmin, g, b1);
     double* o = side == 0 ? w_out : e_out;
     for (int c = 0; c < 3; ++c) o[i + (size_t)c * nn] = (a0[c] + a1[c]) * w + (b0[c] + b1[c]) * (1 - w);
   } else if (t < 2 * nn + 2 * mm) {  // south / north: parent rows (kk, kk+1)
@@ -335,10 +337,10 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
     const int ii = SN_nx[i];
     const double w = SN_cx[i];
     double a0[3], a1[3], b0[3], b1[3];
-    feed_clm(ii, kk, pitch, dep, eta, xu, yv, cc, hmin, g, a0);
-    feed_clm(ii, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, a1);
-    feed_clm(ii + 1, kk, pitch, dep, eta, xu, yv, cc, hmin, g, b0);
-    feed_clm(ii + 1, kk + 1, pitch, dep, eta, xu, yv, 1 - cc, hmin, g, b1);
+    feed_clm(ii, kk, pitch, dep, srf, xu, yv, cc, hmin, g, a0);
+    feed_clm(ii, kk + 1, pitch, dep, srf, xu, yv, 1 - cc, hmin, g, a1);
+    feed_clm(ii + 1, kk, pitch, dep, srf, xu, yv, cc, hmin, g, b0);
+    feed_clm(ii + 1, kk + 1, pitch, dep, srf, xu, yv, 1 - cc, hmin, g, b1);
     double* o = side == 0 ? s_out : n_out;
     for (int c = 0; c < 3; ++c) o[i + (size_t)c * mm] = (a0[c] + a1[c]) * w + (b0[c] + b1[c]) * (1 - w);
   }
@@ -379,10 +381,10 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   const int s = c->cur, o = 1 - c->cur;
   A.pitch = c->pitch;
   A.dep = c->dep;
-  A.eta = c->eta[s];
+  A.srf = c->srf[s];
   A.xu = c->xu[s];
   A.yv = c->yv[s];
-  A.eta_o = c->eta[o];
+  A.srf_o = c->srf[o];
   A.xu_o = c->xu[o];
   A.yv_o = c->yv[o];
   A.hmax = fuse_max ? c->hmax : nullptr;
@@ -396,6 +398,7 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   if (fA || fB) {
     float* eb = iu == 1 ? c->edge_x : c->edge_y;
     const int nl = iu == 1 ? c->ny : c->nx;
+    ++c->launches;
     edges_kernel<<<(nl + 127) / 128, 128, 0, c->stream>>>(nl, flen, fA, fB, irec, cc, iu == 1 ? 0 : 1,
                                                           iu == 1 ? 1 : 0, eb);
     CK(cudaGetLastError());
@@ -436,10 +439,12 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   if (iu == 1) {
     const int cells = c->blk_x * kCellsPerThread;
     const dim3 grid((A.n + cells - 1) / cells, A.nlines);
+    ++c->launches;
     fast_kernel<0, true><<<grid, c->blk_x, 0, c->stream>>>(A);
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
+    ++c->launches;
     fast_kernel<1, true><<<grid, 32 * c->warps_y, 0, c->stream>>>(A);
   }
   CK(cudaGetLastError());
@@ -452,14 +457,15 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   return CLIFFS_OK;
 }
 
-__global__ void k_maxwave_update(int nx, int ny, int pitch, const float* __restrict__ eta,
-                                 const float* __restrict__ xu, const float* __restrict__ yv,
-                                 float* hmax, float* velmax) {
+__global__ void k_maxwave_update(int nx, int ny, int pitch, const float* __restrict__ dep,
+                                 const float* __restrict__ srf, const float* __restrict__ xu,
+                                 const float* __restrict__ yv, float* hmax, float* velmax) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= nx || j >= ny) return;
   const size_t q = (size_t)j * pitch + i;
-  if (eta[q] > hmax[q]) hmax[q] = eta[q];
+  const float eta = eta_of(srf[q], dep[q]);
+  if (eta > hmax[q]) hmax[q] = eta;
   const float s = xu[q] * xu[q] + yv[q] * yv[q];
   if (s > velmax[q]) velmax[q] = s;
 }
@@ -551,7 +557,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   };
   if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
   c->stream = c->own;
-  if (dalloc(&c->dep, cells) || dalloc(&c->eta[0], cells) || dalloc(&c->eta[1], cells) ||
+  if (dalloc(&c->dep, cells) || dalloc(&c->srf[0], cells) || dalloc(&c->srf[1], cells) ||
       dalloc(&c->xu[0], cells) || dalloc(&c->xu[1], cells) || dalloc(&c->yv[0], cells) ||
       dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
       dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
@@ -625,7 +631,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   if (!c) return;
   cudaStreamSynchronize(c->stream);
   flush_profile(c);
-  void* ptrs[] = {c->dep, c->eta[0], c->eta[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
+  void* ptrs[] = {c->dep, c->srf[0], c->srf[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
                   c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
                   c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y};
@@ -660,11 +666,13 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
   if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r) {
     c->cur = 0;
+    ++c->launches;
     k_init_state<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(
-        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, c->eta[0], c->xu[0], c->yv[0], c->ground, kGrav);
+        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, c->srf[0], c->xu[0], c->yv[0], c->ground, kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
   if (!r && reset_max) {
+    ++c->launches;
     k_reset_max<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
@@ -696,7 +704,8 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   int r = CLIFFS_OK;
   if (dalloc(&a, n) || dalloc(&b, n) || dalloc(&e, n)) r = CLIFFS_ERR_NOMEM;
   if (!r) {
-    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur],
+    ++c->launches;
+    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
                                                           c->xu[c->cur], c->yv[c->cur], a, b, e, kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
@@ -867,7 +876,8 @@ int cliffs_gpu_set_edges(cliffs_ctx* c, const double* edge1, const double* edge2
 int cliffs_gpu_maxwave_update(cliffs_ctx* c) {
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
-  k_maxwave_update<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->eta[c->cur],
+  ++c->launches;
+  k_maxwave_update<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
                                                               c->xu[c->cur], c->yv[c->cur], c->hmax, c->velmax);
   CK(cudaGetLastError());
   return CLIFFS_OK;
@@ -880,6 +890,7 @@ int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
   int r = CLIFFS_OK;
   if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
   if (!r) {
+    ++c->launches;
     k_maxwave_out<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax,
                                                              c->velmax, (float)c->ground, a, b);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
@@ -899,6 +910,7 @@ int cliffs_gpu_get_max_raw(cliffs_ctx* c, double* hm, double* vm) {
   int r = CLIFFS_OK;
   if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
   if (!r) {
+    ++c->launches;
     k_max_raw<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax,
                                                          a, b, kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
@@ -920,7 +932,8 @@ int cliffs_gpu_get_sea_state(cliffs_ctx* c, int32_t lonsub, int32_t latsub, floa
   if (dalloc(&a, 3 * n)) return CLIFFS_ERR_NOMEM;
   int r = CLIFFS_OK;
   const int s = c->cur;
-  k_sea_state<<<grid2(nxs, nys), 128, 0, c->stream>>>(nxs, nys, c->pitch, lonsub, latsub, c->dep, c->eta[s],
+  ++c->launches;
+  k_sea_state<<<grid2(nxs, nys), 128, 0, c->stream>>>(nxs, nys, c->pitch, lonsub, latsub, c->dep, c->srf[s],
                                                       c->xu[s], c->yv[s], (float)c->ground, a, a + n, a + 2 * n);
   if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && (cudaMemcpyAsync(h, a, n * 4, cudaMemcpyDeviceToHost, c->stream) ||
@@ -951,7 +964,8 @@ int cliffs_gpu_get_gauges(cliffs_ctx* c, int32_t n, const int32_t* I, const int3
     r = CLIFFS_ERR_CUDA;
   if (!r) {
     const int s = c->cur;
-    k_gauges<<<(n + 127) / 128, 128, 0, c->stream>>>(n, dij, dij + n, c->pitch, c->dep, c->eta[s], c->xu[s],
+    ++c->launches;
+    k_gauges<<<(n + 127) / 128, 128, 0, c->stream>>>(n, dij, dij + n, c->pitch, c->dep, c->srf[s], c->xu[s],
                                                      c->yv[s], (float)c->ground, out);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
@@ -975,7 +989,8 @@ int cliffs_gpu_runup(cliffs_ctx* c, cliffs_runup* o) {
     if (dalloc(&c->red, 4 * (size_t)blocks)) return CLIFFS_ERR_NOMEM;
     c->red_cap = 4 * blocks;
   }
-  k_runup<<<blocks, 256, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->eta[c->cur], c->hmax,
+  ++c->launches;
+  k_runup<<<blocks, 256, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur], c->hmax,
                                          (float)c->ground, c->red);
   CK(cudaGetLastError());
   std::vector<double> h(4 * (size_t)blocks);
@@ -1045,7 +1060,8 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
     k2 += 1;
     i2 += 1;
     CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-    k_arrival<<<152, 256, 0, c->stream>>>(i1, i2, k1, k2, c->pitch, c->dep, c->eta[st], c->xu[st], c->yv[st],
+    ++c->launches;
+    k_arrival<<<152, 256, 0, c->stream>>>(i1, i2, k1, k2, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st],
                                           c->ground, cuke, kGrav, c->d_flag);
     CK(cudaGetLastError());
     int f = 0;
@@ -1060,9 +1076,10 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
   if (dalloc(&buf, 6 * (size_t)(mm + nn))) return CLIFFS_ERR_NOMEM;
   double *dw = buf, *de = buf + 3 * (size_t)nn, *ds = buf + 6 * (size_t)nn, *dn = ds + 3 * (size_t)mm;
   const int threads = 2 * (mm + nn);
+  ++c->launches;
   k_feed_child<<<(threads + 127) / 128, 128, 0, c->stream>>>(
       mm, nn, n.d.W_nx, n.d.E_nx, n.d.S_ny, n.d.N_ny, n.d.W_cx, n.d.E_cx, n.d.S_cy, n.d.N_cy, n.WE_ny, n.WE_cy,
-      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->eta[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn);
+      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn);
   int r = CLIFFS_OK;
   if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && (cudaMemcpyAsync(w, dw, 3 * nn * 8, cudaMemcpyDeviceToHost, c->stream) ||
@@ -1108,6 +1125,12 @@ int cliffs_gpu_profile_read(cliffs_ctx* c, double* x_ms, int64_t* x_n, double* y
   if (x_n) *x_n = c->prof_n[0];
   if (y_ms) *y_ms = c->prof_n[1] ? c->prof_ms[1] / c->prof_n[1] : 0.0;
   if (y_n) *y_n = c->prof_n[1];
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_launch_count(cliffs_ctx* c, int64_t* n) {
+  if (!c || !n) return CLIFFS_ERR_ARG;
+  *n = c->launches;
   return CLIFFS_OK;
 }
 
@@ -1166,7 +1189,7 @@ static int noalloc_scratch(NoAllocScratch* out) {
 }
 
 int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, const float* dep,
-                             const float* eta, const float* xvel, const float* yvel, float* eta_out,
+                             const float* srf, const float* xvel, const float* yvel, float* srf_out,
                              float* xvel_out, float* yvel_out, double dx, double dy, double ground,
                              double crough, double dt, void* stream) {
   if (iu != 1 && iu != 2) return CLIFFS_ERR_ARG;
@@ -1174,7 +1197,7 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
   if ((iu == 1 && nx <= 2) || (iu == 2 && ny <= 2)) return CLIFFS_ERR_ARG;
   if ((int64_t)nx * (int64_t)ny > kNoAllocCells) return CLIFFS_ERR_ARG;
   if (pitch < nx || pitch % 4 != 0) return CLIFFS_ERR_ARG;
-  const void* ptrs[] = {dep, eta, xvel, yvel, eta_out, xvel_out, yvel_out};
+  const void* ptrs[] = {dep, srf, xvel, yvel, srf_out, xvel_out, yvel_out};
   for (const void* q : ptrs)
     if (!q || ((uintptr_t)q % 16) != 0) return CLIFFS_ERR_ARG;
   if (!(dt > 0) || !(ground > 0) || crough < 0) return CLIFFS_ERR_ARG;
@@ -1186,10 +1209,10 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
   SweepArgs A{};
   A.pitch = pitch;
   A.dep = dep;
-  A.eta = eta;
+  A.srf = srf;
   A.xu = xvel;
   A.yv = yvel;
-  A.eta_o = eta_out;
+  A.srf_o = srf_out;
   A.xu_o = xvel_out;
   A.yv_o = yvel_out;
   A.hmax = nullptr;

@@ -1,15 +1,13 @@
-// march.cuh -- streaming VTCS-2 line update (one line per thread).
+// march.cuh -- the VTCS-2 update of one line cell, in the forms the sweep
+// kernels use.
 //
-// Restates cliffs.f:17-346 (subroutine cliffs) for a single grid line as a
-// pipeline that consumes raw cell k and emits the final value of cell k-3:
-//
-//   stage A (cell k)    derive H = d + eta and land = H <= ground
-//   stage B (cell k-1)  flooding: R(k) and L(k-1) decide whether a dry cell is
-//                       taken into the wet segment (cliffs.f:74-111); the
-//                       flood-modified state of k-1 becomes final
-//   stage C (cell k-2)  VTCS-2 interior update (cliffs.f:175-262) or the
-//                       open/forced edge update (cliffs.f:287-329)
-//   stage D (cell k-3)  shoreline angle limiter (cliffs.f:264-285) and output
+// Restates cliffs.f:17-346 (subroutine cliffs) cell by cell:
+//   interior_update     VTCS-2 interior update (cliffs.f:175-262)
+//   edge_left/right     open or forced line ends (cliffs.f:287-329)
+//   general_cell        the whole of cliffs.f:56-329 for one cell: flooding
+//                       (cliffs.f:74-111), newland (118-122), mirror ghosts
+//                       (137-152), the update, the shoreline angle limiter
+//                       (264-285)
 //
 // The serial segment scan of the reference is replaced by per-cell rules that
 // depend on cells i-1..i+1 only; the oracle's orc_line_local proves them
@@ -18,9 +16,19 @@
 // the mirror ghost of itself (cliffs.f:137-152).  A line without any wet cell
 // is left untouched (cliffs.f:113); the caller supplies that line flag.
 //
-// State is carried as surface elevation eta (not celerity) so that FP32 keeps
-// ~1e-7 m resolution in deep water: the hydrostatic balance
-// (1/8)(e2+ej)(p2-pj) - g(d2-dj) is rewritten with c^2 = g(d+eta) as
+// Stored state.  The reference carries celerity c = sqrt(gH) in FP64.  Here
+// the surface is carried as one FP32 number per cell, the surface state s:
+//   s = eta           where the bed is below datum (d >= 0, the sea),
+//   s = H = d + eta   where it is above (d < 0, land).
+// At sea eta keeps ~1e-7 m resolution whatever the depth, where c or H would
+// lose it to the depth.  On land eta = H + |d| would keep only ulp(|d|) of a
+// run-up film a few millimetres thick, and the rounding of every step's
+// increment to that ulp is what drives an FP32 run-down away from FP64; H keeps
+// full relative precision in the film.  Both forms move by the same increment
+// (eta and H differ by the constant d), so the update is written once.
+//
+// The hydrostatic balance (1/8)(e2+ej)(p2-pj) - g(d2-dj) is rewritten with
+// c^2 = g(d+eta) as
 //   g(eta2-eta1) + (u1+u2)(c2-c1) + (u1+u2+c1+c2)(u2-u1)/2
 // which is exact in real arithmetic and free of the catastrophic cancellation
 // of the celerity form.  A negative celerity (a cell drying out) is kept as a
@@ -98,23 +106,19 @@ struct Geo {
   R scl;             // metric term (zeta in the y-sweep, 0 in the x-sweep)
 };
 
-// One cell of the pipeline ring.
+// Surface state s <-> (eta, H) for bed elevation -d (see the file header).
 template <typename R>
-struct RCell {
-  R d, eta, u, v;      // raw input (u normal, v tangential)
-  R H;                 // d + eta
-  R c, ef, uf, vf;     // flood-modified celerity, eta, u, v
-  R cn, un, vn, en;    // updated celerity, u, v, eta
-  unsigned fl;         // flag bits below
-};
-
-enum : unsigned {
-  F_PRESENT = 1u,  // 1 <= k <= n
-  F_LAND = 2u,     // h <= celmin
-  F_R = 4u,        // flooded from the left neighbour (cliffs.f:77-82)
-  F_L = 8u,        // flooded from the right neighbour (cliffs.f:92-98)
-  F_EW = 16u,      // wet or flooded (not newland)
-};
+CL_HD R eta_of(R s, R d) {
+  return d < R(0) ? s - d : s;
+}
+template <typename R>
+CL_HD R depth_of(R s, R d) {
+  return d < R(0) ? s : d + s;
+}
+template <typename R>
+CL_HD R state_from_depth(R H, R d) {
+  return d < R(0) ? H : H - d;
+}
 
 template <typename R>
 struct EdgeVals {
@@ -123,7 +127,7 @@ struct EdgeVals {
 
 template <typename R>
 struct OutCell {
-  R eta, u, v;  // final eta, normal and tangential velocity
+  R s, u, v;  // final surface state, normal and tangential velocity
 };
 
 template <typename R>
@@ -137,32 +141,34 @@ CL_HD void face_flux(R ul, R cl, R el, R ur, R cr, R er, const Phys<R>& p,
   FQ = gde - Udc + R(0.5) * (U - C) * du;
 }
 
-// H from celerity with the sign of c kept: H = c|c|/g.
+// Surface state of celerity c (sign kept: H = c|c|/g).
 template <typename R>
-CL_HD R eta_from_c(R c, R d, const Phys<R>& p) {
-  return c * (c < R(0) ? -c : c) * p.ginv - d;
+CL_HD R state_from_c(R c, R d, const Phys<R>& p) {
+  return state_from_depth(c * (c < R(0) ? -c : c) * p.ginv, d);
 }
 
-// New eta after celerity c0 (with eta e0) moved by dc: exact increment form
-// when both celerities are positive.
-template <typename R>
-CL_HD R eta_step(R c0, R e0, R dc, R d, const Phys<R>& p) {
-  const R c1 = c0 + dc;
-  if (c0 > R(0) && c1 > R(0)) return e0 + dc * (R(2) * c0 + dc) * p.ginv;
-  return eta_from_c(c1, d, p);
-}
-
-// State of one cell as the interior update sees it (after flooding).
+// State of one cell as the interior update sees it (after flooding).  e and H
+// are both given; the one the cell stores (eta at sea, H on land) is exact.
 template <typename R>
 struct CellState {
   R u, c, e, d, v, H;  // normal velocity, celerity, eta, depth, tangential, H
 };
 
+// New surface state after the celerity c0 of cell j moved by dc: the exact
+// increment dH = dc(2c0+dc)/g added to the stored form when both celerities
+// are positive.
+template <typename R>
+CL_HD R state_step(const CellState<R>& j, R dc, const Phys<R>& p) {
+  const R c0 = j.c, c1 = c0 + dc;
+  if (c0 > R(0) && c1 > R(0)) return (j.d < R(0) ? j.H : j.e) + dc * (R(2) * c0 + dc) * p.ginv;
+  return state_from_c(c1, j.d, p);
+}
+
 struct NoFlux {};
 
 // VTCS-2 interior update of cell j between real neighbours a (left) and b
 // (right), cliffs.f:200-262, in the eta form.  FPl/FQl, FPr/FQr are the face
-// fluxes (a,j) and (j,b).  Returns the new (eta, u, v); *cn gets the new
+// fluxes (a,j) and (j,b).  Returns the new (s, u, v); *cn gets the new
 // celerity.
 template <typename R>
 CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, const CellState<R>& b,
@@ -197,7 +203,7 @@ CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, c
   const R dc = R(0.25) * (dP - dQ);
   *cn_out = cj + dc;
   o.u = uj + R(0.5) * (dP + dQ);
-  o.eta = eta_step(cj, j.e, dc, dj, p);
+  o.s = state_step(j, dc, p);
   return o;
 }
 
@@ -205,7 +211,7 @@ CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, c
 // and B cell 2 (flood-modified), both wet or flooded.
 template <typename R>
 CL_HD void edge_left(const CellState<R>& C, const CellState<R>& B, const EdgeVals<R>& e, R inv_dx1, R scl1,
-                     const Phys<R>& p, R& cn, R& un, R& vn, R& en) {
+                     const Phys<R>& p, R& cn, R& un, R& vn, R& sn) {
   R FP, FQ;
   face_flux(C.u, C.c, C.e, B.u, B.c, B.e, p, FP, FQ);
   const R sphr = R(8) * C.c * C.u * scl1;
@@ -216,14 +222,14 @@ CL_HD void edge_left(const CellState<R>& C, const CellState<R>& B, const EdgeVal
   const R dc = R(0.25) * (dP - dQ);
   cn = C.c + dc;
   un = C.u + R(0.5) * (dP + dQ);
-  en = eta_step(C.c, C.e, dc, C.d, p);
+  sn = state_step(C, dc, p);
 }
 
 // Open / forced edge update of line cell n (cliffs.f:309-329): D is cell n-1,
 // C cell n.
 template <typename R>
 CL_HD void edge_right(const CellState<R>& D, const CellState<R>& C, const EdgeVals<R>& e, R inv_dxn1, R scln,
-                      const Phys<R>& p, R& cn, R& un, R& vn, R& en) {
+                      const Phys<R>& p, R& cn, R& un, R& vn, R& sn) {
   R FP, FQ;
   face_flux(D.u, D.c, D.e, C.u, C.c, C.e, p, FP, FQ);
   const R sphr = R(8) * C.c * C.u * scln;
@@ -234,13 +240,13 @@ CL_HD void edge_right(const CellState<R>& D, const CellState<R>& C, const EdgeVa
   const R dc = R(0.25) * (dP - dQ);
   cn = C.c + dc;
   un = C.u + R(0.5) * (dP + dQ);
-  en = eta_step(C.c, C.e, dc, C.d, p);
+  sn = state_step(C, dc, p);
 }
 
 // Raw input of one line cell; present iff 1 <= position <= n.
 template <typename R>
 struct RawCell {
-  R d, e, u, v;
+  R d, s, u, v;  // depth, surface state, normal and tangential velocity
   bool present;
 };
 
@@ -266,19 +272,20 @@ template <typename R>
 CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L, const Geo<R> geo[3],
                               const Phys<R>& p) {
   bool land[7], Rf[7], Lf[7], ew[7];
-  R H[7];
+  R H[7], E[7];
 #pragma unroll
   for (int t = 0; t < 7; ++t) {
-    H[t] = w[t].d + w[t].e;
+    H[t] = depth_of(w[t].s, w[t].d);
+    E[t] = eta_of(w[t].s, w[t].d);
     land[t] = !w[t].present || H[t] <= p.ground;
     Rf[t] = Lf[t] = false;
   }
 #pragma unroll
   for (int t = 1; t <= 5; ++t) {
     if (w[t].present && land[t]) {
-      Rf[t] = w[t - 1].present && !land[t - 1] && w[t - 1].u >= R(0) && (w[t - 1].e + w[t].d > p.ground);
+      Rf[t] = w[t - 1].present && !land[t - 1] && w[t - 1].u >= R(0) && (E[t - 1] + w[t].d > p.ground);
       Lf[t] = !Rf[t] && w[t + 1].present && !land[t + 1] && w[t + 1].u <= R(0) &&
-              (w[t + 1].e + w[t].d > p.ground);
+              (E[t + 1] + w[t].d > p.ground);
     }
   }
   CellState<R> fm[7];
@@ -289,18 +296,18 @@ CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L,
       const int s = Rf[t] ? t - 1 : t + 1;
       fm[t] = CellState<R>{w[s].u, p.celmin, p.ground - w[t].d, w[t].d, w[s].v, p.ground};
     } else {
-      fm[t] = CellState<R>{w[t].u, fsqrt_pos(p.g * (H[t] > p.ground ? H[t] : p.ground)), w[t].e, w[t].d, w[t].v,
+      fm[t] = CellState<R>{w[t].u, fsqrt_pos(p.g * (H[t] > p.ground ? H[t] : p.ground)), E[t], w[t].d, w[t].v,
                            H[t]};
     }
   }
   OutCell<R> out;
   if (!ew[3]) {
     if (L.wet) {  // newland in a line with water: h=u=v=0 (cliffs.f:118-122)
-      out.eta = -w[3].d;
+      out.s = state_from_depth(R(0), w[3].d);
       out.u = R(0);
       out.v = R(0);
     } else {  // a line without water is left untouched (cliffs.f:113)
-      out.eta = w[3].e;
+      out.s = w[3].s;
       out.u = w[3].u;
       out.v = w[3].v;
     }
@@ -309,18 +316,18 @@ CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L,
   const int n = L.n;
   if (o == 1 || o == n) {
     // flood-modified value unless the edge condition holds
-    out.eta = fm[3].e;
+    out.s = (Rf[3] || Lf[3]) ? state_from_depth(p.ground, w[3].d) : w[3].s;
     out.u = fm[3].u;
     out.v = fm[3].v;
-    R cn, un, vn, en;
+    R cn, un, vn, sn;
     if (o == 1 && n >= 2 && ew[4] && (L.eL.eta + w[3].d > p.ground)) {
-      edge_left(fm[3], fm[4], L.eL, L.inv_dx1, L.scl1, p, cn, un, vn, en);
-      out.eta = en;
+      edge_left(fm[3], fm[4], L.eL, L.inv_dx1, L.scl1, p, cn, un, vn, sn);
+      out.s = sn;
       out.u = un;
       out.v = vn;
     } else if (o == n && n >= 2 && ew[2] && (L.eR.eta + w[3].d > p.ground)) {
-      edge_right(fm[2], fm[3], L.eR, L.inv_dxn1, L.scln, p, cn, un, vn, en);
-      out.eta = en;
+      edge_right(fm[2], fm[3], L.eR, L.inv_dxn1, L.scln, p, cn, un, vn, sn);
+      out.s = sn;
       out.u = un;
       out.v = vn;
     }
@@ -351,7 +358,7 @@ CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L,
     }
     if (p.sqr2 * cO > hj) {
       cO = hj / p.sqr2;
-      out.eta = eta_from_c(cO, w[3].d, p);
+      out.s = state_from_c(cO, w[3].d, p);
     }
     if (out.u < uj) out.u = uj;
   } else if (Rf[3] && !ew[4]) {
@@ -366,283 +373,11 @@ CL_HD OutCell<R> general_cell(const RawCell<R> w[7], int o, const LineCtx<R>& L,
     }
     if (p.sqr2 * cO > hj) {
       cO = hj / p.sqr2;
-      out.eta = eta_from_c(cO, w[3].d, p);
+      out.s = state_from_c(cO, w[3].d, p);
     }
     if (out.u > uj) out.u = uj;
   }
   return out;
 }
-
-template <typename R>
-struct LineMarch {
-  Phys<R> p;
-  int n;       // line length
-  bool wet;    // the line holds at least one wet cell (else untouched)
-  EdgeVals<R> eL, eR;
-  R inv_dx1, inv_dxn1;  // 1/dx(1), 1/dx(n-1)
-  R scl1, scln;         // scl(1), scl(n)
-  // ring: a = k, b = k-1, c = k-2, d = k-3, e = k-4
-  RCell<R> ra, rb, rc, rd, re;
-  R fpr_P, fpr_Q;  // flux at face (k-2, k-1) carried to the next update
-  bool fpr_ok;
-
-  CL_HD void init(const Phys<R>& ph, int n_, bool wet_) {
-    p = ph;
-    n = n_;
-    wet = wet_;
-    fpr_ok = false;
-    RCell<R> z{};
-    ra = rb = rc = rd = re = z;
-  }
-
-  // Push raw cell k (present iff 1 <= k <= n); returns true and fills `out`
-  // when cell k-3 lies in [1, n].  geo_m is the geometry of m = k-2.
-  CL_HD bool push(int k, R d, R eta, R u, R v, const Geo<R>& geo_m,
-                  OutCell<R>& out) {
-    // shift ring
-    re = rd;
-    rd = rc;
-    rc = rb;
-    rb = ra;
-    RCell<R>& A = ra;  // k
-    RCell<R>& B = rb;  // k-1
-    RCell<R>& C = rc;  // k-2
-    RCell<R>& D = rd;  // k-3
-    RCell<R>& E = re;  // k-4
-    // ---- stage A: cell k
-    A.fl = 0;
-    if (k >= 1 && k <= n) {
-      A.d = d;
-      A.eta = eta;
-      A.u = u;
-      A.v = v;
-      A.H = d + eta;
-      A.fl = F_PRESENT | (A.H <= p.ground ? F_LAND : 0u);
-      // R(k): flooded from the wet cell k-1 moving landward (cliffs.f:76-82)
-      if ((A.fl & F_LAND) && (B.fl & F_PRESENT) && !(B.fl & F_LAND) &&
-          B.u >= R(0) && (B.eta + A.d > p.ground))
-        A.fl |= F_R;
-    }
-    // ---- stage B: finalize cell k-1
-    if (B.fl & F_PRESENT) {
-      // L(k-1): flooded from the wet cell k moving landward (cliffs.f:89-98)
-      if ((B.fl & F_LAND) && !(B.fl & F_R) && (A.fl & F_PRESENT) &&
-          !(A.fl & F_LAND) && A.u <= R(0) && (A.eta + B.d > p.ground))
-        B.fl |= F_L;
-      if (B.fl & F_R) {
-        B.c = p.celmin;
-        B.ef = p.ground - B.d;
-        B.uf = C.u;
-        B.vf = C.v;
-        B.fl |= F_EW;
-      } else if (B.fl & F_L) {
-        B.c = p.celmin;
-        B.ef = p.ground - B.d;
-        B.uf = A.u;
-        B.vf = A.v;
-        B.fl |= F_EW;
-      } else if (!(B.fl & F_LAND)) {
-        B.c = fsqrt_pos(p.g * B.H);
-        B.ef = B.eta;
-        B.uf = B.u;
-        B.vf = B.v;
-        B.fl |= F_EW;
-      }
-    }
-    // ---- stage C: update cell m = k-2
-    const int m = k - 2;
-    bool carried = false;
-    R carP = R(0), carQ = R(0);
-    if ((C.fl & F_EW) && m >= 2 && m <= n - 1) {
-      const bool lreal = (D.fl & F_EW) != 0;
-      const bool rreal = (B.fl & F_EW) != 0;
-      const R uj = C.uf, cj = C.c, vj = C.vf, dj = C.d;
-      R FPl, FQl, FPr, FQr;
-      R ua, ca, da, va, ub, cb, db, vb;
-      if (lreal) {
-        ua = D.uf; ca = D.c; da = D.d; va = D.vf;
-        if (fpr_ok) {
-          FPl = fpr_P;
-          FQl = fpr_Q;
-        } else {
-          face_flux(ua, ca, D.ef, uj, cj, C.ef, p, FPl, FQl);
-        }
-      } else {  // mirror ghost of cell m (cliffs.f:137-144)
-        ua = -uj; ca = cj; da = dj; va = vj;
-        FPl = R(2) * cj * uj;
-        FQl = -FPl;
-      }
-      if (rreal) {
-        ub = B.uf; cb = B.c; db = B.d; vb = B.vf;
-        face_flux(uj, cj, C.ef, ub, cb, B.ef, p, FPr, FQr);
-        carried = true;
-        carP = FPr;
-        carQ = FQr;
-      } else {  // mirror ghost (cliffs.f:145-152)
-        ub = -uj; cb = cj; db = dj; vb = vj;
-        FPr = R(-2) * cj * uj;
-        FQr = -FPr;
-      }
-      const R inv_fm = geo_m.inv_fm, inv_fp = geo_m.inv_fp, dtx = geo_m.dtx;
-      const R Hj = (C.fl & F_LAND) ? p.ground : C.H;  // h^2/g
-      R cc = R(0);
-      if (p.gcrough != R(0)) {  // "almost Manning" friction (cliffs.f:204)
-        const R r = frsqrt(Hj);  // sqrt((u^2+v^2)/H)/H = |u,v| / H^1.5
-        cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
-      }
-      const R sphr = R(8) * cj * uj * geo_m.scl;  // (P-Q)(P+Q)*scl
-      const bool water = (dj > p.ground) && (da > p.ground) && (db > p.ground);
-      R sdiff = R(0);
-      const bool sonP = water && (ua + ca < R(0)) && (ub + cb > R(0));
-      const bool sonQ = water && (ua - ca < R(0)) && (ub - cb > R(0));
-      if (sonP || sonQ) sdiff = R(2) * p.g * (csqrt(dj * db) - csqrt(dj * da));
-      const R isum = dtx * p.idt;  // 1/(fm+fp)
-      // P equation (cliffs.f:223-234)
-      R QpP = FPr * inv_fp, QmP = FPl * inv_fm, QsP;
-      const R ejP = uj + cj;  // e_j/4
-      if (sonP)
-        QsP = (ejP * ((ub - ua) + R(2) * (cb - ca)) - sdiff) * isum;
-      else
-        QsP = R(0.5) * (QpP + QmP);
-      QsP = QsP + ejP * dtx * (QmP - QpP);
-      const R dP = -p.dt * (QsP + cc - sphr);
-      // Q equation (cliffs.f:236-247)
-      R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm, QsQ;
-      const R ejQ = uj - cj;
-      if (sonQ)
-        QsQ = (ejQ * ((ub - ua) - R(2) * (cb - ca)) - sdiff) * isum;
-      else
-        QsQ = R(0.5) * (QpQ + QmQ);
-      QsQ = QsQ + ejQ * dtx * (QmQ - QpQ);
-      const R dQ = -p.dt * (QsQ + cc + sphr);
-      // tangential velocity (cliffs.f:249-250)
-      const R Qv = (vb - vj) * inv_fp - (vj - va) * inv_fm;
-      C.vn = vj - uj * dtx * ((vb - va) - Qv * (uj * p.dt + geo_m.dfpm));
-      const R dc = R(0.25) * (dP - dQ);
-      C.cn = cj + dc;
-      C.un = uj + R(0.5) * (dP + dQ);
-      C.en = eta_step(cj, C.ef, dc, dj, p);
-    } else if (m == 1 && (C.fl & F_EW)) {
-      // left edge (cliffs.f:288-308)
-      C.cn = C.c; C.un = C.uf; C.vn = C.vf; C.en = C.ef;
-      if ((B.fl & F_EW) && (eL.eta + C.d > p.ground)) {
-        R FP, FQ;
-        face_flux(C.uf, C.c, C.ef, B.uf, B.c, B.ef, p, FP, FQ);
-        const R sphr = R(8) * C.c * C.uf * scl1;
-        const R dQ = -p.dt * (FQ * inv_dx1 + sphr);
-        const R cbnd = csqrt(p.g * (C.d + eL.eta));
-        const R dP = (eL.un - C.uf) + R(2) * p.g * (eL.eta - C.ef) / (cbnd + C.c);
-        C.vn = (C.uf < R(0)) ? C.vf - p.dt * (B.vf - C.vf) * C.uf * inv_dx1 : eL.vt;
-        const R dc = R(0.25) * (dP - dQ);
-        C.cn = C.c + dc;
-        C.un = C.uf + R(0.5) * (dP + dQ);
-        C.en = eta_step(C.c, C.ef, dc, C.d, p);
-      }
-    } else if (m == n && (C.fl & F_EW)) {
-      // right edge (cliffs.f:309-329)
-      C.cn = C.c; C.un = C.uf; C.vn = C.vf; C.en = C.ef;
-      if ((D.fl & F_EW) && (eR.eta + C.d > p.ground)) {
-        R FP, FQ;
-        face_flux(D.uf, D.c, D.ef, C.uf, C.c, C.ef, p, FP, FQ);
-        const R sphr = R(8) * C.c * C.uf * scln;
-        const R dP = -p.dt * (FP * inv_dxn1 - sphr);
-        const R cbnd = csqrt(p.g * (C.d + eR.eta));
-        const R dQ = (eR.un - C.uf) - R(2) * p.g * (eR.eta - C.ef) / (cbnd + C.c);
-        C.vn = (C.uf > R(0)) ? C.vf - p.dt * (C.vf - D.vf) * C.uf * inv_dxn1 : eR.vt;
-        const R dc = R(0.25) * (dP - dQ);
-        C.cn = C.c + dc;
-        C.un = C.uf + R(0.5) * (dP + dQ);
-        C.en = eta_step(C.c, C.ef, dc, C.d, p);
-      }
-    }
-    fpr_ok = carried;
-    fpr_P = carP;
-    fpr_Q = carQ;
-    // ---- stage D: output cell o = k-3
-    const int o = k - 3;
-    if (!(D.fl & F_PRESENT)) return false;
-    if (D.fl & F_EW) {
-      R cO = D.cn, uO = D.un, eO = D.en;
-      if (o >= 2 && o <= n - 1) {
-        // shoreline angle limiter on newly wetted cells (cliffs.f:264-285)
-        if ((D.fl & F_L) && !(E.fl & F_EW)) {
-          const R hj = (o + 1 <= n - 1) ? C.cn : C.c;
-          const R uj = (o + 1 <= n - 1) ? C.un : C.uf;
-          if (p.sqr2 * cO > hj) {
-            cO = hj / p.sqr2;
-            eO = eta_from_c(cO, D.d, p);
-          }
-          if (uO < uj) uO = uj;
-        } else if ((D.fl & F_R) && !(C.fl & F_EW)) {
-          const R hj = (o - 1 >= 2) ? E.cn : E.c;
-          const R uj = (o - 1 >= 2) ? E.un : E.uf;
-          if (p.sqr2 * cO > hj) {
-            cO = hj / p.sqr2;
-            eO = eta_from_c(cO, D.d, p);
-          }
-          if (uO > uj) uO = uj;
-        }
-      }
-      out.eta = eO;
-      out.u = uO;
-      out.v = D.vn;
-    } else if (wet) {  // newland in a line with water: h=u=v=0 (cliffs.f:118-122)
-      out.eta = -D.d;
-      out.u = R(0);
-      out.v = R(0);
-    } else {  // fully dry line: untouched
-      out.eta = D.eta;
-      out.u = D.u;
-      out.v = D.v;
-    }
-    (void)o;
-    return true;
-  }
-
-  // push() for a stretch where cells k-3..k are all wet (H > ground) and
-  // interior (2 <= k-3, k <= n-1): no flooding, no shoreline ghost, no
-  // limiter, no edge.  Leaves the ring exactly as push() would.
-  CL_HD OutCell<R> push_fast(R d, R eta, R u, R v, const Geo<R>& geo_m) {
-    re = rd;
-    rd = rc;
-    rc = rb;
-    rb = ra;
-    RCell<R>& A = ra;
-    RCell<R>& B = rb;
-    RCell<R>& C = rc;
-    RCell<R>& D = rd;
-    A.d = d;
-    A.eta = eta;
-    A.u = u;
-    A.v = v;
-    A.H = d + eta;
-    A.fl = F_PRESENT;
-    B.c = fsqrt_pos(p.g * B.H);
-    B.ef = B.eta;
-    B.uf = B.u;
-    B.vf = B.v;
-    B.fl = F_PRESENT | F_EW;
-    // interior VTCS-2 update of C with real neighbours D (left), B (right)
-    R FPl, FQl, FPr, FQr;
-    if (fpr_ok) {
-      FPl = fpr_P;
-      FQl = fpr_Q;
-    } else {
-      face_flux(D.uf, D.c, D.ef, C.uf, C.c, C.ef, p, FPl, FQl);
-    }
-    face_flux(C.uf, C.c, C.ef, B.uf, B.c, B.ef, p, FPr, FQr);
-    fpr_ok = true;
-    fpr_P = FPr;
-    fpr_Q = FQr;
-    const CellState<R> a{D.uf, D.c, D.ef, D.d, D.vf, D.H};
-    const CellState<R> j{C.uf, C.c, C.ef, C.d, C.vf, C.H};
-    const CellState<R> b{B.uf, B.c, B.ef, B.d, B.vf, B.H};
-    const OutCell<R> r = interior_update(a, j, b, FPl, FQl, FPr, FQr, geo_m, p, &C.cn);
-    C.en = r.eta;
-    C.un = r.u;
-    C.vn = r.v;
-    return OutCell<R>{D.en, D.un, D.vn};
-  }
-};
 
 }  // namespace cliffs

@@ -32,10 +32,10 @@ struct SweepArgs {
   int nlines;  // number of lines (ny for x, nx for y)
   int lo, hi;  // swept lines, 1-based; other lines are copied through
   const float* dep;
-  const float* eta;
+  const float* srf;  // surface state: eta where dep >= 0, water depth where dep < 0
   const float* xu;
   const float* yv;
-  float* eta_o;
+  float* srf_o;
   float* xu_o;
   float* yv_o;
   float* hmax;    // max eta, nullptr when the max-wave update is not fused
@@ -100,18 +100,18 @@ __device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L
     if (k >= 1 && k <= n) {
       const size_t q = cidx<DIR>(L, k, A.pitch);
       const float xu = __ldg(A.xu + q), yv = __ldg(A.yv + q);
-      w[t] = RawCell<float>{__ldg(A.dep + q), __ldg(A.eta + q), DIR == 0 ? xu : yv, DIR == 0 ? yv : xu, true};
-      anywet |= w[t].d + w[t].e > p.ground;
+      w[t] = RawCell<float>{__ldg(A.dep + q), __ldg(A.srf + q), DIR == 0 ? xu : yv, DIR == 0 ? yv : xu, true};
+      anywet |= depth_of(w[t].s, w[t].d) > p.ground;
     }
   }
   LineCtx<float> C;
   C.n = n;
   C.wet = anywet;
-  if (!anywet && !(w[3].d + w[3].e == 0.f && w[3].u == 0.f && w[3].v == 0.f)) {
+  if (!anywet && !(depth_of(w[3].s, w[3].d) == 0.f && w[3].u == 0.f && w[3].v == 0.f)) {
     // does the line hold a wet cell anywhere (cliffs.f:113)?
     for (int k = 1; k <= n && !C.wet; ++k) {
       const size_t q = cidx<DIR>(L, k, A.pitch);
-      C.wet = __ldg(A.dep + q) + __ldg(A.eta + q) > p.ground;
+      C.wet = depth_of(__ldg(A.srf + q), __ldg(A.dep + q)) > p.ground;
     }
   }
   C.eL = eL;
@@ -154,6 +154,7 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   }
   const size_t q = cidx<DIR>(L, o, A.pitch);
   // every global read this cell needs goes out before the compute
+  const float dq = __ldg(A.dep + q);
   float hm = 0.f, vm = 0.f;
   if (A.hmax) {
     hm = A.hmax[q];
@@ -164,21 +165,21 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   const OutCell<float> r = general_path<DIR>(A, L, o, alpha, ialpha, eL, eR);
   const float xo = DIR == 0 ? r.u : r.v;
   const float yo = DIR == 0 ? r.v : r.u;
-  A.eta_o[q] = r.eta;
+  A.srf_o[q] = r.s;
   A.xu_o[q] = xo;
   A.yv_o[q] = yo;
   if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
-    A.hmax[q] = fmaxf(hm, r.eta);
+    A.hmax[q] = fmaxf(hm, eta_of(r.s, dq));
     A.velmax[q] = fmaxf(vm, xo * xo + yo * yo);
   }
-  if (!isfinite(r.eta + xo + yo)) atomicOr(A.status, ST_NAN);
+  if (!isfinite(r.s + xo + yo)) atomicOr(A.status, ST_NAN);
 }
 
 // LOCAL: the block finishes its own listed cells after its fast cells (a
 // block-local list in shared memory); otherwise they go to the global
 // worklist for general_kernel.
 template <int DIR, bool LOCAL>
-__global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
+__global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
   __shared__ uint32_t s_list[LOCAL ? 256 * 4 : 1];
   __shared__ unsigned s_n;
   if (LOCAL) {
@@ -200,7 +201,8 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
   const bool active = L <= A.nlines && i0 <= n;
   const bool swept = active && L >= A.lo && L <= A.hi;
   const Phys<float>& p = A.ph;
-  // window w[0..5] = positions i0-1 .. i0+4 (u normal, v tangential)
+  // window w[0..5] = positions i0-1 .. i0+4 (u normal, v tangential); e
+  // holds the surface state as loaded, then eta
   float d[6], e[6], u[6], v[6];
   float hm[kCellsPerThread], vm[kCellsPerThread];
   size_t q0 = 0;
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     float4 D4 = make_float4(0, 0, 0, 0), E4 = D4, X4 = D4, Y4 = D4, H4 = D4, V4 = D4;
     if (active) {
       D4 = __ldg(reinterpret_cast<const float4*>(A.dep + q0));
-      E4 = __ldg(reinterpret_cast<const float4*>(A.eta + q0));
+      E4 = __ldg(reinterpret_cast<const float4*>(A.srf + q0));
       X4 = __ldg(reinterpret_cast<const float4*>(A.xu + q0));
       Y4 = __ldg(reinterpret_cast<const float4*>(A.yv + q0));
       if (A.hmax) {
@@ -233,13 +235,13 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     v[5] = __shfl_down_sync(0xffffffffu, Y4.x, 1);
     if (active && lane == 0 && i0 > 1) {
       d[0] = __ldg(A.dep + q0 - 1);
-      e[0] = __ldg(A.eta + q0 - 1);
+      e[0] = __ldg(A.srf + q0 - 1);
       u[0] = __ldg(A.xu + q0 - 1);
       v[0] = __ldg(A.yv + q0 - 1);
     }
     if (active && lane == 31 && i0 + 4 <= n) {
       d[5] = __ldg(A.dep + q0 + 4);
-      e[5] = __ldg(A.eta + q0 + 4);
+      e[5] = __ldg(A.srf + q0 + 4);
       u[5] = __ldg(A.xu + q0 + 4);
       v[5] = __ldg(A.yv + q0 + 4);
     }
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
       d[w] = e[w] = u[w] = v[w] = 0.f;
       if (active) {
         d[w] = __ldg(A.dep + q);
-        e[w] = __ldg(A.eta + q);
+        e[w] = __ldg(A.srf + q);
         v[w] = __ldg(A.xu + q);  // tangential in the y-sweep
         u[w] = __ldg(A.yv + q);  // normal
       }
@@ -267,16 +269,22 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
       }
     }
   }
-  float oe[kCellsPerThread], ou[kCellsPerThread], ov[kCellsPerThread];
-  unsigned need = 0u;  // bit r: cell i0+r goes to the general kernel
-  if (!swept) {  // lines not swept are copied through
+  float H[6];
 #pragma unroll
-    for (int r = 0; r < kCellsPerThread; ++r) {
-      oe[r] = e[r + 1];
-      ou[r] = u[r + 1];
-      ov[r] = v[r + 1];
-    }
-  } else if (active) {
+  for (int w = 0; w < 6; ++w) {  // surface state -> (eta, H); the stored form stays exact in one of them
+    H[w] = depth_of(e[w], d[w]);
+    e[w] = eta_of(e[w], d[w]);
+  }
+  // os: new surface state of cells i0..i0+3, initially the state as loaded
+  float os[kCellsPerThread], ou[kCellsPerThread], ov[kCellsPerThread];
+#pragma unroll
+  for (int r = 0; r < kCellsPerThread; ++r) {
+    os[r] = d[r + 1] < 0.f ? H[r + 1] : e[r + 1];
+    ou[r] = u[r + 1];
+    ov[r] = v[r + 1];
+  }
+  unsigned need = 0u;  // bit r: cell i0+r goes to the general path
+  if (swept) {  // lines not swept are copied through
     float alpha = 1.f, ialpha = 1.f;
     if (DIR == 0 && A.lscale != nullptr) {
       const float2 s = A.lscale[L - 1];
@@ -284,11 +292,10 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
       ialpha = s.y;
     }
     bool wet[6];
-    float H[6], c[6];
+    float c[6];
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
       const int k = i0 - 1 + w;
-      H[w] = d[w] + e[w];
       wet[w] = (k >= 1 && k <= n) && H[w] > p.ground;
       c[w] = fsqrt_pos(p.g * fmaxf(H[w], p.ground));
     }
@@ -299,9 +306,6 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     for (int r = 0; r < kCellsPerThread; ++r) {
       const int k = i0 + r;
       const int w = r + 1;
-      oe[r] = e[w];
-      ou[r] = u[w];
-      ov[r] = v[w];
       if (k > n) continue;
       if (k >= 2 && k <= n - 1 && wet[w - 1] && wet[w] && wet[w + 1]) {
         const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
@@ -310,7 +314,7 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
         float cn;
         const OutCell<float> o =
             interior_update(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], geo_at(A, k, alpha, ialpha), p, &cn);
-        oe[r] = o.eta;
+        os[r] = o.s;
         ou[r] = o.u;
         ov[r] = o.v;
       } else if ((k == 1 && wet[w] && wet[w + 1]) || (k == n && wet[w - 1] && wet[w])) {
@@ -322,10 +326,10 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
           float cn;
           if (k == 1) {
             const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
-            edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], oe[r]);
+            edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], os[r]);
           } else {
             const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
-            edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r], oe[r]);
+            edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r], os[r]);
           }
         }
       } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
@@ -352,9 +356,9 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     xo[r] = DIR == 0 ? ou[r] : ov[r];
     yo[r] = DIR == 0 ? ov[r] : ou[r];
     const bool done = i0 + r <= n && !((need >> r) & 1u);
-    if (done) bad |= !isfinite(oe[r] + xo[r] + yo[r]);
+    if (done) bad |= !isfinite(os[r] + xo[r] + yo[r]);
     if (A.hmax && done) {  // max-wave update (cliffs_main.f:347-355)
-      hm[r] = fmaxf(hm[r], oe[r]);
+      hm[r] = fmaxf(hm[r], eta_of(os[r], d[r + 1]));
       vm[r] = fmaxf(vm[r], xo[r] * xo[r] + yo[r] * yo[r]);
     }
   }
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
     // nothing to store
   } else if (DIR == 0) {
     // whole float4s: the row padding beyond nx takes the values of no cell
-    *reinterpret_cast<float4*>(A.eta_o + q0) = make_float4(oe[0], oe[1], oe[2], oe[3]);
+    *reinterpret_cast<float4*>(A.srf_o + q0) = make_float4(os[0], os[1], os[2], os[3]);
     *reinterpret_cast<float4*>(A.xu_o + q0) = make_float4(xo[0], xo[1], xo[2], xo[3]);
     *reinterpret_cast<float4*>(A.yv_o + q0) = make_float4(yo[0], yo[1], yo[2], yo[3]);
     if (A.hmax) {
@@ -375,7 +379,7 @@ __global__ void __launch_bounds__(256) fast_kernel(const SweepArgs A) {
       const int k = i0 + r;
       if (k > n) break;
       const size_t q = cidx<1>(L, k, A.pitch);
-      A.eta_o[q] = oe[r];
+      A.srf_o[q] = os[r];
       A.xu_o[q] = xo[r];
       A.yv_o[q] = yo[r];
       if (A.hmax) {

@@ -184,6 +184,10 @@ int cliffs_gpu_profile(cliffs_ctx *ctx, int32_t enable);
 int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
                             double *y_ms, int64_t *y_count);
 
+/* Number of kernels this context has launched since it was created (every
+ * entry point counts its own launches; copies and memsets are not kernels). */
+int cliffs_gpu_launch_count(cliffs_ctx *ctx, int64_t *n);
+
 /* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
  * and warps per block of the y-sweep kernel (<= 8).  0 keeps the current
  * value.  Results do not depend on the tiling. */
@@ -197,8 +201,9 @@ int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
  * of cliffs_gpu_sweep on arrays the caller owns.
  *
  * Arrays are device FP32 in the library's own state form: dep (depth, >0
- * water), eta (surface elevation = H - dep; a drying cell keeps H = c|c|/g),
- * xvel, yvel, ny rows of `pitch` floats (pitch >= nx, a multiple of 4, every
+ * water), srf (surface state: the elevation eta = H - dep where dep >= 0, the
+ * water depth H where dep < 0; a drying cell keeps H = c|c|/g), xvel, yvel,
+ * ny rows of `pitch` floats (pitch >= nx, a multiple of 4, every
  * pointer 16-byte aligned).  Output rows are written whole, so columns
  * nx..pitch-1 of the outputs may change.  The grid is Cartesian with uniform
  * spacing dx (x-sweep) or dy (y-sweep), still-water open edges, no max-wave.
@@ -213,9 +218,9 @@ int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
  * on it.  The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture. */
 int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch,
-                             const float *dep, const float *eta,
+                             const float *dep, const float *srf,
                              const float *xvel, const float *yvel,
-                             float *eta_out, float *xvel_out, float *yvel_out,
+                             float *srf_out, float *xvel_out, float *yvel_out,
                              double dx, double dy, double ground, double crough,
                              double dt, void *stream);
 

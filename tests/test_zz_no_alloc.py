@@ -21,9 +21,12 @@ pkg = importlib.import_module("cliffs-src_gb300")
 GRAV = 9.800000190734863
 
 
-def _to_eta_state(cel, dep):
-    """Celerity form (the context's download) -> the library's eta form."""
-    return cel * np.abs(cel) / GRAV - dep
+def _to_surface_state(cel, dep):
+    """Celerity form (the context's download) -> the library's surface state:
+    eta where dep >= 0, the water depth H where dep < 0 (on FP32 depths)."""
+    d = dep.astype(np.float32).astype(np.float64)
+    H = cel * np.abs(cel) / GRAV
+    return np.where(d < 0, H, H - d)
 
 
 def _dev(torch, a2d, pitch):
@@ -50,7 +53,7 @@ def test_noalloc_matches_context_two_calls():
     dep = case["dep"]
     pitch = (nx + 31) // 32 * 32
     d_dep = _dev(torch, dep, pitch)
-    bufs = [[_dev(torch, a, pitch) for a in (_to_eta_state(cel, dep), u, v)],
+    bufs = [[_dev(torch, a, pitch) for a in (_to_surface_state(cel, dep), u, v)],
             [torch.zeros((ny, pitch), dtype=torch.float32, device="cuda") for _ in range(3)]]
     stream = torch.cuda.current_stream().cuda_stream
     src = 0
@@ -64,11 +67,11 @@ def test_noalloc_matches_context_two_calls():
         torch.cuda.synchronize()
         g.sweep(iu)  # the same sweep through the allocating API
         cg, ug, vg = g.download_state()
-        eta_ref = _to_eta_state(cg, dep)
-        eta_na = b[0][:, :nx].cpu().numpy().astype(np.float64)
+        srf_ref = _to_surface_state(cg, dep)
+        srf_na = b[0][:, :nx].cpu().numpy().astype(np.float64)
         # same kernels, same arithmetic: agreement well inside the parity
         # tolerance of the suite (1e-4 of a 2 m source amplitude)
-        assert np.abs(eta_na - eta_ref).max() <= 1e-6, call
+        assert np.abs(srf_na - srf_ref).max() <= 1e-6, call
         assert np.abs(b[1][:, :nx].cpu().numpy() - ug).max() <= 1e-7, call
         assert np.abs(b[2][:, :nx].cpu().numpy() - vg).max() <= 1e-7, call
         src = 1 - src
