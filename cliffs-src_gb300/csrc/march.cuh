@@ -74,6 +74,16 @@ CL_HD float fsqrt0(float x) {
 }
 CL_HD double fsqrt0(double x) { return csqrt(x); }
 
+// x / y where ~2 ulp is enough (y away from 0 and from huge values)
+CL_HD float fdiv(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(x, y);
+#else
+  return x / y;
+#endif
+}
+CL_HD double fdiv(double x, double y) { return x / y; }
+
 // 1/sqrt(x), x > 0
 CL_HD float frsqrt(float x) {
 #ifdef __CUDA_ARCH__
@@ -169,8 +179,9 @@ struct NoFlux {};
 // VTCS-2 interior update of cell j between real neighbours a (left) and b
 // (right), cliffs.f:200-262, in the eta form.  FPl/FQl, FPr/FQr are the face
 // fluxes (a,j) and (j,b).  Returns the new (s, u, v); *cn gets the new
-// celerity.
-template <typename R>
+// celerity.  TC = false leaves out the transcritical-point test, for callers
+// that know no neighbour is supercritical (|u| <= c), where it cannot fire.
+template <typename R, bool TC = true>
 CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, const CellState<R>& b,
                                  R FPl, R FQl, R FPr, R FQr, const Geo<R>& geo, const Phys<R>& p,
                                  R* cn_out) {
@@ -184,12 +195,12 @@ CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, c
   const R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm;
   R QsP = R(0.5) * (QpP + QmP);
   R QsQ = R(0.5) * (QpQ + QmQ);
-  const bool sonP = (a.u + a.c < R(0)) && (b.u + b.c > R(0));
-  const bool sonQ = (a.u - a.c < R(0)) && (b.u - b.c > R(0));
+  const bool sonP = TC && (a.u + a.c < R(0)) && (b.u + b.c > R(0));
+  const bool sonQ = TC && (a.u - a.c < R(0)) && (b.u - b.c > R(0));
   if ((sonP || sonQ) && (dj > p.ground) && (a.d > p.ground) && (b.d > p.ground)) {
     // transcritical point (cliffs.f:228-232, 241-245)
     const R isum = dtx * p.idt;
-    const R sdiff = R(2) * p.g * (csqrt(dj * b.d) - csqrt(dj * a.d));
+    const R sdiff = R(2) * p.g * (fsqrt_pos(dj * b.d) - fsqrt_pos(dj * a.d));
     if (sonP) QsP = (ejP * ((b.u - a.u) + R(2) * (b.c - a.c)) - sdiff) * isum;
     if (sonQ) QsQ = (ejQ * ((b.u - a.u) - R(2) * (b.c - a.c)) - sdiff) * isum;
   }
@@ -216,8 +227,8 @@ CL_HD void edge_left(const CellState<R>& C, const CellState<R>& B, const EdgeVal
   face_flux(C.u, C.c, C.e, B.u, B.c, B.e, p, FP, FQ);
   const R sphr = R(8) * C.c * C.u * scl1;
   const R dQ = -p.dt * (FQ * inv_dx1 + sphr);
-  const R cbnd = csqrt(p.g * (C.d + e.eta));
-  const R dP = (e.un - C.u) + R(2) * p.g * (e.eta - C.e) / (cbnd + C.c);
+  const R cbnd = fsqrt_pos(p.g * (C.d + e.eta));  // C.d + e.eta > ground: the caller's edge condition
+  const R dP = (e.un - C.u) + fdiv(R(2) * p.g * (e.eta - C.e), cbnd + C.c);
   vn = (C.u < R(0)) ? C.v - p.dt * (B.v - C.v) * C.u * inv_dx1 : e.vt;
   const R dc = R(0.25) * (dP - dQ);
   cn = C.c + dc;
@@ -234,8 +245,8 @@ CL_HD void edge_right(const CellState<R>& D, const CellState<R>& C, const EdgeVa
   face_flux(D.u, D.c, D.e, C.u, C.c, C.e, p, FP, FQ);
   const R sphr = R(8) * C.c * C.u * scln;
   const R dP = -p.dt * (FP * inv_dxn1 - sphr);
-  const R cbnd = csqrt(p.g * (C.d + e.eta));
-  const R dQ = (e.un - C.u) - R(2) * p.g * (e.eta - C.e) / (cbnd + C.c);
+  const R cbnd = fsqrt_pos(p.g * (C.d + e.eta));  // C.d + e.eta > ground: the caller's edge condition
+  const R dQ = (e.un - C.u) - fdiv(R(2) * p.g * (e.eta - C.e), cbnd + C.c);
   vn = (C.u > R(0)) ? C.v - p.dt * (C.v - D.v) * C.u * inv_dxn1 : e.vt;
   const R dc = R(0.25) * (dP - dQ);
   cn = C.c + dc;

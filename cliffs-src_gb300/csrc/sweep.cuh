@@ -293,49 +293,68 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
     }
     bool wet[6];
     float c[6];
+    bool sup = false;  // a supercritical cell (|u| > c) in the window
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
       const int k = i0 - 1 + w;
       wet[w] = (k >= 1 && k <= n) && H[w] > p.ground;
       c[w] = fsqrt_pos(p.g * fmaxf(H[w], p.ground));
+      sup = sup || fabsf(u[w]) > c[w];
     }
     float FP[5], FQ[5];  // face fluxes between window cells w and w+1
 #pragma unroll
     for (int f = 0; f < 5; ++f) face_flux(u[f], c[f], e[f], u[f + 1], c[f + 1], e[f + 1], p, FP[f], FQ[f]);
+    // Every cell takes the plain VTCS-2 interior update, straight through
+    // (no per-cell branches); it is kept where the cell is interior, wet
+    // between wet neighbours, and no transcritical point can occur (a
+    // transcritical point needs a supercritical neighbour).
+    unsigned rest = 0u;  // bit r: cell i0+r is not a plain interior cell
 #pragma unroll
     for (int r = 0; r < kCellsPerThread; ++r) {
       const int k = i0 + r;
       const int w = r + 1;
-      if (k > n) continue;
-      if (k >= 2 && k <= n - 1 && wet[w - 1] && wet[w] && wet[w + 1]) {
-        const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
-        const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
-        const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
-        float cn;
-        const OutCell<float> o =
-            interior_update(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], geo_at(A, k, alpha, ialpha), p, &cn);
-        os[r] = o.s;
-        ou[r] = o.u;
-        ov[r] = o.v;
-      } else if ((k == 1 && wet[w] && wet[w + 1]) || (k == n && wet[w - 1] && wet[w])) {
-        // line end next to a wet cell: no flooding reaches it; the open or
-        // forced edge update (cliffs.f:287-329), or the cell as it is
-        const EdgeVals<float> ev = edge_vals(A, L, k == 1 ? 0 : 1);
-        if (ev.eta + d[w] > p.ground) {
-          const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
-          float cn;
-          if (k == 1) {
-            const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
-            edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], os[r]);
-          } else {
-            const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
-            edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r], os[r]);
+      const bool plain = !sup && k >= 2 && k <= n - 1 && wet[w - 1] && wet[w] && wet[w + 1];
+      const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
+      const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
+      const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
+      float cn;
+      const OutCell<float> o = interior_update<float, false>(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w],
+                                                             geo_at(A, k, alpha, ialpha), p, &cn);
+      os[r] = plain ? o.s : os[r];
+      ou[r] = plain ? o.u : ou[r];
+      ov[r] = plain ? o.v : ov[r];
+      if (!plain && k <= n) rest |= 1u << r;
+    }
+    if (rest) {  // line ends, shorelines, dry cells, supercritical flow
+#pragma unroll
+      for (int r = 0; r < kCellsPerThread; ++r) {
+        if (!((rest >> r) & 1u)) continue;
+        const int k = i0 + r;
+        const int w = r + 1;
+        if ((r == 0 && k == 1 && wet[w] && wet[w + 1]) ||
+            (r == kCellsPerThread - 1 && k == n && wet[w - 1] && wet[w])) {
+          // line end next to a wet cell: no flooding reaches it; the open or
+          // forced edge update (cliffs.f:287-329), or the cell as it is.
+          // Only the thread's first and last cell can take it here (one copy
+          // each in the unrolled loop); other line ends go to the general path.
+          const EdgeVals<float> ev = edge_vals(A, L, k == 1 ? 0 : 1);
+          if (ev.eta + d[w] > p.ground) {
+            const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
+            float cn;
+            if (k == 1) {
+              const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
+              edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], os[r]);
+            } else {
+              const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
+              edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r],
+                         os[r]);
+            }
           }
+        } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
+          need |= 1u << r;
         }
-      } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
-        need |= 1u << r;
+        // else: dry, zero state: unchanged whether or not the line holds water
       }
-      // else: dry, zero state: unchanged whether or not the line holds water
     }
   }
   if (LOCAL) {
