@@ -75,7 +75,7 @@ struct cliffs_ctx {
   std::vector<Nest> nests;
   int* d_flag = nullptr;
   bool have_state = false;
-  int blk_x = 128, warps_y = 8;
+  int blk_x = 128, warps_y = 4;
   // worklist of cells for the general kernel and one counter per sweep parity
   uint32_t* list = nullptr;
   uint32_t* cnt = nullptr;
