@@ -1,7 +1,10 @@
-"""Build recipe of the CUDA library behind include/cliffs_gpu.h.
+"""Build recipe of the CUDA library behind include/cliffs_gpu.h and of the
+driver executable above it.
 
 nvcc compiles csrc/cliffs_gpu.cu for sm_103a only (GB300) into
-_lib/libcliffs_gpu.so, in the source tree.  No torch, no cmake.
+_lib/libcliffs_gpu.so; g++ compiles host/*.cpp (the Cliffs driver with its
+NetCDF classic I/O) into _lib/cliffs_gb300, linked against that library.
+Both stay in the source tree.  No torch, no cmake.
 """
 import glob
 import os
@@ -12,6 +15,8 @@ ROOT = os.path.dirname(HERE)
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libcliffs_gpu.so")
 SRC = os.path.join(HERE, "csrc", "cliffs_gpu.cu")
+DRIVER = os.path.join(LIBDIR, "cliffs_gb300")
+HOST_SRC = sorted(glob.glob(os.path.join(HERE, "host", "*.cpp")))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -25,6 +30,26 @@ def nvcc():
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    """Build the library, then the driver; returns the library's path."""
+    lib = build_lib(force, verbose)
+    build_driver(force)
+    return lib
+
+
+def build_driver(force: bool = False) -> str:
+    deps = HOST_SRC + glob.glob(os.path.join(HERE, "host", "*.hpp")) + [LIB, os.path.join(ROOT, "include", "cliffs_gpu.h")]
+    if not force and os.path.exists(DRIVER):
+        if os.path.getmtime(DRIVER) >= max(os.path.getmtime(p) for p in deps):
+            return DRIVER
+    tmp = DRIVER + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", *HOST_SRC, "-L" + LIBDIR, "-lcliffs_gpu",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
+def build_lib(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     if not force and os.path.exists(LIB):
         if os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in _deps()):

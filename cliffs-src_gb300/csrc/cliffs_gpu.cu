@@ -53,6 +53,7 @@ struct cliffs_ctx {
   float *hmax = nullptr, *velmax = nullptr;
   int cur = 0;
   int64_t launches = 0;  // kernels this context has launched
+  std::vector<double> dep64;  // the caller's FP64 depth, for the state conversions
   float4 *geo_x = nullptr, *geo_y = nullptr;
   float* scl_y = nullptr;
   float2* lscale = nullptr;
@@ -97,10 +98,15 @@ int dalloc(T** p, size_t n) {
   return CLIFFS_OK;
 }
 
+// dep64 is the caller's FP64 depth.  The device keeps FP32 depths, which a
+// deformed bottom need not hit exactly; the surface state is taken against
+// the FP64 depth so that the elevation eta = H - dep stays exact and the
+// depth's rounding (a relative ~3e-8) goes into the total depth instead.
 __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict__ src,
                              int src_is_celerity, const double* __restrict__ xv,
                              const double* __restrict__ yvv, const float* __restrict__ dep,
-                             float* srf, float* xu, float* yv, double ground, double g) {
+                             const double* __restrict__ dep64, float* srf, float* xu, float* yv,
+                             double ground, double g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= pitch || j >= ny) return;
@@ -112,7 +118,7 @@ __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict
     return;
   }
   const size_t s = (size_t)j * nx + i;
-  const double d = (double)dep[q];
+  const bool land = dep[q] < 0.f;  // the same land test as the sweeps
   double H;
   if (src_is_celerity) {
     const double c = src[s];
@@ -121,7 +127,7 @@ __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict
     // celerity transform of cliffs_main.f:218-227 expressed on H
     H = src[s] <= ground ? 0.0 : src[s];
   }
-  srf[q] = (float)(d < 0 ? H : H - d);  // surface state: H on land, eta at sea
+  srf[q] = (float)(land ? H : H - dep64[s]);  // surface state: H on land, eta at sea
   xu[q] = xv ? (float)xv[s] : 0.f;
   yv[q] = yvv ? (float)yvv[s] : 0.f;
 }
@@ -137,14 +143,15 @@ __global__ void k_reset_max(int nx, int ny, int pitch, const float* __restrict__
 }
 
 __global__ void k_download(int nx, int ny, int pitch, const float* __restrict__ dep,
-                           const float* __restrict__ srf, const float* __restrict__ xu,
-                           const float* __restrict__ yv, double* cel, double* xo, double* yo,
-                           double g) {
+                           const double* __restrict__ dep64, const float* __restrict__ srf,
+                           const float* __restrict__ xu, const float* __restrict__ yv, double* cel,
+                           double* xo, double* yo, double g) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= nx || j >= ny) return;
   const size_t q = (size_t)j * pitch + i, s = (size_t)j * nx + i;
-  const double H = depth_of((double)srf[q], (double)dep[q]);
+  // the inverse of k_init_state: eta is exact against the FP64 depth
+  const double H = dep[q] < 0.f ? (double)srf[q] : dep64[s] + (double)srf[q];
   if (cel) cel[s] = H < 0 ? -sqrt(-g * H) : sqrt(g * H);
   if (xo) xo[s] = xu[q];
   if (yo) yo[s] = yv[q];
@@ -567,6 +574,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       dalloc(&c->cnt, 2))
     return fail(CLIFFS_ERR_NOMEM);
   // bathymetry, padded rows
+  c->dep64.assign(d->dep, d->dep + (size_t)c->nx * c->ny);
   std::vector<float> h((size_t)c->pitch * c->ny, 0.f);
   for (int j = 0; j < c->ny; ++j)
     for (int i = 0; i < c->nx; ++i) h[(size_t)j * c->pitch + i] = (float)d->dep[(size_t)j * c->nx + i];
@@ -658,17 +666,20 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
                          const double* yv, bool reset_max) {
   if (!c || !src) return CLIFFS_ERR_ARG;
   const size_t n = (size_t)c->nx * c->ny;
-  double *dsrc = nullptr, *dx = nullptr, *dy = nullptr;
+  double *dsrc = nullptr, *dx = nullptr, *dy = nullptr, *dd = nullptr;
   int r = CLIFFS_OK;
-  if (dalloc(&dsrc, n) || (xv && dalloc(&dx, n)) || (yv && dalloc(&dy, n))) r = CLIFFS_ERR_NOMEM;
+  if (dalloc(&dsrc, n) || dalloc(&dd, n) || (xv && dalloc(&dx, n)) || (yv && dalloc(&dy, n))) r = CLIFFS_ERR_NOMEM;
   if (!r && cudaMemcpyAsync(dsrc, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && cudaMemcpyAsync(dd, c->dep64.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
+    r = CLIFFS_ERR_CUDA;
   if (!r && xv && cudaMemcpyAsync(dx, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r) {
     c->cur = 0;
     ++c->launches;
     k_init_state<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(
-        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, c->srf[0], c->xu[0], c->yv[0], c->ground, kGrav);
+        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, dd, c->srf[0], c->xu[0], c->yv[0], c->ground,
+        kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
   if (!r && reset_max) {
@@ -678,6 +689,7 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   cudaFree(dsrc);
+  if (dd) cudaFree(dd);
   if (dx) cudaFree(dx);
   if (dy) cudaFree(dy);
   if (!r) c->have_state = true;
@@ -700,13 +712,16 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   const size_t n = (size_t)c->nx * c->ny;
-  double *a = nullptr, *b = nullptr, *e = nullptr;
+  double *a = nullptr, *b = nullptr, *e = nullptr, *dd = nullptr;
   int r = CLIFFS_OK;
-  if (dalloc(&a, n) || dalloc(&b, n) || dalloc(&e, n)) r = CLIFFS_ERR_NOMEM;
+  if (dalloc(&a, n) || dalloc(&b, n) || dalloc(&e, n) || dalloc(&dd, n)) r = CLIFFS_ERR_NOMEM;
+  if (!r && cudaMemcpyAsync(dd, c->dep64.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
+    r = CLIFFS_ERR_CUDA;
   if (!r) {
     ++c->launches;
-    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
-                                                          c->xu[c->cur], c->yv[c->cur], a, b, e, kGrav);
+    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dd,
+                                                          c->srf[c->cur], c->xu[c->cur], c->yv[c->cur], a,
+                                                          b, e, kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
   if (!r && cel && cudaMemcpyAsync(cel, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
@@ -716,6 +731,7 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (a) cudaFree(a);
   if (b) cudaFree(b);
   if (e) cudaFree(e);
+  if (dd) cudaFree(dd);
   return r;
 }
 
