@@ -6,4 +6,4 @@ Python binding.  workloads holds seeded synthetic inputs shaped like the
 benchmark configurations.
 """
 from . import build, workloads  # noqa: F401
-from .cliffs_gpu import GpuGrid, CliffsError, load, metrics  # noqa: F401
+from .cliffs_gpu import GpuGrid, Batch, CliffsError, load, metrics  # noqa: F401

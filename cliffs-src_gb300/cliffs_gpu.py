@@ -46,6 +46,14 @@ class Runup(ctypes.Structure):
                 ("wet_now", ctypes.c_int64)]
 
 
+class BatchPlan(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("graph_steps", ctypes.c_int32)]
+
+
+PERSISTENT, GRAPH = 0, 1
+
+
 class CliffsError(RuntimeError):
     def __init__(self, code, what):
         self.code = code
@@ -85,6 +93,14 @@ SIGNATURES = {
     "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
+    "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),
+    "cliffs_batch_destroy": ([_V], None),
+    "cliffs_batch_set_plan": ([_V, ctypes.POINTER(BatchPlan)], ctypes.c_int),
+    "cliffs_batch_get_plan": ([_V, ctypes.POINTER(BatchPlan)], ctypes.c_int),
+    "cliffs_batch_step": ([_V, _I], ctypes.c_int),
+    "cliffs_batch_autotune": ([_V, _I, _dp], ctypes.c_int),
+    "cliffs_batch_check_barrier_timeout": ([_V, _I], ctypes.c_int),
+    "cliffs_batch_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_sweep_noalloc": ([_I, _I, _I, _I] + [_V] * 7 + [_D] * 5 + [_V], ctypes.c_int),
 }
 
@@ -345,3 +361,57 @@ class GpuGrid:
 
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")
+
+
+class Batch:
+    """Grids stepped together (cliffs_batch_*): one source scenario per grid,
+    grids of any size; bit-identical to stepping each GpuGrid on its own."""
+
+    def __init__(self, grids):
+        self.L = load()
+        self.grids = list(grids)
+        arr = (_V * len(self.grids))(*[g.h.value if isinstance(g.h, ctypes.c_void_p) else g.h
+                                       for g in self.grids])
+        h = _V()
+        _chk(self.L.cliffs_batch_create(arr, len(self.grids), ctypes.byref(h)), "batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cliffs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n):
+        """Advance every grid n steps; each grid's model time follows."""
+        _chk(self.L.cliffs_batch_step(self.h, int(n)), "batch_step")
+        for g in self.grids:
+            g.t.value += n * g.dt
+
+    def set_plan(self, mode, ctas_per_sm=1, graph_steps=32):
+        p = BatchPlan(int(mode), int(ctas_per_sm), int(graph_steps))
+        _chk(self.L.cliffs_batch_set_plan(self.h, ctypes.byref(p)), "batch_set_plan")
+
+    def plan(self):
+        p = BatchPlan()
+        _chk(self.L.cliffs_batch_get_plan(self.h, ctypes.byref(p)), "batch_get_plan")
+        return dict(mode=p.mode, ctas_per_sm=p.ctas_per_sm, graph_steps=p.graph_steps)
+
+    def autotune(self, probe_steps=8):
+        ms = ctypes.c_double()
+        _chk(self.L.cliffs_batch_autotune(self.h, int(probe_steps), ctypes.byref(ms)), "batch_autotune")
+        return ms.value
+
+    def check_barrier_timeout(self, wait_ms=100):
+        """Status of a launch whose grid barrier waits for an absent block."""
+        return self.L.cliffs_batch_check_barrier_timeout(self.h, int(wait_ms))
+
+    def launches(self):
+        n = ctypes.c_int64()
+        _chk(self.L.cliffs_batch_launch_count(self.h, ctypes.byref(n)), "batch_launch_count")
+        return int(n.value)

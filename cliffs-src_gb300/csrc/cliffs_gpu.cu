@@ -9,7 +9,7 @@
 #include <vector>
 
 #include "../../include/cliffs_gpu.h"
-#include "sweep.cuh"
+#include "batch.cuh"
 
 using namespace cliffs;
 
@@ -382,10 +382,10 @@ constexpr int kGeneralBlocks = 304;
 
 // Launch one sweep: the fast kernel, then the general kernel over the cells it
 // listed.  fuse_max: update hmax/velmax on the way out.
-int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
-                 int flen, int irec, double cc) {
+// The arguments of one sweep reading state copy s and writing 1 - s.
+SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
   SweepArgs A{};
-  const int s = c->cur, o = 1 - c->cur;
+  const int o = 1 - s;
   A.pitch = c->pitch;
   A.dep = c->dep;
   A.srf = c->srf[s];
@@ -402,15 +402,6 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
   A.count = c->cnt + (c->sweeps & 1u);
   A.count_next = c->cnt + ((c->sweeps + 1u) & 1u);
   A.edges = nullptr;
-  if (fA || fB) {
-    float* eb = iu == 1 ? c->edge_x : c->edge_y;
-    const int nl = iu == 1 ? c->ny : c->nx;
-    ++c->launches;
-    edges_kernel<<<(nl + 127) / 128, 128, 0, c->stream>>>(nl, flen, fA, fB, irec, cc, iu == 1 ? 0 : 1,
-                                                          iu == 1 ? 1 : 0, eb);
-    CK(cudaGetLastError());
-    A.edges = eb;
-  }
   if (iu == 1) {
     A.n = c->nx;
     A.nlines = c->ny;
@@ -435,6 +426,22 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     A.lscale = nullptr;
     A.inv_dx1 = c->inv_dx1_y;
     A.inv_dxn1 = c->inv_dxn1_y;
+  }
+  return A;
+}
+
+int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
+                 int flen, int irec, double cc) {
+  SweepArgs A = sweep_args(c, iu, fuse_max, c->cur);
+  const int o = 1 - c->cur;
+  if (fA || fB) {
+    float* eb = iu == 1 ? c->edge_x : c->edge_y;
+    const int nl = iu == 1 ? c->ny : c->nx;
+    ++c->launches;
+    edges_kernel<<<(nl + 127) / 128, 128, 0, c->stream>>>(nl, flen, fA, fB, irec, cc, iu == 1 ? 0 : 1,
+                                                          iu == 1 ? 1 : 0, eb);
+    CK(cudaGetLastError());
+    A.edges = eb;
   }
   ProfPair pp{};
   if (c->prof) {
@@ -506,6 +513,7 @@ const char* cliffs_gpu_strerror(int code) {
     case CLIFFS_ERR_NOMEM: return "device allocation failed";
     case CLIFFS_ERR_STATE: return "call out of order";
     case CLIFFS_ERR_DEVICE: return "no usable sm_103 device";
+    case CLIFFS_ERR_TIMEOUT: return "a device-side wait ran out";
     default: return "unknown status";
   }
 }
@@ -1279,3 +1287,300 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Ensembles: many contexts stepped together (batch.cuh).
+// ---------------------------------------------------------------------------
+
+struct cliffs_batch {
+  std::vector<cliffs_ctx*> ctx;
+  int dev = 0, sms = 0, max_ctas = 0;
+  cudaStream_t stream = nullptr;
+  SweepArgs* d_args = nullptr;
+  int* d_off = nullptr;
+  int* d_gx = nullptr;
+  unsigned* d_sync = nullptr;  // [0] barrier counter, [1] timeout flag
+  int total[2] = {0, 0};
+  cliffs_batch_plan plan{CLIFFS_BATCH_PERSISTENT, 1, 32};
+  cudaGraphExec_t graph = nullptr;
+  int graph_built = 0;  // steps in the instantiated graph
+  int64_t launches = 0;
+};
+
+static BatchArgs batch_args(const cliffs_batch* b, int steps) {
+  BatchArgs B;
+  B.args = b->d_args;
+  B.off = b->d_off;
+  B.gx = b->d_gx;
+  B.n = (int)b->ctx.size();
+  B.steps = steps;
+  B.bar = b->d_sync;
+  B.err = b->d_sync + 1;
+  B.wait_ns = kBarrierNs;
+  B.extra = 0;
+  return B;
+}
+
+static void batch_free(cliffs_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->d_args) cudaFree(b->d_args);
+  if (b->d_off) cudaFree(b->d_off);
+  if (b->d_gx) cudaFree(b->d_gx);
+  if (b->d_sync) cudaFree(b->d_sync);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) {
+  if (!ctxs || n < 1 || !out) return CLIFFS_ERR_ARG;
+  *out = nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CLIFFS_ERR_DEVICE;
+  for (int k = 0; k < n; ++k) {
+    const cliffs_ctx* c = ctxs[k];
+    if (!c || c->dev != dev || !c->xrun || !c->yrun || c->feed_on || c->edges_static) return CLIFFS_ERR_ARG;
+    if (!c->have_state) return CLIFFS_ERR_STATE;
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  auto* b = new cliffs_batch;
+  b->ctx.assign(ctxs, ctxs + n);
+  b->dev = dev;
+  auto fail = [&](int r) {
+    batch_free(b);
+    delete b;
+    return r;
+  };
+  if (cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->max_ctas, batch_persistent, kBatchThreads, 0) !=
+      cudaSuccess)
+    return fail(CLIFFS_ERR_CUDA);
+  if (!coop) b->max_ctas = 0;  // graph schedule only
+  // per scenario: the x-sweep reads copy cur and writes 1-cur, the y-sweep
+  // (with the max-wave update) reads 1-cur and writes cur
+  std::vector<SweepArgs> args(2 * (size_t)n);
+  std::vector<int> off(2 * ((size_t)n + 1), 0), gx(2 * (size_t)n, 0);
+  for (int k = 0; k < n; ++k) {
+    cliffs_ctx* c = ctxs[k];
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
+    args[2 * k] = sweep_args(c, 1, false, c->cur);
+    args[2 * k + 1] = sweep_args(c, 2, true, 1 - c->cur);
+    const int xgx = (c->nx + kBatchThreads * kCellsPerThread - 1) / (kBatchThreads * kCellsPerThread);
+    const int ygx = (c->ny + (kBatchThreads / 32) * kCellsPerThread - 1) / ((kBatchThreads / 32) * kCellsPerThread);
+    gx[k] = xgx;
+    gx[n + k] = ygx;
+    off[k + 1] = off[k] + xgx * c->ny;
+    off[(n + 1) + k + 1] = off[(n + 1) + k] + ygx * ((c->nx + 31) / 32);
+  }
+  b->total[0] = off[n];
+  b->total[1] = off[(n + 1) + n];
+  if (dalloc(&b->d_args, args.size()) || dalloc(&b->d_off, off.size()) || dalloc(&b->d_gx, gx.size()) ||
+      dalloc(&b->d_sync, 2))
+    return fail(CLIFFS_ERR_NOMEM);
+  if (cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_gx, gx.data(), gx.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking))
+    return fail(CLIFFS_ERR_CUDA);
+  b->plan.mode = b->max_ctas > 0 ? CLIFFS_BATCH_PERSISTENT : CLIFFS_BATCH_GRAPH;
+  b->plan.ctas_per_sm = std::max(1, b->max_ctas);
+  b->plan.graph_steps = 32;
+  *out = b;
+  return CLIFFS_OK;
+}
+
+void cliffs_batch_destroy(cliffs_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_free(b);
+  delete b;
+}
+
+int cliffs_batch_set_plan(cliffs_batch* b, const cliffs_batch_plan* p) {
+  if (!b || !p) return CLIFFS_ERR_ARG;
+  if (p->mode == CLIFFS_BATCH_PERSISTENT) {
+    if (p->ctas_per_sm < 1 || p->ctas_per_sm > b->max_ctas) return CLIFFS_ERR_ARG;
+  } else if (p->mode == CLIFFS_BATCH_GRAPH) {
+    if (p->graph_steps < 1 || p->graph_steps > 4096) return CLIFFS_ERR_ARG;
+  } else {
+    return CLIFFS_ERR_ARG;
+  }
+  b->plan = *p;
+  return CLIFFS_OK;
+}
+
+int cliffs_batch_get_plan(const cliffs_batch* b, cliffs_batch_plan* p) {
+  if (!b || !p) return CLIFFS_ERR_ARG;
+  *p = b->plan;
+  return CLIFFS_OK;
+}
+
+int cliffs_batch_launch_count(const cliffs_batch* b, int64_t* n) {
+  if (!b || !n) return CLIFFS_ERR_ARG;
+  *n = b->launches;
+  return CLIFFS_OK;
+}
+
+static int batch_launch_phases(cliffs_batch* b, int steps) {
+  const BatchArgs B = batch_args(b, 1);
+  for (int s = 0; s < steps; ++s) {
+    batch_phase<0><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
+    batch_phase<1><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    b->launches += 2;
+  }
+  return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+}
+
+static int batch_build_graph(cliffs_batch* b, int steps) {
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_built = 0;
+  }
+  const int64_t before = b->launches;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const int r = batch_launch_phases(b, steps);
+  const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  b->launches = before;  // captured, not launched
+  if (r || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return CLIFFS_ERR_CUDA;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return CLIFFS_ERR_CUDA;
+  b->graph_built = steps;
+  return CLIFFS_OK;
+}
+
+int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
+  if (!b || nsteps < 0) return CLIFFS_ERR_ARG;
+  if (nsteps == 0) return CLIFFS_OK;
+  int r = CLIFFS_OK;
+  if (b->plan.mode == CLIFFS_BATCH_PERSISTENT) {
+    const int grid = b->plan.ctas_per_sm * b->sms;
+    // at most 2^31 / grid barrier arrivals per launch keeps the counter exact
+    const int chunk = std::max(1, std::min(100000, (int)(0x7fffffffu / (2u * (unsigned)grid)) - 1));
+    for (int done = 0; done < nsteps && !r; done += chunk) {
+      const int steps = std::min(chunk, nsteps - done);
+      BatchArgs B = batch_args(b, steps);
+      void* kargs[] = {&B};
+      if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
+          cudaLaunchCooperativeKernel((const void*)batch_persistent, dim3(grid), dim3(kBatchThreads), kargs, 0,
+                                      b->stream) != cudaSuccess) {
+        r = CLIFFS_ERR_CUDA;
+        break;
+      }
+      ++b->launches;
+      unsigned flags[2] = {0, 0};
+      if (cudaMemcpyAsync(flags, b->d_sync, sizeof(flags), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+          cudaStreamSynchronize(b->stream) != cudaSuccess)
+        r = CLIFFS_ERR_CUDA;
+      else if (flags[1])
+        r = CLIFFS_ERR_TIMEOUT;
+    }
+  } else {
+    const int k = b->plan.graph_steps;
+    if (nsteps >= k && b->graph_built != k) r = batch_build_graph(b, k);
+    int done = 0;
+    for (; !r && done + k <= nsteps; done += k) {
+      if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+      b->launches += 2 * (int64_t)k;
+    }
+    if (!r && done < nsteps) r = batch_launch_phases(b, nsteps - done);
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r)
+    for (cliffs_ctx* c : b->ctx) c->sweeps += 2u * (unsigned)nsteps;
+  return r;
+}
+
+int cliffs_batch_check_barrier_timeout(cliffs_batch* b, int32_t wait_ms) {
+  if (!b || wait_ms < 1 || wait_ms > 2000) return CLIFFS_ERR_ARG;
+  if (b->max_ctas < 1) return CLIFFS_ERR_DEVICE;
+  BatchArgs B = batch_args(b, 1);
+  B.wait_ns = (unsigned long long)wait_ms * 1000000ull;
+  B.extra = 1;  // an arrival no block makes: the first barrier's wait runs out
+  void* kargs[] = {&B};
+  const int grid = b->sms;  // one block per SM
+  if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
+      cudaLaunchCooperativeKernel((const void*)batch_persistent, dim3(grid), dim3(kBatchThreads), kargs, 0,
+                                  b->stream) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  ++b->launches;
+  unsigned flags[2] = {0, 0};
+  if (cudaMemcpyAsync(flags, b->d_sync, sizeof(flags), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  return flags[1] ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
+}
+
+int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_step) {
+  if (!b || probe_steps < 1) return CLIFFS_ERR_ARG;
+  // snapshot of every context's state and max-wave fields
+  std::vector<float*> saved;
+  auto cleanup = [&]() {
+    for (float* p : saved) cudaFree(p);
+  };
+  auto copy_state = [&](bool save) -> int {
+    size_t k = 0;
+    for (cliffs_ctx* c : b->ctx) {
+      const size_t cells = (size_t)c->pitch * c->ny;
+      float* fields[5] = {c->srf[c->cur], c->xu[c->cur], c->yv[c->cur], c->hmax, c->velmax};
+      for (float* f : fields) {
+        if (save) {
+          float* p = nullptr;
+          if (dalloc(&p, cells)) return CLIFFS_ERR_NOMEM;
+          saved.push_back(p);
+        }
+        float* dst = save ? saved[k] : f;
+        const float* src = save ? f : saved[k];
+        if (cudaMemcpyAsync(dst, src, cells * sizeof(float), cudaMemcpyDeviceToDevice, b->stream) != cudaSuccess)
+          return CLIFFS_ERR_CUDA;
+        ++k;
+      }
+    }
+    return cudaStreamSynchronize(b->stream) == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+  };
+  int r = copy_state(true);
+  if (r) {
+    cleanup();
+    return r;
+  }
+  std::vector<cliffs_batch_plan> cand;
+  for (int k = 1; k <= b->max_ctas; ++k) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_PERSISTENT, k, 32});
+  for (int g : {8, 32}) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_GRAPH, 1, g});
+  const cliffs_batch_plan keep = b->plan;
+  cliffs_batch_plan best = keep;
+  double best_ms = 1e300;
+  const int64_t launches0 = b->launches;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) || cudaEventCreate(&e1)) r = CLIFFS_ERR_CUDA;
+  for (const cliffs_batch_plan& p : cand) {
+    if (r) break;
+    b->plan = p;
+    r = cliffs_batch_step(b, 1);  // warm-up; builds the graph of a graph plan
+    if (!r && cudaEventRecord(e0, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+    if (!r) r = cliffs_batch_step(b, probe_steps);
+    if (!r && cudaEventRecord(e1, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+    float ms = 0;
+    if (!r && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      r = CLIFFS_ERR_CUDA;
+    if (!r && ms / probe_steps < best_ms) {
+      best_ms = ms / probe_steps;
+      best = p;
+    }
+    if (!r) r = copy_state(false);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  // the probes advanced the contexts' sweep counters; the restored state is
+  // the one before the probes
+  const int64_t probes = (int64_t)cand.size() * (probe_steps + 1);
+  for (cliffs_ctx* c : b->ctx) c->sweeps -= (unsigned)(2 * probes);
+  b->launches = launches0;
+  cleanup();
+  b->plan = r ? keep : best;
+  if (!r && ms_per_step) *ms_per_step = best_ms;
+  return r;
+}

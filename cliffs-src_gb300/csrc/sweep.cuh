@@ -59,6 +59,20 @@ struct SweepArgs {
 
 enum : unsigned { ST_NAN = 1u };
 
+// Loads of the state fields (surface, u, v, max-wave).  A sweep kernel reads
+// the fields another launch wrote, through the read-only path (COH = false).
+// The batched persistent kernel (batch.cuh) reads fields that other blocks of
+// the same launch wrote before a grid barrier: those loads go to L2
+// (COH = true), where the writes are, not to a possibly stale L1 line.
+template <bool COH>
+__device__ __forceinline__ float ld_state(const float* p) {
+  return COH ? __ldcg(p) : __ldg(p);
+}
+template <bool COH>
+__device__ __forceinline__ float4 ld_state4(const float* p) {
+  return COH ? __ldcg(reinterpret_cast<const float4*>(p)) : __ldg(reinterpret_cast<const float4*>(p));
+}
+
 template <int DIR>
 __device__ __forceinline__ size_t cidx(int L, int k, int pitch) {
   // DIR 0: line L is row j, position k is column i; DIR 1: line L is column i
@@ -86,7 +100,7 @@ __device__ __forceinline__ EdgeVals<float> edge_vals(const SweepArgs& A, int L, 
 }
 
 // The cell's value through the full wet/dry rules (cliffs.f:56-329).
-template <int DIR>
+template <int DIR, bool COH>
 __device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L, int o, float alpha, float ialpha,
                                                        const EdgeVals<float>& eL, const EdgeVals<float>& eR) {
   const int n = A.n;
@@ -99,8 +113,9 @@ __device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L
     w[t] = RawCell<float>{0.f, 0.f, 0.f, 0.f, false};
     if (k >= 1 && k <= n) {
       const size_t q = cidx<DIR>(L, k, A.pitch);
-      const float xu = __ldg(A.xu + q), yv = __ldg(A.yv + q);
-      w[t] = RawCell<float>{__ldg(A.dep + q), __ldg(A.srf + q), DIR == 0 ? xu : yv, DIR == 0 ? yv : xu, true};
+      const float xu = ld_state<COH>(A.xu + q), yv = ld_state<COH>(A.yv + q);
+      w[t] = RawCell<float>{__ldg(A.dep + q), ld_state<COH>(A.srf + q), DIR == 0 ? xu : yv, DIR == 0 ? yv : xu,
+                            true};
       anywet |= depth_of(w[t].s, w[t].d) > p.ground;
     }
   }
@@ -111,7 +126,7 @@ __device__ __forceinline__ OutCell<float> general_path(const SweepArgs& A, int L
     // does the line hold a wet cell anywhere (cliffs.f:113)?
     for (int k = 1; k <= n && !C.wet; ++k) {
       const size_t q = cidx<DIR>(L, k, A.pitch);
-      C.wet = depth_of(__ldg(A.srf + q), __ldg(A.dep + q)) > p.ground;
+      C.wet = depth_of(ld_state<COH>(A.srf + q), __ldg(A.dep + q)) > p.ground;
     }
   }
   C.eL = eL;
@@ -141,7 +156,7 @@ __device__ __forceinline__ void enqueue(const SweepArgs& A, bool want, uint32_t 
 constexpr int kCellsPerThread = 4;
 
 // One listed cell through the full rules, written with its max-wave update.
-template <int DIR>
+template <int DIR, bool COH>
 __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   const int n = A.n;
   const int L = (int)(ent / (uint32_t)n) + 1;
@@ -157,12 +172,12 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   const float dq = __ldg(A.dep + q);
   float hm = 0.f, vm = 0.f;
   if (A.hmax) {
-    hm = A.hmax[q];
-    vm = A.velmax[q];
+    hm = ld_state<COH>(A.hmax + q);
+    vm = ld_state<COH>(A.velmax + q);
   }
   const EdgeVals<float> eL = o == 1 ? edge_vals(A, L, 0) : EdgeVals<float>{0.f, 0.f, 0.f};
   const EdgeVals<float> eR = o == n ? edge_vals(A, L, 1) : EdgeVals<float>{0.f, 0.f, 0.f};
-  const OutCell<float> r = general_path<DIR>(A, L, o, alpha, ialpha, eL, eR);
+  const OutCell<float> r = general_path<DIR, COH>(A, L, o, alpha, ialpha, eL, eR);
   const float xo = DIR == 0 ? r.u : r.v;
   const float yo = DIR == 0 ? r.v : r.u;
   A.srf_o[q] = r.s;
@@ -178,25 +193,28 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
 // LOCAL: the block finishes its own listed cells after its fast cells (a
 // block-local list in shared memory); otherwise they go to the global
 // worklist for general_kernel.
-template <int DIR, bool LOCAL>
-__global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
+// One tile of a sweep: the block's cells at block coordinates (bx, by) of the
+// sweep's grid (x: (columns / (4 * blockDim.x), rows); y: (rows / (4 * warps),
+// columns / 32)).  The whole block calls it.
+template <int DIR, bool LOCAL, bool COH>
+__device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
   __shared__ uint32_t s_list[LOCAL ? 256 * 4 : 1];
   __shared__ unsigned s_n;
   if (LOCAL) {
     if (threadIdx.x == 0) s_n = 0u;
     __syncthreads();
-  } else if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+  } else if (bx == 0 && by == 0 && threadIdx.x == 0) {
     *A.count_next = 0u;
   }
   const int lane = threadIdx.x & 31;
   const int n = A.n;
   int L, i0;  // line, first position (1-based)
   if (DIR == 0) {
-    L = blockIdx.y + 1;
-    i0 = (blockIdx.x * blockDim.x + threadIdx.x) * kCellsPerThread + 1;
+    L = by + 1;
+    i0 = (bx * (int)blockDim.x + (int)threadIdx.x) * kCellsPerThread + 1;
   } else {
-    L = blockIdx.y * 32 + lane + 1;
-    i0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kCellsPerThread + 1;
+    L = by * 32 + lane + 1;
+    i0 = (bx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5)) * kCellsPerThread + 1;
   }
   const bool active = L <= A.nlines && i0 <= n;
   const bool swept = active && L >= A.lo && L <= A.hi;
@@ -211,12 +229,12 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
     float4 D4 = make_float4(0, 0, 0, 0), E4 = D4, X4 = D4, Y4 = D4, H4 = D4, V4 = D4;
     if (active) {
       D4 = __ldg(reinterpret_cast<const float4*>(A.dep + q0));
-      E4 = __ldg(reinterpret_cast<const float4*>(A.srf + q0));
-      X4 = __ldg(reinterpret_cast<const float4*>(A.xu + q0));
-      Y4 = __ldg(reinterpret_cast<const float4*>(A.yv + q0));
+      E4 = ld_state4<COH>(A.srf + q0);
+      X4 = ld_state4<COH>(A.xu + q0);
+      Y4 = ld_state4<COH>(A.yv + q0);
       if (A.hmax) {
-        H4 = *reinterpret_cast<const float4*>(A.hmax + q0);
-        V4 = *reinterpret_cast<const float4*>(A.velmax + q0);
+        H4 = ld_state4<COH>(A.hmax + q0);
+        V4 = ld_state4<COH>(A.velmax + q0);
       }
     }
     d[1] = D4.x; d[2] = D4.y; d[3] = D4.z; d[4] = D4.w;
@@ -235,15 +253,15 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
     v[5] = __shfl_down_sync(0xffffffffu, Y4.x, 1);
     if (active && lane == 0 && i0 > 1) {
       d[0] = __ldg(A.dep + q0 - 1);
-      e[0] = __ldg(A.srf + q0 - 1);
-      u[0] = __ldg(A.xu + q0 - 1);
-      v[0] = __ldg(A.yv + q0 - 1);
+      e[0] = ld_state<COH>(A.srf + q0 - 1);
+      u[0] = ld_state<COH>(A.xu + q0 - 1);
+      v[0] = ld_state<COH>(A.yv + q0 - 1);
     }
     if (active && lane == 31 && i0 + 4 <= n) {
       d[5] = __ldg(A.dep + q0 + 4);
-      e[5] = __ldg(A.srf + q0 + 4);
-      u[5] = __ldg(A.xu + q0 + 4);
-      v[5] = __ldg(A.yv + q0 + 4);
+      e[5] = ld_state<COH>(A.srf + q0 + 4);
+      u[5] = ld_state<COH>(A.xu + q0 + 4);
+      v[5] = ld_state<COH>(A.yv + q0 + 4);
     }
   } else {
 #pragma unroll
@@ -253,9 +271,9 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
       d[w] = e[w] = u[w] = v[w] = 0.f;
       if (active) {
         d[w] = __ldg(A.dep + q);
-        e[w] = __ldg(A.srf + q);
-        v[w] = __ldg(A.xu + q);  // tangential in the y-sweep
-        u[w] = __ldg(A.yv + q);  // normal
+        e[w] = ld_state<COH>(A.srf + q);
+        v[w] = ld_state<COH>(A.xu + q);  // tangential in the y-sweep
+        u[w] = ld_state<COH>(A.yv + q);  // normal
       }
     }
 #pragma unroll
@@ -264,8 +282,8 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
       const int k = min(i0 + r, n);
       if (active && A.hmax) {
         const size_t q = cidx<1>(L, k, A.pitch);
-        hm[r] = A.hmax[q];
-        vm[r] = A.velmax[q];
+        hm[r] = ld_state<COH>(A.hmax + q);
+        vm[r] = ld_state<COH>(A.velmax + q);
       }
     }
   }
@@ -411,8 +429,13 @@ __global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
   if (LOCAL) {
     __syncthreads();  // the block's fast values are stored; its listed cells overwrite theirs
     const unsigned cnt = s_n;
-    for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) general_store<DIR>(A, s_list[t]);
+    for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) general_store<DIR, COH>(A, s_list[t]);
   }
+}
+
+template <int DIR, bool LOCAL>
+__global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
+  sweep_tile<DIR, LOCAL, false>(A, blockIdx.x, blockIdx.y);
 }
 
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
@@ -420,7 +443,7 @@ template <int DIR>
 __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {
   const uint32_t cnt = *A.count;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
-    general_store<DIR>(A, A.list[t]);
+    general_store<DIR, false>(A, A.list[t]);
   }
 }
 

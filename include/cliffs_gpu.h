@@ -35,7 +35,8 @@ enum {
   CLIFFS_ERR_NAN = -3,        /* a non-finite eta/u/v appeared */
   CLIFFS_ERR_NOMEM = -4,      /* device allocation failed */
   CLIFFS_ERR_STATE = -5,      /* call out of order (e.g. no state uploaded) */
-  CLIFFS_ERR_DEVICE = -6      /* no usable sm_103 device */
+  CLIFFS_ERR_DEVICE = -6,     /* no usable sm_103 device */
+  CLIFFS_ERR_TIMEOUT = -7     /* a device-side wait ran out (batch barrier) */
 };
 
 /* status bits reported by cliffs_gpu_status() */
@@ -223,6 +224,49 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch,
                              float *srf_out, float *xvel_out, float *yvel_out,
                              double dx, double dy, double ground, double crough,
                              double dt, void *stream);
+
+/* ---- ensembles ------------------------------------------------------------
+ * No reference counterpart: the reference runs one grid per process.  A batch
+ * steps many independent contexts (one source scenario each, grids of any
+ * size) together: every scenario's sweeps are cut into the single-grid
+ * kernels' tiles, the tiles of all scenarios form one list per sweep
+ * direction, and either one cooperative launch covers many steps (blocks meet
+ * at a grid barrier between the x and y phases) or one launch per phase and
+ * step covers every scenario, replayed from a CUDA graph.  Results are
+ * bit-identical to stepping the contexts one by one with cliffs_gpu_step.
+ * Contexts must be 2-D, hold a state, have no boundary forcing, and live on
+ * the current device; their own entry points (gauges, max-wave, runup,
+ * download) stay usable between batch steps.  The caller keeps each
+ * context's model time (t += nsteps * dt). */
+typedef struct cliffs_batch cliffs_batch;
+enum { CLIFFS_BATCH_PERSISTENT = 0, CLIFFS_BATCH_GRAPH = 1 };
+typedef struct cliffs_batch_plan {
+  int32_t mode;         /* CLIFFS_BATCH_PERSISTENT or CLIFFS_BATCH_GRAPH */
+  int32_t ctas_per_sm;  /* persistent: resident blocks per SM of the launch */
+  int32_t graph_steps;  /* graph: steps captured in one CUDA graph */
+} cliffs_batch_plan;
+
+int cliffs_batch_create(cliffs_ctx *const *ctxs, int32_t n, cliffs_batch **out);
+void cliffs_batch_destroy(cliffs_batch *b);
+int cliffs_batch_set_plan(cliffs_batch *b, const cliffs_batch_plan *plan);
+int cliffs_batch_get_plan(const cliffs_batch *b, cliffs_batch_plan *plan);
+/* Advance every context nsteps steps; synchronises at the end.  Returns
+ * CLIFFS_ERR_TIMEOUT if a grid barrier wait ran out (the state is then
+ * partial). */
+int cliffs_batch_step(cliffs_batch *b, int32_t nsteps);
+/* Time the candidate plans (persistent with 1..max resident blocks per SM,
+ * graphs of 8 and 32 steps) over probe_steps steps each from a snapshot of
+ * the state, restore the snapshot and keep the fastest plan; *ms_per_step
+ * gets its time per step. */
+int cliffs_batch_autotune(cliffs_batch *b, int32_t probe_steps, double *ms_per_step);
+/* Failure-detection check of the grid barrier: one persistent launch whose
+ * first barrier waits for an arrival that no block makes, with the wait
+ * limited to wait_ms (1..2000).  Expected result: CLIFFS_ERR_TIMEOUT, read by
+ * the host, with the device usable afterwards.  The launch applies the
+ * x-sweep of one step to the contexts before the barrier. */
+int cliffs_batch_check_barrier_timeout(cliffs_batch *b, int32_t wait_ms);
+/* Kernels the batch has launched (a persistent launch counts once). */
+int cliffs_batch_launch_count(const cliffs_batch *b, int64_t *n);
 
 const char *cliffs_gpu_strerror(int code);
 
