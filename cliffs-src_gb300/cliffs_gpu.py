@@ -46,6 +46,22 @@ class Runup(ctypes.Structure):
                 ("wet_now", ctypes.c_int64)]
 
 
+class SourceDesc(ctypes.Structure):
+    _fields_ = [("x0", ctypes.c_double), ("y0", ctypes.c_double), ("ax", ctypes.c_double),
+                ("ay", ctypes.c_double), ("angle", ctypes.c_double), ("amp", ctypes.c_double),
+                ("dipole", ctypes.c_double), ("rise_time", ctypes.c_double), ("bottom", ctypes.c_int32)]
+
+
+def source_field(x, y, *, x0, y0, ax, ay, angle=0.0, amp=1.0, dipole=0.0):
+    """The uplift of cliffs_gpu_add_source on the grid (ny, nx), in numpy FP64."""
+    X, Y = np.meshgrid(np.asarray(x, np.float64), np.asarray(y, np.float64))
+    dx, dy = X - x0, Y - y0
+    ca, sa = np.cos(angle), np.sin(angle)
+    xi, et = ca * dx + sa * dy, -sa * dx + ca * dy
+    a, b, b2 = xi / ax, et / ay, (et + 2.0 * ay) / ay
+    return amp * (np.exp(-(a * a + b * b)) - dipole * np.exp(-(a * a + b2 * b2)))
+
+
 class BatchPlan(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("graph_steps", ctypes.c_int32)]
@@ -93,6 +109,7 @@ SIGNATURES = {
     "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
+    "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
     "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),
     "cliffs_batch_destroy": ([_V], None),
     "cliffs_batch_set_plan": ([_V, ctypes.POINTER(BatchPlan)], ctypes.c_int),
@@ -242,6 +259,14 @@ class GpuGrid:
         return np.where(cel > self.celmin, H - self.dep, np.nan)
 
     # -- forcing --------------------------------------------------------------
+    def add_source(self, x, y, *, x0, y0, ax, ay, angle=0.0, amp=1.0, dipole=0.0, rise_time=0.0,
+                   bottom=False):
+        """An analytic uplift (cliffs_gpu_add_source) on grid coordinates x, y."""
+        d = SourceDesc(float(x0), float(y0), float(ax), float(ay), float(angle), float(amp),
+                       float(dipole), float(rise_time), int(bool(bottom)))
+        _chk(self.L.cliffs_gpu_add_source(self.h, _p(_f64(x)), _p(_f64(y)), ctypes.byref(d)),
+             "add_source")
+
     def set_feed(self, tinput, west=None, east=None, south=None, north=None, irec=1, freeze=True):
         arr = [_f64(a) for a in (tinput, west, east, south, north)]
         self._feed = arr

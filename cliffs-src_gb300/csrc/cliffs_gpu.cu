@@ -54,6 +54,11 @@ struct cliffs_ctx {
   int cur = 0;
   int64_t launches = 0;  // kernels this context has launched
   std::vector<double> dep64;  // the caller's FP64 depth, for the state conversions
+  // a source rising over time (cliffs_gpu_add_source): its full uplift, its
+  // duration, the time since it was added and the fraction applied so far
+  float* rise_q = nullptr;
+  double rise_T = 0, rise_el = 0, rise_w = 0;
+  bool rise_on = false;
   float4 *geo_x = nullptr, *geo_y = nullptr;
   float* scl_y = nullptr;
   float2* lscale = nullptr;
@@ -382,6 +387,66 @@ constexpr int kGeneralBlocks = 304;
 
 // Launch one sweep: the fast kernel, then the general kernel over the cells it
 // listed.  fuse_max: update hmax/velmax on the way out.
+// ---- analytic sources (cliffs_gpu_add_source) --------------------------------
+
+struct SourceParams {
+  double x0, y0, ax, ay, ca, sa, amp, dipole;
+};
+
+// Uplift of an elliptical Gaussian with its first axis rotated by angle from
+// +x, minus a trough of relative depth `dipole` two half-widths along the
+// second axis.
+__device__ __forceinline__ double source_at(const SourceParams& S, double x, double y) {
+  const double dx = x - S.x0, dy = y - S.y0;
+  const double xi = S.ca * dx + S.sa * dy, et = -S.sa * dx + S.ca * dy;
+  const double a = xi / S.ax, b = et / S.ay, b2 = (et + 2.0 * S.ay) / S.ay;
+  return S.amp * (exp(-(a * a + b * b)) - S.dipole * exp(-(a * a + b2 * b2)));
+}
+
+__global__ void k_source(int nx, int ny, int pitch, const double* __restrict__ x, const double* __restrict__ y,
+                         SourceParams S, float* q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= pitch || j >= ny) return;
+  q[(size_t)j * pitch + i] = i < nx ? (float)source_at(S, x[i], y[j]) : 0.f;
+}
+
+// The surface rises by (w_now - w_prev) q where water stands; a dry cell takes
+// the water column dep + w_now q once that exceeds ground, as the initial
+// surface deformation of cliffs_main.f:209-213 does before the celerity
+// transform.
+__global__ void k_add_surface(int nx, int ny, int pitch, const float* __restrict__ dep, float* srf,
+                              const float* __restrict__ q, float w_now, float w_prev, float ground) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)j * pitch + i;
+  const float d = dep[k], s = srf[k], qq = q[k];
+  if (depth_of(s, d) > ground) {
+    srf[k] = s + (w_now - w_prev) * qq;  // eta and H move together
+  } else {
+    const float Hd = d + w_now * qq;
+    if (Hd > ground) srf[k] = state_from_depth(Hd, d);
+  }
+}
+
+// The bottom moves from dep_old to dep_new under a standing water column
+// (cliffs_main.f:205-208): eta rises where it is sea before and after, the
+// depth stays where it is land before and after, and a cell changing sides
+// converts through its total depth.
+__global__ void k_move_bottom(int nx, int ny, int pitch, const float* __restrict__ dep_old,
+                              const float* __restrict__ dep_new, float* srf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)j * pitch + i;
+  const float d0 = dep_old[k], d1 = dep_new[k], s = srf[k];
+  if (d0 >= 0.f && d1 >= 0.f)
+    srf[k] = s + (d0 - d1);
+  else if (!(d0 < 0.f && d1 < 0.f))
+    srf[k] = state_from_depth(depth_of(s, d0), d1);
+}
+
 // The arguments of one sweep reading state copy s and writing 1 - s.
 SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
   SweepArgs A{};
@@ -650,7 +715,8 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   void* ptrs[] = {c->dep, c->srf[0], c->srf[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
                   c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
-                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y};
+                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y,
+                  c->rise_q};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& n : c->nests) {
@@ -740,6 +806,69 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (b) cudaFree(b);
   if (e) cudaFree(e);
   if (dd) cudaFree(dd);
+  return r;
+}
+
+int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd, const cliffs_source* src) {
+  if (!c || !xcrd || !ycrd || !src) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if (!(src->ax > 0) || !(src->ay > 0) || !(src->rise_time >= 0) || !std::isfinite(src->amp) ||
+      !std::isfinite(src->dipole) || (src->bottom && src->rise_time > 0) || c->rise_on)
+    return CLIFFS_ERR_ARG;
+  const size_t cells = (size_t)c->pitch * c->ny;
+  double *dx = nullptr, *dy = nullptr;
+  float *q = nullptr, *dnew = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&dx, (size_t)c->nx) || dalloc(&dy, (size_t)c->ny) || dalloc(&q, cells)) r = CLIFFS_ERR_NOMEM;
+  if (!r && (cudaMemcpyAsync(dx, xcrd, c->nx * sizeof(double), cudaMemcpyHostToDevice, c->stream) ||
+             cudaMemcpyAsync(dy, ycrd, c->ny * sizeof(double), cudaMemcpyHostToDevice, c->stream)))
+    r = CLIFFS_ERR_CUDA;
+  SourceParams S{src->x0, src->y0, src->ax, src->ay, cos(src->angle), sin(src->angle), src->amp, src->dipole};
+  if (!r) {
+    ++c->launches;
+    k_source<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, dx, dy, S, q);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && src->bottom) {
+    // the FP64 depth moves on the host, the device depth is its rounding
+    std::vector<float> hq(cells), hd(cells, 0.f);
+    if (cudaMemcpyAsync(hq.data(), q, cells * sizeof(float), cudaMemcpyDeviceToHost, c->stream) ||
+        cudaStreamSynchronize(c->stream))
+      r = CLIFFS_ERR_CUDA;
+    for (int j = 0; !r && j < c->ny; ++j)
+      for (int i = 0; i < c->nx; ++i) {
+        double& d = c->dep64[(size_t)j * c->nx + i];
+        d -= (double)hq[(size_t)j * c->pitch + i];
+        hd[(size_t)j * c->pitch + i] = (float)d;
+      }
+    if (!r && (dalloc(&dnew, cells) ||
+               cudaMemcpyAsync(dnew, hd.data(), cells * sizeof(float), cudaMemcpyHostToDevice, c->stream)))
+      r = CLIFFS_ERR_CUDA;
+    if (!r) {
+      ++c->launches;
+      k_move_bottom<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dnew,
+                                                                c->srf[c->cur]);
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(c->dep, dnew, cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream))
+        r = CLIFFS_ERR_CUDA;
+    }
+  } else if (!r && src->rise_time == 0) {
+    ++c->launches;
+    k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur], q,
+                                                              1.f, 0.f, (float)c->ground);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  } else if (!r) {  // applied step by step from now on
+    std::swap(c->rise_q, q);
+    c->rise_T = src->rise_time;
+    c->rise_el = 0;
+    c->rise_w = 0;
+    c->rise_on = true;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(dx);
+  cudaFree(dy);
+  if (q) cudaFree(q);
+  if (dnew) cudaFree(dnew);
   return r;
 }
 
@@ -844,6 +973,17 @@ int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_don
     }
     double cc = 0;
     if (c->feed_on) cc = (c->tinput[c->irec - 1] - *t) / (c->tinput[c->irec - 1] - c->tinput[c->irec - 2]);
+    if (c->rise_on) {  // the rising source's share of this step
+      c->rise_el += c->dt;
+      const double w = std::min(1.0, c->rise_el / c->rise_T);
+      ++c->launches;
+      k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
+                                                                c->rise_q, (float)w, (float)c->rise_w,
+                                                                (float)c->ground);
+      CK(cudaGetLastError());
+      c->rise_w = w;
+      if (w >= 1.0) c->rise_on = false;
+    }
     if (c->xrun) {
       int r = launch_sweep(c, 1, !c->yrun, c->feed_on ? c->fw : nullptr, c->feed_on ? c->fe : nullptr, c->ny,
                            c->irec, cc);
@@ -1337,7 +1477,8 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
   if (cudaGetDevice(&dev) != cudaSuccess) return CLIFFS_ERR_DEVICE;
   for (int k = 0; k < n; ++k) {
     const cliffs_ctx* c = ctxs[k];
-    if (!c || c->dev != dev || !c->xrun || !c->yrun || c->feed_on || c->edges_static) return CLIFFS_ERR_ARG;
+    if (!c || c->dev != dev || !c->xrun || !c->yrun || c->feed_on || c->edges_static || c->rise_on)
+      return CLIFFS_ERR_ARG;
     if (!c->have_state) return CLIFFS_ERR_STATE;
   }
   int coop = 0;

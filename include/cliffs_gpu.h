@@ -113,6 +113,30 @@ int cliffs_gpu_upload_state(cliffs_ctx *ctx, const double *cel,
 int cliffs_gpu_download_state(cliffs_ctx *ctx, double *cel, double *xvel,
                               double *yvel);
 
+/* Analytic source (no reference counterpart; the reference reads a deformation
+ * lattice and interpolates it, apply_initial_conditions.f, which the driver
+ * keeps).  Uplift q(x,y) = amp * (exp(-(a^2+b^2)) - dipole * exp(-(a^2+b2^2)))
+ * with (a, b) the offset from (x0, y0) in the source's own axes (first axis
+ * rotated by angle from +x, counter-clockwise) divided by (ax, ay), and b2 =
+ * b + 2 (a trough two half-widths along the second axis).  Coordinates are
+ * the grid's (metres, or degrees on a spherical grid). */
+typedef struct cliffs_source {
+  double x0, y0;     /* centre */
+  double ax, ay;     /* e-folding half-widths along the source's axes (> 0) */
+  double angle;      /* radians, counter-clockwise from +x */
+  double amp;        /* peak uplift (m) */
+  double dipole;     /* trough depth as a fraction of amp (0: none) */
+  double rise_time;  /* s: the surface uplift grows linearly over this time,
+                        applied by cliffs_gpu_step; 0: at once */
+  int32_t bottom;    /* 1: the bottom moves under the water column
+                        (cliffs_main.f:205-208, quake = 1; rise_time must be
+                        0); 0: the surface moves (209-213) */
+} cliffs_source;
+/* Evaluate the source on the device (FP64) and apply it to the current state;
+ * xcrd (nx), ycrd (ny) are the grid coordinates. */
+int cliffs_gpu_add_source(cliffs_ctx *ctx, const double *xcrd, const double *ycrd,
+                          const cliffs_source *src);
+
 /* Boundary forcing (get_boundary_feed.f): nt records at times tinput(nt);
  * west/east (ny,3,nt) and south/north (nx,3,nt) hold (u, v, eta) per edge
  * node, either pair may be NULL when that sweep does not run.  irec is the
