@@ -1477,8 +1477,7 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
   if (cudaGetDevice(&dev) != cudaSuccess) return CLIFFS_ERR_DEVICE;
   for (int k = 0; k < n; ++k) {
     const cliffs_ctx* c = ctxs[k];
-    if (!c || c->dev != dev || !c->xrun || !c->yrun || c->feed_on || c->edges_static || c->rise_on)
-      return CLIFFS_ERR_ARG;
+    if (!c || c->dev != dev || !c->xrun || !c->yrun || c->feed_on || c->edges_static) return CLIFFS_ERR_ARG;
     if (!c->have_state) return CLIFFS_ERR_STATE;
   }
   int coop = 0;
@@ -1594,10 +1593,40 @@ static int batch_build_graph(cliffs_batch* b, int steps) {
   return CLIFFS_OK;
 }
 
+// Steps while a source is still rising: each rising context's share of the
+// step (as cliffs_gpu_step applies it), then the batched sweep phases.
+static int batch_rising_steps(cliffs_batch* b, int* nsteps) {
+  int r = CLIFFS_OK;
+  auto rising = [&]() {
+    for (cliffs_ctx* c : b->ctx)
+      if (c->rise_on) return true;
+    return false;
+  };
+  while (*nsteps > 0 && !r && rising()) {
+    for (cliffs_ctx* c : b->ctx) {
+      if (!c->rise_on) continue;
+      c->rise_el += c->dt;
+      const double w = std::min(1.0, c->rise_el / c->rise_T);
+      k_add_surface<<<grid2(c->nx, c->ny), 128, 0, b->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
+                                                                 c->rise_q, (float)w, (float)c->rise_w,
+                                                                 (float)c->ground);
+      ++b->launches;
+      c->rise_w = w;
+      if (w >= 1.0) c->rise_on = false;
+    }
+    r = batch_launch_phases(b, 1);
+    for (cliffs_ctx* c : b->ctx) c->sweeps += 2u;
+    --*nsteps;
+  }
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  return r;
+}
+
 int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
   if (!b || nsteps < 0) return CLIFFS_ERR_ARG;
+  int r = batch_rising_steps(b, &nsteps);
+  if (r) return r;
   if (nsteps == 0) return CLIFFS_OK;
-  int r = CLIFFS_OK;
   if (b->plan.mode == CLIFFS_BATCH_PERSISTENT) {
     const int grid = b->plan.ctas_per_sm * b->sms;
     // at most 2^31 / grid barrier arrivals per launch keeps the counter exact
@@ -1683,6 +1712,19 @@ int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_s
     }
     return cudaStreamSynchronize(b->stream) == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
   };
+  struct Rise {
+    double el, w;
+    bool on;
+  };
+  std::vector<Rise> rise;
+  for (cliffs_ctx* c : b->ctx) rise.push_back(Rise{c->rise_el, c->rise_w, c->rise_on});
+  auto restore_rise = [&]() {
+    for (size_t k = 0; k < b->ctx.size(); ++k) {
+      b->ctx[k]->rise_el = rise[k].el;
+      b->ctx[k]->rise_w = rise[k].w;
+      b->ctx[k]->rise_on = rise[k].on;
+    }
+  };
   int r = copy_state(true);
   if (r) {
     cleanup();
@@ -1712,6 +1754,7 @@ int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_s
       best = p;
     }
     if (!r) r = copy_state(false);
+    restore_rise();
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

@@ -259,7 +259,8 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch,
  * step covers every scenario, replayed from a CUDA graph.  Results are
  * bit-identical to stepping the contexts one by one with cliffs_gpu_step.
  * Contexts must be 2-D, hold a state, have no boundary forcing, and live on
- * the current device; their own entry points (gauges, max-wave, runup,
+ * the current device; a source still rising (cliffs_gpu_add_source) is
+ * stepped through its rise one step at a time before the plan takes over; their own entry points (gauges, max-wave, runup,
  * download) stay usable between batch steps.  The caller keeps each
  * context's model time (t += nsteps * dt). */
 typedef struct cliffs_batch cliffs_batch;

@@ -112,3 +112,23 @@ def test_batch_rejects_what_it_cannot_step():
                 np.zeros((nt, 3, c2["dep"].shape[1])), irec=2, freeze=False)
     with pytest.raises(cg.CliffsError):
         pkg.Batch([g2])  # boundary forcing is per grid
+
+
+def test_batch_with_rising_sources_is_bit_identical():
+    cases = _cases()[:4]
+    grids = [pkg.GpuGrid.from_case(c) for c in cases]
+    twins = [pkg.GpuGrid.from_case(c) for c in cases]
+    for k, (g, t, c) in enumerate(zip(grids, twins, cases)):
+        L = c["xcrd"][-1]
+        src = dict(x0=0.4 * L, y0=0.5 * c["ycrd"][-1], ax=0.15 * L, ay=0.1 * L, angle=0.3 * k, amp=1.0,
+                   dipole=0.2, rise_time=(3 + 4 * k) * c["dt"] if k % 2 == 0 else 0.0)
+        g.add_source(c["xcrd"], c["ycrd"], **src)
+        t.add_source(c["xcrd"], c["ycrd"], **src)
+    b = pkg.Batch(grids)
+    b.set_plan(cg.GRAPH, graph_steps=8)
+    b.step(30)
+    for t in twins:
+        t.step(30)
+    for g, t in zip(grids, twins):
+        _same(g, t)
+    b.close()
