@@ -14,14 +14,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libcliffs_gpu.so")
-SRC = os.path.join(HERE, "csrc", "cliffs_gpu.cu")
+SRC = [os.path.join(HERE, "csrc", "cliffs_gpu.cu"), os.path.join(HERE, "csrc", "mlp.cu")]
 DRIVER = os.path.join(LIBDIR, "cliffs_gb300")
 HOST_SRC = sorted(glob.glob(os.path.join(HERE, "host", "*.cpp")))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
 def _deps():
-    return glob.glob(os.path.join(HERE, "csrc", "*")) + [os.path.join(ROOT, "include", "cliffs_gpu.h")]
+    return glob.glob(os.path.join(HERE, "csrc", "*")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
 
 
 def nvcc():
@@ -55,8 +55,8 @@ def build_lib(force: bool = False, verbose: bool = False) -> str:
         if os.path.getmtime(LIB) >= max(os.path.getmtime(p) for p in _deps()):
             return LIB
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
-           "-shared", SRC, "-o", tmp]
+    cmd = [nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", "--threads", "2",
+           "-shared", *SRC, "-o", tmp]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     subprocess.run(cmd, check=True)

@@ -118,6 +118,18 @@ SIGNATURES = {
     "cliffs_batch_autotune": ([_V, _I, _dp], ctypes.c_int),
     "cliffs_batch_check_barrier_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_batch_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_mlp_create": ([ctypes.c_void_p, ctypes.POINTER(_V)], ctypes.c_int),
+    "cliffs_mlp_destroy": ([_V], None),
+    "cliffs_mlp_layers": ([_V, ctypes.POINTER(_I)], ctypes.c_int),
+    "cliffs_mlp_shape": ([_V, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], ctypes.c_int),
+    "cliffs_mlp_get": ([_V, _I, _I, ctypes.POINTER(ctypes.c_float), ctypes.c_int64], ctypes.c_int),
+    "cliffs_mlp_set": ([_V, _I, _I, ctypes.POINTER(ctypes.c_float), ctypes.c_int64], ctypes.c_int),
+    "cliffs_mlp_predict": ([_V, _I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "cliffs_mlp_gradients": ([_V, _I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                              ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "cliffs_mlp_train": ([_V, _I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _I, _I,
+                          ctypes.c_float, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "cliffs_mlp_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_sweep_noalloc": ([_I, _I, _I, _I] + [_V] * 7 + [_D] * 5 + [_V], ctypes.c_int),
 }
 

@@ -1,0 +1,609 @@
+// mlp.cu -- the surrogate network of include/cliffs_surrogate.h.
+//
+// A ReLU multilayer perceptron, trained and evaluated on the GPU:
+//   forward   H_{l+1} = relu(H_l W_l^T + b_l), out = H_d W_d^T + b_d
+//   loss      mean over batch and outputs of (out - t)^2
+//   backward  dW_l = dY_l^T H_l, db_l = sum_b dY_l, dH_l = dY_l W_l
+//   update    Adam (FP32 master weights and moments), BF16 copies refreshed
+// Every matrix product is gemm_tn below: C = A B^T with both operands in BF16
+// and their reduction dimension contiguous, on the tensor cores through
+// mma.sync m16n8k16 with FP32 accumulation; the epilogue adds the bias,
+// applies the ReLU and writes the activations in the two layouts the backward
+// pass reads (row-major for dH = dY W, transposed for dW = dY^T H).  Sizes are
+// small (a few hundred to a few thousand rows); one 64x64 tile per block of
+// four warps, K in steps of 32 through shared memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../include/cliffs_gpu.h"
+#include "../../include/cliffs_surrogate.h"
+
+namespace cliffs_nn {
+
+using bf16 = __nv_bfloat16;
+constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+
+inline int pad16(int n) { return (n + 15) & ~15; }
+
+struct Epi {
+  const float* bias;  // [N] or null
+  int relu;
+  float* f32;         // [M][ldf] or null
+  int ldf;
+  bf16* b16;          // [M][ldb] or null
+  int ldb;
+  bf16* b16t;         // [N][ldt] (transposed) or null
+  int ldt;
+};
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[M,N] = A[M,K] B[N,K]^T.  A and B are BF16 with K contiguous (leading
+// dimensions lda, ldb, multiples of 8, 16-byte aligned rows); K is a multiple
+// of 16 and both operands hold zeros in [K, round_up(K, 32)) or that range is
+// past the end of the tile load (guarded).  M and N are arbitrary.
+__global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* __restrict__ A, int lda,
+                                               const bf16* __restrict__ B, int ldb, Epi e) {
+  __shared__ __align__(16) bf16 sA[BM][BK + PAD];
+  __shared__ __align__(16) bf16 sB[BN][BK + PAD];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int g = lane >> 2, t = lane & 3;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    // 64 rows x 32 columns per operand: 256 chunks of 8 elements (16 B)
+    for (int c = tid; c < 256; c += 128) {
+      const int r = c >> 2, col = (c & 3) * 8;
+      const int gk = k0 + col;
+      uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
+      if (m0 + r < M && gk < K) va = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + gk);
+      if (n0 + r < N && gk < K) vb = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + gk);
+      *reinterpret_cast<uint4*>(&sA[r][col]) = va;
+      *reinterpret_cast<uint4*>(&sB[r][col]) = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16) {
+      uint32_t af[2][4], bf[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r = wm + i * 16;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&sA[r + g][kk + 2 * t]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&sA[r + g + 8][kk + 2 * t]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&sA[r + g][kk + 2 * t + 8]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&sA[r + g + 8][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn + j * 8;
+        bf[j][0] = *reinterpret_cast<const uint32_t*>(&sB[c + g][kk + 2 * t]);
+        bf[j][1] = *reinterpret_cast<const uint32_t*>(&sB[c + g][kk + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bf[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = m0 + wm + i * 16 + g + 8 * (q >> 1);
+        const int col = n0 + wn + j * 8 + 2 * t + (q & 1);
+        if (row >= M || col >= N) continue;
+        float v = acc[i][j][q];
+        if (e.bias) v += e.bias[col];
+        if (e.relu) v = fmaxf(v, 0.f);
+        if (e.f32) e.f32[(size_t)row * e.ldf + col] = v;
+        const bf16 h = __float2bfloat16(v);
+        if (e.b16) e.b16[(size_t)row * e.ldb + col] = h;
+        if (e.b16t) e.b16t[(size_t)col * e.ldt + row] = h;
+      }
+}
+
+// Rows idx[r] (or r) of a row-major FP32 matrix into BF16 rows of length ld
+// (columns past `cols` zero) and, when dst_t is set, the transpose [ld][ldt].
+__global__ void k_pack(int rows, int cols, const float* __restrict__ src, const int* __restrict__ idx, bf16* dst,
+                       int ld, bf16* dst_t, int ldt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (c >= ld || r >= rows) return;
+  const int sr = idx ? idx[r] : r;
+  const float v = c < cols ? src[(size_t)sr * cols + c] : 0.f;
+  const bf16 h = __float2bfloat16(v);
+  dst[(size_t)r * ld + c] = h;
+  if (dst_t) dst_t[(size_t)c * ldt + r] = h;
+}
+
+__global__ void k_gather(int rows, int cols, const float* __restrict__ src, const int* __restrict__ idx, float* dst) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (c >= cols || r >= rows) return;
+  dst[(size_t)r * cols + c] = src[(size_t)(idx ? idx[r] : r) * cols + c];
+}
+
+// dY = scale (y - t) and per-block sums of (y - t)^2, in a fixed order.
+__global__ void __launch_bounds__(256) k_mse(int n, const float* __restrict__ y, const float* __restrict__ tg,
+                                             float* dy, float scale, float* part) {
+  __shared__ float s[256];
+  float acc = 0.f;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float d = y[k] - tg[k];
+    dy[k] = scale * d;
+    acc += d * d;
+  }
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+
+// An FP32 gradient [B][N] into BF16 rows [B][ldb] (zero past N) and the
+// transpose [N][ldt]; with H set, the ReLU derivative (H > 0) is applied and
+// the FP32 gradient is overwritten with the masked one.
+__global__ void k_grad_pack(int B, int N, float* dyf, const bf16* __restrict__ H, int ldH, bf16* dyb, int ldb,
+                            bf16* dyt, int ldt) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+  if (c >= ldb || r >= B) return;
+  float v = 0.f;
+  if (c < N) {
+    v = dyf[(size_t)r * N + c];
+    if (H && !(__bfloat162float(H[(size_t)r * ldH + c]) > 0.f)) v = 0.f;
+    dyf[(size_t)r * N + c] = v;
+  }
+  const bf16 h = __float2bfloat16(v);
+  dyb[(size_t)r * ldb + c] = h;
+  if (c < N) dyt[(size_t)c * ldt + r] = h;
+}
+
+// db[n] = sum over rows of dY[:, n], in row order (deterministic).
+__global__ void k_colsum(int B, int N, const float* __restrict__ dy, float* db) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  float s = 0.f;
+  for (int r = 0; r < B; ++r) s += dy[(size_t)r * N + c];
+  db[c] = s;
+}
+
+// Adam on an FP32 [rows][cols] parameter; W (BF16 [rows][ldW]) and Wt (BF16
+// [cols..][ldWt], transposed) are refreshed when given.
+__global__ void k_adam(int rows, int cols, float* w, const float* __restrict__ gr, float* m, float* v, float lr,
+                       float b1, float b2, float eps, float c1, float c2, bf16* W, int ldW, bf16* Wt, int ldWt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= rows * cols) return;
+  const float gk = gr[k];
+  const float mk = b1 * m[k] + (1.f - b1) * gk;
+  const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+  m[k] = mk;
+  v[k] = vk;
+  const float wk = w[k] - lr * (mk * c1) / (sqrtf(vk * c2) + eps);
+  w[k] = wk;
+  const int r = k / cols, c = k % cols;
+  const bf16 h = __float2bfloat16(wk);
+  if (W) W[(size_t)r * ldW + c] = h;
+  if (Wt) Wt[(size_t)c * ldWt + r] = h;
+}
+
+}  // namespace cliffs_nn
+
+using namespace cliffs_nn;
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+  if (cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
+    *p = nullptr;
+    return 1;
+  }
+  return cudaMemset(*p, 0, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess;
+}
+
+struct Layer {
+  int rows = 0, cols = 0;  // W: rows x cols
+  int kp = 0, rp = 0;      // cols and rows padded to 16
+  float *w = nullptr, *b = nullptr, *gw = nullptr, *gb = nullptr;
+  float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;
+  bf16* W = nullptr;   // [rows][kp]
+  bf16* Wt = nullptr;  // [kp][rp]
+};
+
+}  // namespace
+
+struct cliffs_mlp {
+  cliffs_mlp_desc d{};
+  std::vector<Layer> L;
+  cudaStream_t stream = nullptr;
+  int cap = 0;                   // batch capacity of the activation buffers
+  std::vector<bf16*> H, Ht;      // H[l]: input of layer l, [cap][kp_l]; Ht[l]: [kp_l][cap]
+  float* out = nullptr;          // [cap][n_out]
+  float* dyf = nullptr;          // [cap][maxN]
+  float* dh = nullptr;           // [cap][maxN]
+  bf16* dyb = nullptr;           // [cap][maxNp]
+  bf16* dyt = nullptr;           // [maxNp][cap]
+  float* part = nullptr;         // loss partial sums
+  float* xs = nullptr;           // staged inputs / targets
+  float* ts = nullptr;
+  int staged = 0;
+  int* idx = nullptr;
+  int adam_t = 0;
+  int64_t launches = 0;
+};
+
+namespace {
+
+constexpr int kLossBlocks = 64;
+
+void free_all(cliffs_mlp* m) {
+  for (Layer& l : m->L) {
+    void* p[] = {l.w, l.b, l.gw, l.gb, l.mw, l.vw, l.mb, l.vb, l.W, l.Wt};
+    for (void* q : p)
+      if (q) cudaFree(q);
+  }
+  for (bf16* p : m->H)
+    if (p) cudaFree(p);
+  for (bf16* p : m->Ht)
+    if (p) cudaFree(p);
+  void* p[] = {m->out, m->dyf, m->dh, m->dyb, m->dyt, m->part, m->xs, m->ts, m->idx};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  m->H.clear();
+  m->Ht.clear();
+  m->out = m->dyf = m->dh = m->part = m->xs = m->ts = nullptr;
+  m->dyb = m->dyt = nullptr;
+  m->idx = nullptr;
+}
+
+int max_n(const cliffs_mlp* m) { return std::max(m->d.width, m->d.n_out); }
+
+// Activation buffers for batches up to cap.
+int ensure_cap(cliffs_mlp* m, int cap) {
+  if (cap <= m->cap) return CLIFFS_OK;
+  for (bf16* p : m->H)
+    if (p) cudaFree(p);
+  for (bf16* p : m->Ht)
+    if (p) cudaFree(p);
+  void* p[] = {m->out, m->dyf, m->dh, m->dyb, m->dyt, m->part};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  m->H.assign(m->L.size(), nullptr);
+  m->Ht.assign(m->L.size(), nullptr);
+  const int mn = max_n(m), mnp = pad16(mn);
+  for (size_t l = 0; l < m->L.size(); ++l) {
+    if (dalloc(&m->H[l], (size_t)cap * m->L[l].kp) || dalloc(&m->Ht[l], (size_t)m->L[l].kp * cap))
+      return CLIFFS_ERR_NOMEM;
+  }
+  if (dalloc(&m->out, (size_t)cap * m->d.n_out) || dalloc(&m->dyf, (size_t)cap * mn) ||
+      dalloc(&m->dh, (size_t)cap * mn) || dalloc(&m->dyb, (size_t)cap * mnp) || dalloc(&m->dyt, (size_t)mnp * cap) ||
+      dalloc(&m->part, kLossBlocks))
+    return CLIFFS_ERR_NOMEM;
+  m->cap = cap;
+  return CLIFFS_OK;
+}
+
+void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e) {
+  const dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  gemm_tn<<<grid, 128, 0, m->stream>>>(M, N, K, A, lda, B, ldb, e);
+  ++m->launches;
+}
+
+// Forward pass of rows [0, B) staged in H[0] (and Ht[0]); out gets the result.
+void forward(cliffs_mlp* m, int B) {
+  const int nl = (int)m->L.size();
+  for (int l = 0; l < nl; ++l) {
+    const Layer& y = m->L[l];
+    Epi e{};
+    e.bias = y.b;
+    if (l < nl - 1) {
+      e.relu = 1;
+      e.b16 = m->H[l + 1];
+      e.ldb = m->L[l + 1].kp;
+      e.b16t = m->Ht[l + 1];
+      e.ldt = m->cap;
+    } else {
+      e.f32 = m->out;
+      e.ldf = m->d.n_out;
+    }
+    gemm(m, B, y.rows, y.kp, m->H[l], y.kp, y.W, y.kp, e);
+  }
+}
+
+void stage_inputs(cliffs_mlp* m, int B, const float* x_dev, const int* idx) {
+  const int kp0 = m->L[0].kp;
+  k_pack<<<dim3((kp0 + 127) / 128, B), 128, 0, m->stream>>>(B, m->d.n_in, x_dev, idx, m->H[0], kp0, m->Ht[0], m->cap);
+  ++m->launches;
+}
+
+// Loss and gradients of the batch staged by stage_inputs with targets t_dev
+// (rows idx); returns the sum of squared errors through *part on the device.
+void backward(cliffs_mlp* m, int B, const float* t_dev, const int* idx) {
+  const int nl = (int)m->L.size();
+  const int no = m->d.n_out;
+  // targets of the batch into dh (scratch), then dY of the output layer
+  k_gather<<<dim3((no + 127) / 128, B), 128, 0, m->stream>>>(B, no, t_dev, idx, m->dh);
+  k_mse<<<kLossBlocks, 256, 0, m->stream>>>(B * no, m->out, m->dh, m->dyf, 2.f / ((float)B * no), m->part);
+  m->launches += 2;
+  for (int l = nl - 1; l >= 0; --l) {
+    const Layer& y = m->L[l];
+    const int N = y.rows, Np = y.rp;
+    // dY of this layer: BF16 rows and transpose; ReLU derivative for hidden layers
+    const bf16* Hmask = l < nl - 1 ? m->H[l + 1] : nullptr;
+    const int ldH = l < nl - 1 ? m->L[l + 1].kp : 0;
+    k_grad_pack<<<dim3((Np + 127) / 128, B), 128, 0, m->stream>>>(B, N, m->dyf, Hmask, ldH, m->dyb, Np, m->dyt,
+                                                                  m->cap);
+    k_colsum<<<(N + 127) / 128, 128, 0, m->stream>>>(B, N, m->dyf, y.gb);
+    m->launches += 2;
+    // dW = dY^T H_l: (N x B) (B x cols), reduction over the batch
+    Epi ew{};
+    ew.f32 = y.gw;
+    ew.ldf = y.cols;
+    gemm(m, N, y.cols, B, m->dyt, m->cap, m->Ht[l], m->cap, ew);
+    // dH_l = dY W: (B x Np) (Np x kp), the input gradient of the layer below
+    if (l > 0) {
+      Epi eh{};
+      eh.f32 = m->dyf;  // read above; the next layer's dY is built in place
+      eh.ldf = y.cols;
+      gemm(m, B, y.cols, Np, m->dyb, Np, y.Wt, Np, eh);
+    }
+  }
+}
+
+void adam(cliffs_mlp* m, float lr) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  ++m->adam_t;
+  const float c1 = 1.f / (1.f - std::pow(b1, (float)m->adam_t));
+  const float c2 = 1.f / (1.f - std::pow(b2, (float)m->adam_t));
+  for (Layer& y : m->L) {
+    const int nw = y.rows * y.cols;
+    k_adam<<<(nw + 255) / 256, 256, 0, m->stream>>>(y.rows, y.cols, y.w, y.gw, y.mw, y.vw, lr, b1, b2, eps, c1, c2,
+                                                    y.W, y.kp, y.Wt, y.rp);
+    k_adam<<<(y.rows + 255) / 256, 256, 0, m->stream>>>(y.rows, 1, y.b, y.gb, y.mb, y.vb, lr, b1, b2, eps, c1, c2,
+                                                        nullptr, 0, nullptr, 0);
+    m->launches += 2;
+  }
+}
+
+// The BF16 copies of layer weights from the FP32 master.
+int refresh_bf16(cliffs_mlp* m, Layer& y) {
+  std::vector<float> w((size_t)y.rows * y.cols);
+  if (cudaMemcpy(w.data(), y.w, w.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return CLIFFS_ERR_CUDA;
+  std::vector<bf16> W((size_t)y.rows * y.kp, __float2bfloat16(0.f)), Wt((size_t)y.kp * y.rp, __float2bfloat16(0.f));
+  for (int r = 0; r < y.rows; ++r)
+    for (int c = 0; c < y.cols; ++c) {
+      const bf16 h = __float2bfloat16(w[(size_t)r * y.cols + c]);
+      W[(size_t)r * y.kp + c] = h;
+      Wt[(size_t)c * y.rp + r] = h;
+    }
+  if (cudaMemcpy(y.W, W.data(), W.size() * sizeof(bf16), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(y.Wt, Wt.data(), Wt.size() * sizeof(bf16), cudaMemcpyHostToDevice) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  (void)m;
+  return CLIFFS_OK;
+}
+
+int stage_data(cliffs_mlp* m, int n, const float* x, const float* t) {
+  if (n > m->staged) {
+    if (m->xs) cudaFree(m->xs);
+    if (m->ts) cudaFree(m->ts);
+    if (m->idx) cudaFree(m->idx);
+    m->xs = m->ts = nullptr;
+    m->idx = nullptr;
+    m->staged = 0;
+    if (dalloc(&m->xs, (size_t)n * m->d.n_in) || dalloc(&m->ts, (size_t)n * m->d.n_out) || dalloc(&m->idx, n))
+      return CLIFFS_ERR_NOMEM;
+    m->staged = n;
+  }
+  if (cudaMemcpyAsync(m->xs, x, (size_t)n * m->d.n_in * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  if (t && cudaMemcpyAsync(m->ts, t, (size_t)n * m->d.n_out * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  return CLIFFS_OK;
+}
+
+float loss_of(cliffs_mlp* m, int B) {
+  float part[kLossBlocks];
+  cudaMemcpyAsync(part, m->part, sizeof(part), cudaMemcpyDeviceToHost, m->stream);
+  cudaStreamSynchronize(m->stream);
+  double s = 0;
+  for (float p : part) s += p;
+  return (float)(s / ((double)B * m->d.n_out));
+}
+
+}  // namespace
+
+int cliffs_mlp_create(const cliffs_mlp_desc* d, cliffs_mlp** out) {
+  if (!d || !out || d->n_in < 1 || d->n_in > 16 || d->width < 16 || d->width % 16 || d->width > 4096 ||
+      d->depth < 1 || d->depth > 16 || d->n_out < 1 || d->n_out > 16384)
+    return CLIFFS_ERR_ARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CLIFFS_ERR_DEVICE;
+  auto* m = new cliffs_mlp;
+  m->d = *d;
+  auto fail = [&](int r) {
+    free_all(m);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return r;
+  };
+  if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
+  std::mt19937_64 rng(d->seed);
+  for (int l = 0; l <= d->depth; ++l) {
+    Layer y;
+    y.cols = l == 0 ? d->n_in : d->width;
+    y.rows = l == d->depth ? d->n_out : d->width;
+    y.kp = pad16(y.cols);
+    y.rp = pad16(y.rows);
+    const size_t nw = (size_t)y.rows * y.cols;
+    if (dalloc(&y.w, nw) || dalloc(&y.b, y.rows) || dalloc(&y.gw, nw) || dalloc(&y.gb, y.rows) ||
+        dalloc(&y.mw, nw) || dalloc(&y.vw, nw) || dalloc(&y.mb, y.rows) || dalloc(&y.vb, y.rows) ||
+        dalloc(&y.W, (size_t)y.rows * y.kp) || dalloc(&y.Wt, (size_t)y.kp * y.rp)) {
+      m->L.push_back(y);
+      return fail(CLIFFS_ERR_NOMEM);
+    }
+    // He uniform for ReLU layers, Glorot-like for the linear output layer
+    const double a = l < d->depth ? std::sqrt(6.0 / y.cols) : std::sqrt(3.0 / y.cols);
+    std::uniform_real_distribution<double> U(-a, a);
+    std::vector<float> w(nw);
+    for (float& v : w) v = (float)U(rng);
+    if (cudaMemcpy(y.w, w.data(), nw * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+      m->L.push_back(y);
+      return fail(CLIFFS_ERR_CUDA);
+    }
+    m->L.push_back(y);
+    if (refresh_bf16(m, m->L.back())) return fail(CLIFFS_ERR_CUDA);
+  }
+  *out = m;
+  return CLIFFS_OK;
+}
+
+void cliffs_mlp_destroy(cliffs_mlp* m) {
+  if (!m) return;
+  cudaStreamSynchronize(m->stream);
+  free_all(m);
+  cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+int cliffs_mlp_layers(const cliffs_mlp* m, int32_t* n) {
+  if (!m || !n) return CLIFFS_ERR_ARG;
+  *n = (int32_t)m->L.size();
+  return CLIFFS_OK;
+}
+
+int cliffs_mlp_shape(const cliffs_mlp* m, int32_t l, int32_t* rows, int32_t* cols) {
+  if (!m || l < 0 || l >= (int)m->L.size() || !rows || !cols) return CLIFFS_ERR_ARG;
+  *rows = m->L[l].rows;
+  *cols = m->L[l].cols;
+  return CLIFFS_OK;
+}
+
+static float* param_ptr(const cliffs_mlp* m, int l, int which, int64_t* n) {
+  const Layer& y = m->L[l];
+  *n = which == 0 || which == 2 ? (int64_t)y.rows * y.cols : y.rows;
+  switch (which) {
+    case 0: return y.w;
+    case 1: return y.b;
+    case 2: return y.gw;
+    case 3: return y.gb;
+  }
+  return nullptr;
+}
+
+int cliffs_mlp_get(const cliffs_mlp* m, int32_t l, int32_t which, float* host, int64_t n) {
+  if (!m || l < 0 || l >= (int)m->L.size() || which < 0 || which > 3 || !host) return CLIFFS_ERR_ARG;
+  int64_t cnt = 0;
+  float* p = param_ptr(m, l, which, &cnt);
+  if (n != cnt) return CLIFFS_ERR_ARG;
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess || cudaMemcpy(host, p, cnt * 4, cudaMemcpyDeviceToHost))
+    return CLIFFS_ERR_CUDA;
+  return CLIFFS_OK;
+}
+
+int cliffs_mlp_set(cliffs_mlp* m, int32_t l, int32_t which, const float* host, int64_t n) {
+  if (!m || l < 0 || l >= (int)m->L.size() || which < 0 || which > 1 || !host) return CLIFFS_ERR_ARG;
+  int64_t cnt = 0;
+  float* p = param_ptr(m, l, which, &cnt);
+  if (n != cnt) return CLIFFS_ERR_ARG;
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess || cudaMemcpy(p, host, cnt * 4, cudaMemcpyHostToDevice))
+    return CLIFFS_ERR_CUDA;
+  return which == 0 ? refresh_bf16(m, m->L[l]) : CLIFFS_OK;
+}
+
+int cliffs_mlp_predict(cliffs_mlp* m, int32_t batch, const float* x, float* y) {
+  if (!m || batch < 1 || !x || !y) return CLIFFS_ERR_ARG;
+  const int chunk = 4096;
+  int r = ensure_cap(m, pad16(std::min<int>(batch, chunk)));
+  if (!r) r = stage_data(m, batch, x, nullptr);
+  for (int s = 0; !r && s < batch; s += chunk) {
+    const int B = std::min(chunk, batch - s);
+    stage_inputs(m, B, m->xs + (size_t)s * m->d.n_in, nullptr);
+    forward(m, B);
+    if (cudaMemcpyAsync(y + (size_t)s * m->d.n_out, m->out, (size_t)B * m->d.n_out * 4, cudaMemcpyDeviceToHost,
+                        m->stream) != cudaSuccess)
+      r = CLIFFS_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(m->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  if (!r && cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  return r;
+}
+
+int cliffs_mlp_gradients(cliffs_mlp* m, int32_t batch, const float* x, const float* t, float* loss) {
+  if (!m || batch < 16 || batch % 16 || !x || !t) return CLIFFS_ERR_ARG;
+  int r = ensure_cap(m, batch);
+  if (!r) r = stage_data(m, batch, x, t);
+  if (r) return r;
+  stage_inputs(m, batch, m->xs, nullptr);
+  forward(m, batch);
+  backward(m, batch, m->ts, nullptr);
+  const float l = loss_of(m, batch);
+  if (loss) *loss = l;
+  return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+}
+
+int cliffs_mlp_train(cliffs_mlp* m, int32_t n, const float* x, const float* t, int32_t epochs, int32_t batch,
+                     float lr, uint64_t seed, float* losses) {
+  if (!m || n < batch || batch < 16 || batch % 16 || epochs < 1 || !x || !t || !(lr > 0)) return CLIFFS_ERR_ARG;
+  int r = ensure_cap(m, batch);
+  if (!r) r = stage_data(m, n, x, t);
+  if (r) return r;
+  std::mt19937_64 rng(seed);
+  std::vector<int> perm(n);
+  for (int k = 0; k < n; ++k) perm[k] = k;
+  const int per_epoch = n / batch;
+  const int total = per_epoch * epochs;
+  int it = 0;
+  for (int e = 0; e < epochs && !r; ++e) {
+    std::shuffle(perm.begin(), perm.end(), rng);
+    if (cudaMemcpyAsync(m->idx, perm.data(), (size_t)n * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess) {
+      r = CLIFFS_ERR_CUDA;
+      break;
+    }
+    double sum = 0;
+    for (int b = 0; b < per_epoch; ++b, ++it) {
+      const int* idx = m->idx + (size_t)b * batch;
+      stage_inputs(m, batch, m->xs, idx);
+      forward(m, batch);
+      backward(m, batch, m->ts, idx);
+      const double frac = (double)it / std::max(1, total - 1);
+      const float lr_it = (float)(lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * frac))));
+      adam(m, lr_it);
+      if (losses) sum += loss_of(m, batch);
+    }
+    if (losses) losses[e] = (float)(sum / per_epoch);
+    // the permutation buffer is rewritten next epoch: the stream must be done with it
+    if (cudaStreamSynchronize(m->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r && cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  return r;
+}
+
+int cliffs_mlp_launch_count(const cliffs_mlp* m, int64_t* n) {
+  if (!m || !n) return CLIFFS_ERR_ARG;
+  *n = m->launches;
+  return CLIFFS_OK;
+}

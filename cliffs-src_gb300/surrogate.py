@@ -1,0 +1,339 @@
+"""A learned surrogate of the solver for source studies (include/cliffs_surrogate.h).
+
+The surrogate maps eight source parameters to the quantities a hazard study
+reads from a run: the maximum elevation at 64 gauges and the maximum
+elevation over a 128 x 128 window of the coast (learnt at 32 x 32, 4 x 4
+means, and returned upsampled).  Its training data are runs of the batched
+solver (cliffs_batch_*) on one 512 x 512 shelf/slope grid at 100 m, every
+source applied on the device (cliffs_gpu_add_source, rising over its rise
+time); the network is trained on the GPU by the library's own kernels (BF16
+tensor-core products, FP32 accumulation, Adam).  An ensemble of members
+trained from different seeds answers together; where their gauge predictions
+disagree by more than a set relative spread, the scenario goes back to the
+solver, which also judges the surrogate's error on held-out scenarios.
+
+    python cliffs-src_gb300/surrogate.py [--train 4096] [--test 256] [--steps 2000]
+
+prints one JSON line: data generation time, training losses, accuracy of the
+gated ensemble against the solver, and scenarios per second of the surrogate
+path against one-at-a-time solves.
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+pkg = importlib.import_module("cliffs-src_gb300")
+cg = pkg.cliffs_gpu
+W = pkg.workloads
+
+SIDE = 512
+DX = 100.0
+NGAUGES = 64
+WIN = (slice(192, 320), slice(SIDE - 128, SIDE))  # rows, columns of the coastal window
+POOL = 4
+# parameter ranges, as fractions of the domain length where spatial
+LO = np.array([0.15, 0.20, 0.5, 0.05, 0.05, 0.0, 0.0, 0.0])
+HI = np.array([0.50, 0.80, 3.0, 0.20, 0.20, np.pi, 0.6, 60.0])
+NAMES = ["x0", "y0", "amp", "ax", "ay", "angle", "dipole", "rise_time"]
+
+
+class MlpDesc(ctypes.Structure):
+    _fields_ = [("n_in", ctypes.c_int32), ("width", ctypes.c_int32), ("depth", ctypes.c_int32),
+                ("n_out", ctypes.c_int32), ("seed", ctypes.c_uint64)]
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class MLP:
+    """One network (cliffs_mlp_*)."""
+
+    def __init__(self, n_in, width, depth, n_out, seed=0):
+        self.L = cg.load()
+        d = MlpDesc(n_in, width, depth, n_out, seed)
+        h = ctypes.c_void_p()
+        cg._chk(self.L.cliffs_mlp_create(ctypes.byref(d), ctypes.byref(h)), "mlp_create")
+        self.h = h
+        self.n_in, self.n_out = n_in, n_out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cliffs_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layers(self):
+        n = ctypes.c_int32()
+        cg._chk(self.L.cliffs_mlp_layers(self.h, ctypes.byref(n)), "mlp_layers")
+        return n.value
+
+    def shape(self, layer):
+        r, c = ctypes.c_int32(), ctypes.c_int32()
+        cg._chk(self.L.cliffs_mlp_shape(self.h, layer, ctypes.byref(r), ctypes.byref(c)), "mlp_shape")
+        return r.value, c.value
+
+    def get(self, layer, which):
+        r, c = self.shape(layer)
+        a = np.zeros((r, c) if which in (0, 2) else (r,), np.float32)
+        cg._chk(self.L.cliffs_mlp_get(self.h, layer, which, a.ctypes.data_as(_fp), a.size), "mlp_get")
+        return a
+
+    def set(self, layer, which, a):
+        a = _f32(a)
+        cg._chk(self.L.cliffs_mlp_set(self.h, layer, which, a.ctypes.data_as(_fp), a.size), "mlp_set")
+
+    def weights(self):
+        n = self.layers()
+        return [self.get(l, 0) for l in range(n)], [self.get(l, 1) for l in range(n)]
+
+    def predict(self, x):
+        x = _f32(x)
+        y = np.zeros((x.shape[0], self.n_out), np.float32)
+        cg._chk(self.L.cliffs_mlp_predict(self.h, x.shape[0], x.ctypes.data_as(_fp), y.ctypes.data_as(_fp)),
+                "mlp_predict")
+        return y
+
+    def gradients(self, x, t):
+        x, t = _f32(x), _f32(t)
+        loss = ctypes.c_float()
+        cg._chk(self.L.cliffs_mlp_gradients(self.h, x.shape[0], x.ctypes.data_as(_fp), t.ctypes.data_as(_fp),
+                                            ctypes.byref(loss)), "mlp_gradients")
+        n = self.layers()
+        return loss.value, [self.get(l, 2) for l in range(n)], [self.get(l, 3) for l in range(n)]
+
+    def train(self, x, t, epochs, batch=512, lr=1e-3, seed=0):
+        x, t = _f32(x), _f32(t)
+        losses = np.zeros(epochs, np.float32)
+        cg._chk(self.L.cliffs_mlp_train(self.h, x.shape[0], x.ctypes.data_as(_fp), t.ctypes.data_as(_fp),
+                                        epochs, batch, lr, seed, losses.ctypes.data_as(_fp)), "mlp_train")
+        return losses
+
+    def launches(self):
+        n = ctypes.c_int64()
+        cg._chk(self.L.cliffs_mlp_launch_count(self.h, ctypes.byref(n)), "mlp_launch_count")
+        return n.value
+
+
+# ---- data from the batched solver ------------------------------------------------
+
+def base_grid(seed=0):
+    return W.shelf_2d(seed=seed, nx=SIDE, ny=SIDE, dx=DX, steps=0, amp=0.0, ngauges=NGAUGES)
+
+
+def sample_params(n, seed):
+    rng = np.random.default_rng(seed)
+    return LO + (HI - LO) * rng.random((n, 8))
+
+
+def source_of(p, L):
+    return dict(x0=p[0] * L, y0=p[1] * L, amp=p[2], ax=p[3] * L, ay=p[4] * L, angle=p[5], dipole=p[6],
+                rise_time=p[7])
+
+
+def targets_of(maxe, I, J):
+    """Gauge maxima (64) and the pooled coastal window (32 x 32) from MaxE;
+    never-wet cells count as 0."""
+    m = np.where(maxe > -1e30, maxe, 0.0).astype(np.float64)
+    g = np.maximum(m[J - 1, I - 1], 0.0)
+    w = np.maximum(m[WIN], 0.0)
+    pooled = w.reshape(128 // POOL, POOL, 128 // POOL, POOL).mean(axis=(1, 3))
+    return g, pooled.ravel(), w
+
+
+def solve(params, base, steps, chunk=512):
+    """Runs of the batched solver; returns gauge maxima, pooled windows, full
+    windows, the solver time (s) and the number of runs with a non-finite state."""
+    L = base["xcrd"][-1]
+    I, J = base["gauges"]
+    G, P, F = [], [], []
+    t_solve, bad = 0.0, 0
+    for s in range(0, len(params), chunk):
+        grids = []
+        for p in params[s:s + chunk]:
+            g = pkg.GpuGrid.from_case(dict(base, H0=base["dep"]))
+            g.add_source(base["xcrd"], base["ycrd"], **source_of(p, L))
+            grids.append(g)
+        b = pkg.Batch(grids)
+        b.set_plan(cg.GRAPH, graph_steps=32)
+        t0 = time.perf_counter()
+        b.step(steps)
+        t_solve += time.perf_counter() - t0
+        for g in grids:
+            r, flags = g.status()
+            bad += int(r != 0)
+            me, _ = g.maxwave()
+            gg, pp, ww = targets_of(me, I, J)
+            G.append(gg)
+            P.append(pp)
+            F.append(ww)
+            g.close()
+        b.close()
+    return np.array(G), np.array(P), np.array(F), t_solve, bad
+
+
+# ---- the surrogate ---------------------------------------------------------------
+
+class Norm:
+    """Inputs to [-1, 1]; gauge maxima as standardised log(max + 0.01),
+    weighted x4 so that the 64 gauges weigh as much as the 1024 map cells;
+    map cells standardised."""
+
+    GW = 4.0
+
+    def __init__(self, G, P):
+        lg = np.log(G + 0.01)
+        self.gm, self.gs = lg.mean(0), lg.std(0) + 1e-6
+        self.pm, self.ps = P.mean(0), P.std(0) + 1e-3
+
+    def x(self, params):
+        return 2.0 * (params - LO) / (HI - LO) - 1.0
+
+    def t(self, G, P):
+        return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, (P - self.pm) / self.ps])
+
+    def back(self, Y):
+        g = np.exp(Y[:, :NGAUGES] / self.GW * self.gs + self.gm) - 0.01
+        p = Y[:, NGAUGES:] * self.ps + self.pm
+        return np.maximum(g, 0.0), np.maximum(p, 0.0)
+
+
+def upsample(pooled):
+    """32 x 32 -> 128 x 128, bilinear on cell centres (edges held)."""
+    n = pooled.shape[0]
+    a = pooled.reshape(n, 128 // POOL, 128 // POOL)
+    c = (np.arange(128) + 0.5) / POOL - 0.5
+    i0 = np.clip(np.floor(c).astype(int), 0, 128 // POOL - 1)
+    i1 = np.clip(i0 + 1, 0, 128 // POOL - 1)
+    f = np.clip(c - i0, 0.0, 1.0)
+    r = a[:, i0, :] * (1 - f)[None, :, None] + a[:, i1, :] * f[None, :, None]
+    return r[:, :, i0] * (1 - f)[None, None, :] + r[:, :, i1] * f[None, None, :]
+
+
+class Ensemble:
+    def __init__(self, members=4, width=512, depth=3, seed=0):
+        self.nets = [MLP(8, width, depth, NGAUGES + (128 // POOL) ** 2, seed=seed + 101 * k) for k in range(members)]
+
+    def train(self, X, T, epochs, batch=512, lr=1e-3, seed=0):
+        batch = max(16, min(batch, len(X) // 16 * 16))
+        return [net.train(X, T, epochs, batch, lr, seed + 7 * k) for k, net in enumerate(self.nets)]
+
+    def predict(self, X, norm):
+        outs = [norm.back(net.predict(X)) for net in self.nets]
+        G = np.stack([o[0] for o in outs])  # (members, n, 64)
+        P = np.stack([o[1] for o in outs])
+        return G.mean(0), P.mean(0), G
+
+    def close(self):
+        for n in self.nets:
+            n.close()
+
+
+def spread(Gm, floor=0.05):
+    """Relative disagreement of the members per scenario: the largest over
+    gauges of std / mean (gauges whose mean maximum is below `floor` m are
+    left out)."""
+    mean = Gm.mean(0)
+    rel = Gm.std(0) / np.maximum(mean, 1e-9)
+    rel = np.where(mean >= floor, rel, 0.0)
+    return rel.max(axis=1)
+
+
+def run(n_train=4096, n_test=256, steps=2000, epochs=400, gate=0.05, seed=0):
+    base = base_grid(seed)
+    Xtr = sample_params(n_train, seed + 1)
+    Xte = sample_params(n_test, seed + 2)
+    t0 = time.perf_counter()
+    Gtr, Ptr, _, t_data, bad_tr = solve(Xtr, base, steps)
+    t_gen = time.perf_counter() - t0
+    Gte, Pte, Fte, t_test_solve, bad_te = solve(Xte, base, steps)
+    norm = Norm(Gtr, Ptr)
+    ens = Ensemble(seed=seed)
+    t0 = time.perf_counter()
+    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Ptr), epochs)
+    t_train = time.perf_counter() - t0
+    # the surrogate path: ensemble prediction, then the gate
+    t0 = time.perf_counter()
+    Gp, Pp, Gm = ens.predict(norm.x(Xte), norm)
+    sp = spread(Gm)
+    t_pred = time.perf_counter() - t0
+    accept = sp <= gate
+    # error against the solver on gauges with a maximum of at least 5 cm
+    mask = Gte >= 0.05
+    rel = np.abs(Gp - Gte) / np.maximum(Gte, 1e-9)
+    rel_acc = rel[accept[:, None] & mask]
+    rel_all = rel[mask]
+    win_err = np.abs(upsample(Pp) - Fte)  # m, on the full 128 x 128 window
+    # one-at-a-time solves of a few test scenarios: the method without the surrogate
+    n_single = min(16, n_test)
+    L = base["xcrd"][-1]
+    t_single = 0.0
+    for p in Xte[:n_single]:
+        g = pkg.GpuGrid.from_case(dict(base, H0=base["dep"]))
+        g.add_source(base["xcrd"], base["ycrd"], **source_of(p, L))
+        g.sync()
+        t1 = time.perf_counter()
+        g.step(steps)
+        g.maxwave()
+        t_single += time.perf_counter() - t1
+        g.close()
+    per_single = t_single / n_single
+    per_batch = t_test_solve / n_test
+    n_fallback = int((~accept).sum())
+    t_gated = t_pred + n_fallback * per_batch  # fallbacks go to the batched solver
+    res = dict(train=n_train, test=n_test, steps=steps, epochs=epochs, gate=gate,
+               nonfinite_runs=int(bad_tr + bad_te),
+               data_seconds=round(t_gen, 2), solver_seconds_train=round(t_data, 2),
+               train_seconds=round(t_train, 2),
+               final_loss=[round(float(l[-1]), 5) for l in losses],
+               first_loss=[round(float(l[0]), 5) for l in losses],
+               accepted=int(accept.sum()), fallback=n_fallback,
+               gauge_rel_err_accepted_mean=round(float(rel_acc.mean()), 4) if rel_acc.size else None,
+               gauge_rel_err_accepted_median=round(float(np.median(rel_acc)), 4) if rel_acc.size else None,
+               gauge_rel_err_all_mean=round(float(rel_all.mean()), 4),
+               gauge_rel_err_all_p90=round(float(np.quantile(rel_all, 0.9)), 4),
+               gated_rel_err_mean=round(float(np.where(accept[:, None], rel, 0.0)[mask].mean()), 4),
+               window_abs_err_mean_m=round(float(win_err.mean()), 4),
+               window_max_mean_m=round(float(Fte.max(axis=(1, 2)).mean()), 4),
+               predict_ms=round(1e3 * t_pred, 3),
+               single_solve_s=round(per_single, 4), batched_solve_s_per_scenario=round(per_batch, 5),
+               surrogate_scenarios_per_s=round(n_test / t_pred, 1),
+               gated_scenarios_per_s=round(n_test / t_gated, 1),
+               one_at_a_time_scenarios_per_s=round(1.0 / per_single, 2),
+               gated_speedup_vs_one_at_a_time=round(per_single * n_test / t_gated, 1))
+    ens.close()
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=4096)
+    ap.add_argument("--test", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=400)
+    ap.add_argument("--gate", type=float, default=0.05)
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args()
+    pkg.build.build()
+    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.gate, a.seed)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

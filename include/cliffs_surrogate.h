@@ -1,0 +1,62 @@
+/* cliffs_surrogate.h -- a learned surrogate of the solver for source studies.
+ *
+ * No reference counterpart: the reference is the solver only.  The surrogate
+ * is a multilayer perceptron mapping a source's parameters to quantities of
+ * interest of the run (gauge maxima, a coarse max-inundation map), trained on
+ * runs of the batched solver (cliffs_batch_*) and used with an ensemble of
+ * independently initialised members whose disagreement sends a scenario back
+ * to the solver.  Training and inference run on the GPU in hand-written
+ * kernels: BF16 tensor-core matrix products with FP32 accumulation
+ * (mma.sync m16n8k16), fused bias and ReLU, Adam in FP32 with BF16 copies of
+ * the weights.  Data are plain row-major FP32 host arrays; the library keeps
+ * its own device copies.  Every call returns a CLIFFS_* status
+ * (cliffs_gpu.h). */
+#ifndef CLIFFS_SURROGATE_H
+#define CLIFFS_SURROGATE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cliffs_mlp cliffs_mlp;
+
+typedef struct cliffs_mlp_desc {
+  int32_t n_in;   /* inputs (1..16) */
+  int32_t width;  /* hidden width (multiple of 16, <= 4096) */
+  int32_t depth;  /* hidden layers (1..16) */
+  int32_t n_out;  /* outputs (1..16384) */
+  uint64_t seed;  /* weight initialisation (He uniform) */
+} cliffs_mlp_desc;
+
+int cliffs_mlp_create(const cliffs_mlp_desc *d, cliffs_mlp **out);
+void cliffs_mlp_destroy(cliffs_mlp *m);
+/* Number of layers (depth + 1) and the shape of layer l's weight (rows =
+ * outputs, cols = inputs). */
+int cliffs_mlp_layers(const cliffs_mlp *m, int32_t *n_layers);
+int cliffs_mlp_shape(const cliffs_mlp *m, int32_t layer, int32_t *rows, int32_t *cols);
+
+/* Parameters and gradients of layer l: which = 0 weight (rows x cols), 1 bias
+ * (rows), 2 weight gradient, 3 bias gradient (of the last
+ * cliffs_mlp_gradients or training step). */
+int cliffs_mlp_get(const cliffs_mlp *m, int32_t layer, int32_t which, float *host, int64_t n);
+int cliffs_mlp_set(cliffs_mlp *m, int32_t layer, int32_t which, const float *host, int64_t n);
+
+/* y (batch x n_out) = f(x (batch x n_in)). */
+int cliffs_mlp_predict(cliffs_mlp *m, int32_t batch, const float *x, float *y);
+/* Loss (mean squared error over batch and outputs) and gradients of every
+ * parameter for one batch, without an update.  batch: multiple of 16. */
+int cliffs_mlp_gradients(cliffs_mlp *m, int32_t batch, const float *x, const float *t, float *loss);
+/* Train with Adam on n samples (x: n x n_in, t: n x n_out): `epochs` passes
+ * over a seeded shuffle in batches of `batch` (multiple of 16; the last
+ * partial batch of an epoch is left out), learning rate lr with a cosine
+ * decay to lr/20.  losses (epochs) gets each epoch's mean batch loss. */
+int cliffs_mlp_train(cliffs_mlp *m, int32_t n, const float *x, const float *t, int32_t epochs, int32_t batch,
+                     float lr, uint64_t seed, float *losses);
+/* Kernels launched so far. */
+int cliffs_mlp_launch_count(const cliffs_mlp *m, int64_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
