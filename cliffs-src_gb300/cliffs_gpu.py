@@ -128,7 +128,8 @@ SIGNATURES = {
     "cliffs_mlp_gradients": ([_V, _I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                               ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "cliffs_mlp_train": ([_V, _I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), _I, _I,
-                          ctypes.c_float, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+                          ctypes.c_float, ctypes.c_float, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)],
+                         ctypes.c_int),
     "cliffs_mlp_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_sweep_noalloc": ([_I, _I, _I, _I] + [_V] * 7 + [_D] * 5 + [_V], ctypes.c_int),
 }

@@ -190,10 +190,12 @@ __global__ void k_colsum(int B, int N, const float* __restrict__ dy, float* db) 
   db[c] = s;
 }
 
-// Adam on an FP32 [rows][cols] parameter; W (BF16 [rows][ldW]) and Wt (BF16
-// [cols..][ldWt], transposed) are refreshed when given.
+// Adam with decoupled weight decay wd on an FP32 [rows][cols] parameter; W
+// (BF16 [rows][ldW]) and Wt (BF16 [cols..][ldWt], transposed) are refreshed
+// when given.
 __global__ void k_adam(int rows, int cols, float* w, const float* __restrict__ gr, float* m, float* v, float lr,
-                       float b1, float b2, float eps, float c1, float c2, bf16* W, int ldW, bf16* Wt, int ldWt) {
+                       float wd, float b1, float b2, float eps, float c1, float c2, bf16* W, int ldW, bf16* Wt,
+                       int ldWt) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= rows * cols) return;
   const float gk = gr[k];
@@ -201,7 +203,7 @@ __global__ void k_adam(int rows, int cols, float* w, const float* __restrict__ g
   const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
   m[k] = mk;
   v[k] = vk;
-  const float wk = w[k] - lr * (mk * c1) / (sqrtf(vk * c2) + eps);
+  const float wk = w[k] * (1.f - lr * wd) - lr * (mk * c1) / (sqrtf(vk * c2) + eps);
   w[k] = wk;
   const int r = k / cols, c = k % cols;
   const bf16 h = __float2bfloat16(wk);
@@ -373,17 +375,17 @@ void backward(cliffs_mlp* m, int B, const float* t_dev, const int* idx) {
   }
 }
 
-void adam(cliffs_mlp* m, float lr) {
+void adam(cliffs_mlp* m, float lr, float wd) {
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   ++m->adam_t;
   const float c1 = 1.f / (1.f - std::pow(b1, (float)m->adam_t));
   const float c2 = 1.f / (1.f - std::pow(b2, (float)m->adam_t));
   for (Layer& y : m->L) {
     const int nw = y.rows * y.cols;
-    k_adam<<<(nw + 255) / 256, 256, 0, m->stream>>>(y.rows, y.cols, y.w, y.gw, y.mw, y.vw, lr, b1, b2, eps, c1, c2,
-                                                    y.W, y.kp, y.Wt, y.rp);
-    k_adam<<<(y.rows + 255) / 256, 256, 0, m->stream>>>(y.rows, 1, y.b, y.gb, y.mb, y.vb, lr, b1, b2, eps, c1, c2,
-                                                        nullptr, 0, nullptr, 0);
+    k_adam<<<(nw + 255) / 256, 256, 0, m->stream>>>(y.rows, y.cols, y.w, y.gw, y.mw, y.vw, lr, wd, b1, b2, eps, c1,
+                                                    c2, y.W, y.kp, y.Wt, y.rp);
+    k_adam<<<(y.rows + 255) / 256, 256, 0, m->stream>>>(y.rows, 1, y.b, y.gb, y.mb, y.vb, lr, 0.f, b1, b2, eps, c1,
+                                                        c2, nullptr, 0, nullptr, 0);
     m->launches += 2;
   }
 }
@@ -566,8 +568,9 @@ int cliffs_mlp_gradients(cliffs_mlp* m, int32_t batch, const float* x, const flo
 }
 
 int cliffs_mlp_train(cliffs_mlp* m, int32_t n, const float* x, const float* t, int32_t epochs, int32_t batch,
-                     float lr, uint64_t seed, float* losses) {
-  if (!m || n < batch || batch < 16 || batch % 16 || epochs < 1 || !x || !t || !(lr > 0)) return CLIFFS_ERR_ARG;
+                     float lr, float weight_decay, uint64_t seed, float* losses) {
+  if (!m || n < batch || batch < 16 || batch % 16 || epochs < 1 || !x || !t || !(lr > 0) || !(weight_decay >= 0))
+    return CLIFFS_ERR_ARG;
   int r = ensure_cap(m, batch);
   if (!r) r = stage_data(m, n, x, t);
   if (r) return r;
@@ -591,7 +594,7 @@ int cliffs_mlp_train(cliffs_mlp* m, int32_t n, const float* x, const float* t, i
       backward(m, batch, m->ts, idx);
       const double frac = (double)it / std::max(1, total - 1);
       const float lr_it = (float)(lr * (0.05 + 0.95 * 0.5 * (1.0 + std::cos(M_PI * frac))));
-      adam(m, lr_it);
+      adam(m, lr_it, weight_decay);
       if (losses) sum += loss_of(m, batch);
     }
     if (losses) losses[e] = (float)(sum / per_epoch);

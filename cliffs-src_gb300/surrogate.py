@@ -9,10 +9,14 @@ source applied on the device (cliffs_gpu_add_source, rising over its rise
 time); the network is trained on the GPU by the library's own kernels (BF16
 tensor-core products, FP32 accumulation, Adam).  An ensemble of members
 trained from different seeds answers together; where their gauge predictions
-disagree by more than a set relative spread, the scenario goes back to the
-solver, which also judges the surrogate's error on held-out scenarios.
+disagree by more than a relative spread, the scenario goes back to the
+solver.  The spread threshold is calibrated on a validation split of the
+training runs as the largest that keeps the accepted scenarios' mean gauge
+error within the target; the solver then judges the surrogate's error on
+held-out scenarios.
 
     python cliffs-src_gb300/surrogate.py [--train 4096] [--test 256] [--steps 2000]
+                                         [--epochs 1500] [--target 0.045]
 
 prints one JSON line: data generation time, training losses, accuracy of the
 gated ensemble against the solver, and scenarios per second of the surrogate
@@ -119,11 +123,12 @@ class MLP:
         n = self.layers()
         return loss.value, [self.get(l, 2) for l in range(n)], [self.get(l, 3) for l in range(n)]
 
-    def train(self, x, t, epochs, batch=512, lr=1e-3, seed=0):
+    def train(self, x, t, epochs, batch=512, lr=1e-3, seed=0, weight_decay=0.0):
         x, t = _f32(x), _f32(t)
         losses = np.zeros(epochs, np.float32)
         cg._chk(self.L.cliffs_mlp_train(self.h, x.shape[0], x.ctypes.data_as(_fp), t.ctypes.data_as(_fp),
-                                        epochs, batch, lr, seed, losses.ctypes.data_as(_fp)), "mlp_train")
+                                        epochs, batch, lr, weight_decay, seed, losses.ctypes.data_as(_fp)),
+                "mlp_train")
         return losses
 
     def launches(self):
@@ -204,7 +209,12 @@ class Norm:
         self.pm, self.ps = P.mean(0), P.std(0) + 1e-3
 
     def x(self, params):
-        return 2.0 * (params - LO) / (HI - LO) - 1.0
+        """Features: the parameters scaled to [-1, 1], with the amplitude as its
+        logarithm and the angle as its cosine and sine (rotations wrap)."""
+        z = 2.0 * (params - LO) / (HI - LO) - 1.0
+        la = np.log(params[:, 2])
+        z[:, 2] = 2.0 * (la - np.log(LO[2])) / (np.log(HI[2]) - np.log(LO[2])) - 1.0
+        return np.hstack([z[:, :5], np.cos(params[:, 5:6]), np.sin(params[:, 5:6]), z[:, 6:]])
 
     def t(self, G, P):
         return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, (P - self.pm) / self.ps])
@@ -227,13 +237,17 @@ def upsample(pooled):
     return r[:, :, i0] * (1 - f)[None, None, :] + r[:, :, i1] * f[None, None, :]
 
 
+N_FEATURES = 9  # Norm.x
+
+
 class Ensemble:
     def __init__(self, members=4, width=512, depth=3, seed=0):
-        self.nets = [MLP(8, width, depth, NGAUGES + (128 // POOL) ** 2, seed=seed + 101 * k) for k in range(members)]
+        self.nets = [MLP(N_FEATURES, width, depth, NGAUGES + (128 // POOL) ** 2, seed=seed + 101 * k)
+                     for k in range(members)]
 
-    def train(self, X, T, epochs, batch=512, lr=1e-3, seed=0):
+    def train(self, X, T, epochs, batch=512, lr=1e-3, seed=0, weight_decay=0.0):
         batch = max(16, min(batch, len(X) // 16 * 16))
-        return [net.train(X, T, epochs, batch, lr, seed + 7 * k) for k, net in enumerate(self.nets)]
+        return [net.train(X, T, epochs, batch, lr, seed + 7 * k, weight_decay) for k, net in enumerate(self.nets)]
 
     def predict(self, X, norm):
         outs = [norm.back(net.predict(X)) for net in self.nets]
@@ -247,39 +261,66 @@ class Ensemble:
 
 
 def spread(Gm, floor=0.05):
-    """Relative disagreement of the members per scenario: the largest over
-    gauges of std / mean (gauges whose mean maximum is below `floor` m are
-    left out)."""
+    """Relative disagreement of the members per scenario: the mean over
+    gauges of std / mean, leaving out gauges whose mean maximum is below
+    `floor` m."""
     mean = Gm.mean(0)
     rel = Gm.std(0) / np.maximum(mean, 1e-9)
-    rel = np.where(mean >= floor, rel, 0.0)
-    return rel.max(axis=1)
+    keep = mean >= floor
+    return np.where(keep, rel, 0.0).sum(axis=1) / np.maximum(keep.sum(axis=1), 1)
 
 
-def run(n_train=4096, n_test=256, steps=2000, epochs=400, gate=0.05, seed=0):
+def gauge_errors(Gp, G, floor=0.05):
+    """Relative error per gauge (gauges with a solver maximum of at least
+    `floor` m), and its mean per scenario."""
+    mask = G >= floor
+    rel = np.abs(Gp - G) / np.maximum(G, 1e-9)
+    per = np.where(mask, rel, 0.0).sum(axis=1) / np.maximum(mask.sum(axis=1), 1)
+    return rel, mask, per
+
+
+def calibrate_gate(sp, rel, mask, target):
+    """The largest spread threshold whose accepted scenarios keep the mean
+    gauge error within `target` (on a validation split)."""
+    best = 0.0
+    for thr in np.sort(sp):
+        acc = sp <= thr
+        e = rel[acc[:, None] & mask]
+        if e.size and e.mean() <= target:
+            best = thr
+    return float(best)
+
+
+def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256):
+    """Data from the batched solver, the ensemble trained on n_train - n_val
+    runs, its gate calibrated on the n_val others, judged on n_test held-out
+    runs against the solver."""
     base = base_grid(seed)
-    Xtr = sample_params(n_train, seed + 1)
+    Xall = sample_params(n_train, seed + 1)
     Xte = sample_params(n_test, seed + 2)
     t0 = time.perf_counter()
-    Gtr, Ptr, _, t_data, bad_tr = solve(Xtr, base, steps)
+    Gall, Pall, _, t_data, bad_tr = solve(Xall, base, steps)
     t_gen = time.perf_counter() - t0
     Gte, Pte, Fte, t_test_solve, bad_te = solve(Xte, base, steps)
+    Xtr, Gtr, Ptr = Xall[n_val:], Gall[n_val:], Pall[n_val:]
+    Xva, Gva = Xall[:n_val], Gall[:n_val]
     norm = Norm(Gtr, Ptr)
     ens = Ensemble(seed=seed)
     t0 = time.perf_counter()
     losses = ens.train(norm.x(Xtr), norm.t(Gtr, Ptr), epochs)
     t_train = time.perf_counter() - t0
-    # the surrogate path: ensemble prediction, then the gate
+    # the gate, from the validation split
+    Gv, _, Gvm = ens.predict(norm.x(Xva), norm)
+    rel_v, mask_v, _ = gauge_errors(Gv, Gva)
+    thr = calibrate_gate(spread(Gvm), rel_v, mask_v, target)
+    # the surrogate path on the test split: ensemble prediction, then the gate
     t0 = time.perf_counter()
     Gp, Pp, Gm = ens.predict(norm.x(Xte), norm)
     sp = spread(Gm)
+    accept = sp <= thr
     t_pred = time.perf_counter() - t0
-    accept = sp <= gate
-    # error against the solver on gauges with a maximum of at least 5 cm
-    mask = Gte >= 0.05
-    rel = np.abs(Gp - Gte) / np.maximum(Gte, 1e-9)
+    rel, mask, _ = gauge_errors(Gp, Gte)
     rel_acc = rel[accept[:, None] & mask]
-    rel_all = rel[mask]
     win_err = np.abs(upsample(Pp) - Fte)  # m, on the full 128 x 128 window
     # one-at-a-time solves of a few test scenarios: the method without the surrogate
     n_single = min(16, n_test)
@@ -298,17 +339,17 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=400, gate=0.05, seed=0):
     per_batch = t_test_solve / n_test
     n_fallback = int((~accept).sum())
     t_gated = t_pred + n_fallback * per_batch  # fallbacks go to the batched solver
-    res = dict(train=n_train, test=n_test, steps=steps, epochs=epochs, gate=gate,
+    res = dict(train=len(Xtr), validation=n_val, test=n_test, steps=steps, epochs=epochs, target=target,
                nonfinite_runs=int(bad_tr + bad_te),
                data_seconds=round(t_gen, 2), solver_seconds_train=round(t_data, 2),
                train_seconds=round(t_train, 2),
                final_loss=[round(float(l[-1]), 5) for l in losses],
                first_loss=[round(float(l[0]), 5) for l in losses],
-               accepted=int(accept.sum()), fallback=n_fallback,
+               gate_threshold=round(thr, 4), accepted=int(accept.sum()), fallback=n_fallback,
+               gauge_rel_err_all_mean=round(float(rel[mask].mean()), 4),
+               gauge_rel_err_all_p90=round(float(np.quantile(rel[mask], 0.9)), 4),
                gauge_rel_err_accepted_mean=round(float(rel_acc.mean()), 4) if rel_acc.size else None,
                gauge_rel_err_accepted_median=round(float(np.median(rel_acc)), 4) if rel_acc.size else None,
-               gauge_rel_err_all_mean=round(float(rel_all.mean()), 4),
-               gauge_rel_err_all_p90=round(float(np.quantile(rel_all, 0.9)), 4),
                gated_rel_err_mean=round(float(np.where(accept[:, None], rel, 0.0)[mask].mean()), 4),
                window_abs_err_mean_m=round(float(win_err.mean()), 4),
                window_max_mean_m=round(float(Fte.max(axis=(1, 2)).mean()), 4),
@@ -317,7 +358,8 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=400, gate=0.05, seed=0):
                surrogate_scenarios_per_s=round(n_test / t_pred, 1),
                gated_scenarios_per_s=round(n_test / t_gated, 1),
                one_at_a_time_scenarios_per_s=round(1.0 / per_single, 2),
-               gated_speedup_vs_one_at_a_time=round(per_single * n_test / t_gated, 1))
+               gated_speedup_vs_one_at_a_time=round(per_single * n_test / t_gated, 1),
+               gated_speedup_vs_batched=round(per_batch * n_test / t_gated, 1))
     ens.close()
     return res
 
@@ -327,12 +369,12 @@ def main():
     ap.add_argument("--train", type=int, default=4096)
     ap.add_argument("--test", type=int, default=256)
     ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=400)
-    ap.add_argument("--gate", type=float, default=0.05)
+    ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--target", type=float, default=0.045)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args()
     pkg.build.build()
-    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.gate, a.seed)), flush=True)
+    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed)), flush=True)
 
 
 if __name__ == "__main__":

@@ -50,9 +50,10 @@ int cliffs_mlp_gradients(cliffs_mlp *m, int32_t batch, const float *x, const flo
 /* Train with Adam on n samples (x: n x n_in, t: n x n_out): `epochs` passes
  * over a seeded shuffle in batches of `batch` (multiple of 16; the last
  * partial batch of an epoch is left out), learning rate lr with a cosine
- * decay to lr/20.  losses (epochs) gets each epoch's mean batch loss. */
+ * decay to lr/20, decoupled weight decay weight_decay on the weights (not the
+ * biases).  losses (epochs) gets each epoch's mean batch loss. */
 int cliffs_mlp_train(cliffs_mlp *m, int32_t n, const float *x, const float *t, int32_t epochs, int32_t batch,
-                     float lr, uint64_t seed, float *losses);
+                     float lr, float weight_decay, uint64_t seed, float *losses);
 /* Kernels launched so far. */
 int cliffs_mlp_launch_count(const cliffs_mlp *m, int64_t *n);
 
