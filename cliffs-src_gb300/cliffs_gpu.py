@@ -107,6 +107,7 @@ SIGNATURES = {
     "cliffs_gpu_profile_read": ([_V, _dp, ctypes.POINTER(ctypes.c_int64), _dp,
                                  ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_gpu_set_graph_steps": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
     "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
@@ -396,6 +397,9 @@ class GpuGrid:
         n = ctypes.c_int64()
         _chk(self.L.cliffs_gpu_launch_count(self.h, ctypes.byref(n)), "launch_count")
         return int(n.value)
+
+    def set_graph_steps(self, k):
+        _chk(self.L.cliffs_gpu_set_graph_steps(self.h, int(k)), "set_graph_steps")
 
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")

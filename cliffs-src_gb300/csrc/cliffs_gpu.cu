@@ -88,6 +88,11 @@ struct cliffs_ctx {
   unsigned sweeps = 0;  // fast-kernel block shapes (cliffs_gpu_set_tiling)
   bool geo_uni_x = false, geo_uni_y = false;
   float4 geo0_x = {0, 0, 0, 0}, geo0_y = {0, 0, 0, 0};
+  // steps of the sweep loop captured in a CUDA graph (cliffs_gpu_step);
+  // valid for the tiling and state copy it was captured with
+  int graph_k = 16;
+  cudaGraphExec_t graph = nullptr;
+  int graph_built = 0, graph_cur = -1, graph_blk = 0, graph_wy = 0;
   bool prof = false;
   std::vector<ProfPair> prof_pending;
   double prof_ms[2] = {0, 0};
@@ -725,6 +730,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
     cudaFree(n.SN_nx);
     cudaFree(n.SN_cx);
   }
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
 }
@@ -956,10 +962,69 @@ int cliffs_gpu_feed_start(cliffs_ctx* c, double cuke) {
   return it >= nt ? -1 : it;
 }
 
+// Plain steps (no forcing, profiling or rising source) from a CUDA graph of
+// graph_k steps: one launch per graph_k steps instead of two per step.  A
+// whole step leaves the state copy where it found it, so the graph's
+// arguments hold for every replay.
+static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done, int* done_out) {
+  const int k = c->graph_k;
+  *done_out = 0;
+  if (k < 2 || nsteps < k || c->feed_on || c->prof || c->rise_on) return CLIFFS_OK;
+  if (!c->graph || c->graph_built != k || c->graph_cur != c->cur || c->graph_blk != c->blk_x ||
+      c->graph_wy != c->warps_y) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    const int64_t launches = c->launches;
+    const unsigned sweeps = c->sweeps;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int r = CLIFFS_OK;
+    for (int s = 0; s < k && !r; ++s) {
+      if (c->xrun) r = launch_sweep(c, 1, !c->yrun, nullptr, nullptr, c->ny, 2, 0.0);
+      if (!r && c->yrun) r = launch_sweep(c, 2, true, nullptr, nullptr, c->nx, 2, 0.0);
+    }
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->launches = launches;  // captured, not launched
+    c->sweeps = sweeps;
+    if (r || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return r ? r : CLIFFS_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return CLIFFS_ERR_CUDA;
+    c->graph_built = k;
+    c->graph_cur = c->cur;
+    c->graph_blk = c->blk_x;
+    c->graph_wy = c->warps_y;
+  }
+  const int per = (c->xrun ? 1 : 0) + (c->yrun ? 1 : 0);
+  int done = 0;
+  for (; done + k <= nsteps; done += k) {
+    CK(cudaGraphLaunch(c->graph, c->stream));
+    c->launches += (int64_t)per * k;
+    c->sweeps += (unsigned)(per * k);
+    for (int s = 0; s < k; ++s) *t = *t + c->dt;
+    if (steps_done) *steps_done += k;
+  }
+  *done_out = done;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_set_graph_steps(cliffs_ctx* c, int32_t k) {
+  if (!c || k < 0 || k > 4096) return CLIFFS_ERR_ARG;
+  c->graph_k = k;
+  return CLIFFS_OK;
+}
+
 int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_done) {
   if (!c || !t || nsteps < 0) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   if (steps_done) *steps_done = 0;
+  int gdone = 0;
+  const int gr = graph_steps(c, nsteps, t, steps_done, &gdone);
+  if (gr) return gr;
+  nsteps -= gdone;
   for (int s = 0; s < nsteps; ++s) {
     *t = *t + c->dt;
     // forcing record cursor (cliffs_main.f:305-315)
@@ -994,7 +1059,7 @@ int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_don
                            c->irec, cc);
       if (r) return r;
     }
-    if (steps_done) *steps_done = s + 1;
+    if (steps_done) *steps_done = gdone + s + 1;
     if (c->prof && c->prof_pending.size() > 4096) {
       int r = flush_profile(c);
       if (r) return r;

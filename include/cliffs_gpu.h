@@ -213,6 +213,11 @@ int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
  * entry point counts its own launches; copies and memsets are not kernels). */
 int cliffs_gpu_launch_count(cliffs_ctx *ctx, int64_t *n);
 
+/* Steps captured in one CUDA graph by cliffs_gpu_step (default 16; 0 or 1:
+ * no graph).  Plain steps (no boundary forcing, profiling or rising source)
+ * are replayed from the graph, one launch per k steps. */
+int cliffs_gpu_set_graph_steps(cliffs_ctx *ctx, int32_t k);
+
 /* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
  * and warps per block of the y-sweep kernel (<= 8).  0 keeps the current
  * value.  Results do not depend on the tiling. */
