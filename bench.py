@@ -5,10 +5,14 @@ over all columns with the fused max-wave update), i.e. one pass of the hot
 path of cliffs_main.f:303-355.  Metric: Mcell-updates/s = nx*ny*steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--kernels-only]
+                  [--kernels-only] [--workload shelf2048|sphere4320]
 
 --kernels-only runs the device-resident passes alone (no end-to-end pass, no
 CPU sample): the command the ncu summaries under profiles/ capture.
+
+--workload sphere4320 runs a 4320 x 2160 spherical grid (1/12 degree in
+longitude, 80S-80N) instead of the 2048^2 Cartesian shelf, the default and
+the benchmark line.
 
 --impl reference times the CPU restatement of the reference solver (the
 Fortran reference cannot be compiled on these hosts) with all host threads on
@@ -109,20 +113,37 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def workload():
+def workload(name="shelf2048"):
+    """shelf2048: the benchmark (2048^2 Cartesian shelf basin at 100 m).
+    sphere4320: a 4320 x 2160 spherical grid (1/12 degree in longitude,
+    80 S to 80 N) on the same bathymetry generator, 37 MB per field."""
     import importlib
+
+    import numpy as np
     W = importlib.import_module("cliffs-src_gb300.workloads")
-    case = W.shelf_2d(seed=SEED, nx=NX, ny=NY, dx=DX, steps=3000, ngauges=64)
-    case["crough"] = 0.000625  # Manning n = 0.025, as in the reference's Okushiri example
-    return case
+    if name == "shelf2048":
+        case = W.shelf_2d(seed=SEED, nx=NX, ny=NY, dx=DX, steps=3000, ngauges=64)
+        case["crough"] = 0.000625  # Manning n = 0.025, as in the reference's Okushiri example
+        case["label"] = (f"shelf_2d {NX}x{NY} dx={DX:g} m, FP32 state, runs of at most {HORIZON} steps from the "
+                         f"initial state, 64 gauges every 10 steps (end-to-end pass)")
+        case["source_label"] = "elliptical Gaussian uplift 100x50 km, 2 m"
+        return case
+    if name == "sphere4320":
+        nx, ny = 4320, 2160
+        case = W.sphere_2d(seed=SEED + 3, nx=nx, ny=ny, steps=3000, ngauges=64)
+        case["crough"] = 0.000625
+        case["label"] = (f"spherical {nx}x{ny}, 1/12 deg in longitude, 80S-80N, FP32 state, runs of at most "
+                         f"{HORIZON} steps, 64 gauges every 10 steps (end-to-end pass)")
+        case["source_label"] = "elliptical Gaussian uplift, half-axes 30x15 nodes, 2 m"
+        return case
+    raise ValueError(f"unknown workload {name}")
 
 
 def config_dict(case, impl_note):
-    return {"workload": f"shelf_2d {NX}x{NY} dx={DX:g} m, FP32 state, runs of at most {HORIZON} "
-                        f"steps from the initial state, 64 gauges every 10 steps (end-to-end pass)",
-            "grid": [NX, NY], "dt_s": round(case["dt"], 6), "ground_m": case["ground"],
-            "crough": case["crough"], "source": "elliptical Gaussian uplift 100x50 km, 2 m",
-            "l2": "working set ~151 MB per step > 129 MB L2; no flush",
+    ny, nx = case["dep"].shape
+    return {"workload": case["label"], "grid": [nx, ny], "dt_s": round(case["dt"], 6), "ground_m": case["ground"],
+            "crough": case["crough"], "source": case["source_label"],
+            "l2": f"working set ~{9 * nx * ny * 4 / 1e6:.0f} MB per step > 129 MB L2; no flush",
             "parallelism": "replicas only (one independent grid per GPU)", "impl": impl_note}
 
 
@@ -136,9 +157,10 @@ def cpu_baseline(case, steps, threads):
     t0 = time.perf_counter()
     m.step(steps)
     dt = time.perf_counter() - t0
-    val = NX * NY * steps / dt / 1e6
+    cells = case["dep"].size
+    val = cells * steps / dt / 1e6
     return {"value": round(val, 3), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{NX}x{NY} grid, {steps} time steps after 1 warm-up step, "
+            "sample": f"{case['dep'].shape[1]}x{case['dep'].shape[0]} grid, {steps} time steps after 1 warm-up step, "
                       f"OpenMP over lines ({threads} threads), FP64"}
 
 
@@ -150,12 +172,12 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle  # noqa: F401  (builds/loads the CPU restatement)
-    case = workload()
+    case = workload(args.workload)
     steps = max(1, min(args.steps, 300))
     cb = cpu_baseline(case, steps, threads)
     line = {"metric": "Mcell-updates/s", "value": cb["value"], "unit": "Mcell-updates/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": 1,
-            "ms_per_step": round(1e3 * NX * NY / (cb["value"] * 1e6), 3), "higher_is_better": True,
+            "ms_per_step": round(1e3 * case["dep"].size / (cb["value"] * 1e6), 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(case, "CPU restatement of cliffs.f + cliffs_main.f time loop"),
             "impl": "reference", "cpu_baseline": cb,
@@ -171,12 +193,12 @@ def run_e2e(pkg, case, args, barrier, dist, world):
     import numpy as np
     import torch
 
-    cells = NX * NY
+    cells = case["dep"].size
+    ny, nx = case["dep"].shape
     barrier()
     t0 = time.perf_counter()
-    g2 = pkg.GpuGrid(case["dep"], dx=np.full(NX - 1, DX), dy=np.full(NY - 1, DX),
-                     ground=case["ground"], crough=case["crough"], dt=case["dt"])
-    g2.set_initial(case["H0"], case["u0"], case["v0"])
+    g2 = pkg.GpuGrid.from_case(case)  # metrics, create, initial state
+    g2.set_graph_steps(10)  # one graph per gauge interval
     I, J = case["gauges"]
     nrec = 0
     for s0 in range(0, args.steps, 10):
@@ -191,7 +213,7 @@ def run_e2e(pkg, case, args, barrier, dist, world):
         t = torch.tensor([t_e2e], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_e2e = float(t.item())
-    h2d = cells * 8 * 4 + (NX + NY) * 8 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), spacing, gauge indices
+    h2d = cells * 8 * 4 + (nx + ny) * 8 * 3 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), metrics, gauge indices
     d2h = cells * 8 * 3 + cells * 4 * 2 + nrec * 64 * 3 * 8
     return {"value": round(world * cells * args.steps / t_e2e / 1e6, 3), "unit": "Mcell-updates/s",
             "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps)}
@@ -211,8 +233,8 @@ def run_ours(args):
         dist.init_process_group("gloo")
     pkg = importlib.import_module("cliffs-src_gb300")
     pkg.build.build()
-    case = workload()
-    cells = NX * NY
+    case = workload(args.workload)
+    cells = case["dep"].size
 
     def barrier():
         if dist is not None:
@@ -282,6 +304,7 @@ def run_ours(args):
         with open(tp) as f:
             tr = json.load(f)
         key = "y" if ky >= kx else "x"
+        tr = tr.get(args.workload, {})
         if key in tr:
             traffic = int(tr[key]["bytes_per_cell"] * cells)
     roof = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak,
@@ -314,6 +337,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernels-only", action="store_true")
+    ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -18,8 +18,8 @@ Cliffs run reads (cliffs_main.f, allabout.f):
   gout, seaout output intervals in steps
 
 Sizes, depths and sources follow the benchmark configurations: a 1-D channel
-with a solitary wave running up a 1:20 beach, and a 2-D shelf/slope basin
-with an elliptical Gaussian uplift.
+with a solitary wave running up a 1:20 beach, a 2-D shelf/slope basin with an
+elliptical Gaussian uplift, and the same basin on a spherical grid.
 """
 import numpy as np
 
@@ -121,3 +121,25 @@ def shelf_2d(seed=0, nx=2048, ny=2048, dx=100.0, steps=3000, amp=2.0,
                 ground=0.01, crough=0.0, dt=float(dt), steps=steps,
                 gauges=(I, J), gout=10, seaout=steps + 1, amplitude=float(amp),
                 theta=float(theta))
+
+
+EARTHR = 6371009.0  # earth radius of MasterGrid.f's metric
+
+
+def sphere_2d(seed=3, nx=4320, ny=2160, lat=(-80.0, 80.0), dlon=1.0 / 12.0, steps=3000, ngauges=64,
+              axes_nodes=(60, 30)):
+    """shelf_2d laid out in node units (1 km per node) and placed on a
+    spherical grid: longitudes 0, dlon, ... (nx nodes), latitudes evenly from
+    lat[0] to lat[1] (ny nodes), cartesian False.  The source's full axes
+    span axes_nodes nodes.  dt from CFL 0.8 on the smallest cell (the x
+    spacing at the highest |latitude|) and the maximum depth."""
+    case = shelf_2d(seed=seed, nx=nx, ny=ny, dx=1000.0, steps=steps, ngauges=ngauges,
+                    axes_km=tuple(float(a) for a in axes_nodes))
+    lon = np.arange(nx, dtype=np.float64) * dlon
+    lats = np.linspace(lat[0], lat[1], ny)
+    beta = np.pi * EARTHR / 180.0
+    coslat = np.cos(np.radians(np.max(np.abs(lats))))
+    dmin = min(beta * dlon * coslat, beta * (lats[1] - lats[0]))
+    case.update(name=f"sphere_2d_{nx}x{ny}", xcrd=lon, ycrd=lats, cartesian=False,
+                dt=float(0.8 * dmin / np.sqrt(GRAV * float(np.max(case["H0"])))))
+    return case
