@@ -68,6 +68,7 @@ class BatchPlan(ctypes.Structure):
 
 
 PERSISTENT, GRAPH = 0, 1
+TILED, STAGED = 0, 1  # cliffs_gpu_set_sweep_kernel
 
 
 class CliffsError(RuntimeError):
@@ -109,6 +110,8 @@ SIGNATURES = {
     "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_set_graph_steps": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
+    "cliffs_gpu_set_sweep_kernel": ([_V, _I], ctypes.c_int),
+    "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
     "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
     "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),
@@ -403,6 +406,15 @@ class GpuGrid:
 
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")
+
+    def set_sweep_kernel(self, kind):
+        """STAGED (persistent, TMA-staged windows; the default) or TILED."""
+        _chk(self.L.cliffs_gpu_set_sweep_kernel(self.h, int(kind)), "set_sweep_kernel")
+
+    def check_stage_timeout(self, wait_ms=50):
+        """Failure-detection check of the staged kernels' stage waits; returns
+        the library status (CLIFFS_ERR_TIMEOUT = -7 expected)."""
+        return self.L.cliffs_gpu_check_stage_timeout(self.h, int(wait_ms))
 
 
 class Batch:

@@ -2,6 +2,7 @@
 // auxiliary kernels: state conversion, wetness bitmaps, output conversions,
 // gauges, runup, nested-grid feed.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -10,6 +11,7 @@
 
 #include "../../include/cliffs_gpu.h"
 #include "batch.cuh"
+#include "staged.cuh"
 
 using namespace cliffs;
 
@@ -37,6 +39,33 @@ struct ProfPair {
   cudaEvent_t a, b;
   int dir;
 };
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encoder() {
+  if (g_encode) return CLIFFS_OK;
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return CLIFFS_ERR_CUDA;
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return CLIFFS_OK;
+}
+
+// 2-D FP32 map over an nx x ny field with a row pitch of `pitch` floats and a
+// box of bx x by elements; elements outside the field read 0.
+int make_map(CUtensorMap* m, const float* base, int nx, int ny, int pitch, int bx, int by) {
+  cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  cuuint32_t es[2] = {1, 1};
+  const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+}
 
 }  // namespace
 
@@ -93,6 +122,14 @@ struct cliffs_ctx {
   int graph_k = 16;
   cudaGraphExec_t graph = nullptr;
   int graph_built = 0, graph_cur = -1, graph_blk = 0, graph_wy = 0;
+  // sweep kernels (cliffs_gpu_set_sweep_kernel): the staged persistent pair
+  // needs the y-sweep's tensor maps (one per state copy) and its grid size
+  int sweep_kind = CLIFFS_SWEEP_TILED;
+  bool staged_ok = false;
+  CUtensorMap m_dep, m_srf[2], m_xu[2], m_yv[2], m_hmax, m_velmax;
+  int grid_sx = 0, grid_sy = 0;  // resident blocks of staged_x / staged_y
+  unsigned long long stage_ns = 2000000000ull;  // limit of one stage wait
+  int graph_kind = -1;
   bool prof = false;
   std::vector<ProfPair> prof_pending;
   double prof_ms[2] = {0, 0};
@@ -520,7 +557,19 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     pp.dir = iu - 1;
     CK(cudaEventRecord(pp.a, c->stream));
   }
-  if (iu == 1) {
+  const bool staged = c->sweep_kind == CLIFFS_SWEEP_STAGED && c->staged_ok;
+  if (staged) {
+    const StageCtl S{c->stage_ns, 0u};
+    ++c->launches;
+    if (iu == 1) {
+      const int tiles = (A.n + kXTile - 1) / kXTile * A.nlines;
+      staged_x<<<std::min(tiles, c->grid_sx), kStagedThreads, 0, c->stream>>>(A, S);
+    } else {
+      const int tiles = (A.n + kYRows - 1) / kYRows * ((A.nlines + 31) / 32);
+      const YMaps M{c->m_dep, c->m_srf[c->cur], c->m_xu[c->cur], c->m_yv[c->cur], c->m_hmax, c->m_velmax};
+      staged_y<<<std::min(tiles, c->grid_sy), kStagedThreads, 0, c->stream>>>(A, M, S);
+    }
+  } else if (iu == 1) {
     const int cells = c->blk_x * kCellsPerThread;
     const dim3 grid((A.n + cells - 1) / cells, A.nlines);
     ++c->launches;
@@ -708,6 +757,26 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   if (!zeta_nonzero) {
     cudaFree(c->scl_y);
     c->scl_y = nullptr;
+  }
+  // the staged sweep kernels: tensor maps of the y-sweep's fields and the
+  // resident grid of each kernel; without them the context keeps fast_kernel
+  {
+    int nsm = 0, bx = 0, by = 0;
+    bool ok = get_encoder() == CLIFFS_OK &&
+              cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, staged_x, kStagedThreads, 0) == cudaSuccess &&
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, staged_y, kStagedThreads, 0) == cudaSuccess &&
+              bx > 0 && by > 0;
+    const int nx = c->nx, ny = c->ny, pp = c->pitch;
+    ok = ok && !make_map(&c->m_dep, c->dep, nx, ny, pp, 32, kYWin) && !make_map(&c->m_hmax, c->hmax, nx, ny, pp, 32, kYRows) &&
+         !make_map(&c->m_velmax, c->velmax, nx, ny, pp, 32, kYRows);
+    for (int k = 0; k < 2 && ok; ++k)
+      ok = !make_map(&c->m_srf[k], c->srf[k], nx, ny, pp, 32, kYWin) &&
+           !make_map(&c->m_xu[k], c->xu[k], nx, ny, pp, 32, kYWin) &&
+           !make_map(&c->m_yv[k], c->yv[k], nx, ny, pp, 32, kYWin);
+    c->staged_ok = ok;
+    c->grid_sx = nsm * bx;
+    c->grid_sy = nsm * by;
   }
   *out = c;
   return CLIFFS_OK;
@@ -971,7 +1040,7 @@ static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done
   *done_out = 0;
   if (k < 2 || nsteps < k || c->feed_on || c->prof || c->rise_on) return CLIFFS_OK;
   if (!c->graph || c->graph_built != k || c->graph_cur != c->cur || c->graph_blk != c->blk_x ||
-      c->graph_wy != c->warps_y) {
+      c->graph_wy != c->warps_y || c->graph_kind != c->sweep_kind) {
     if (c->graph) cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
     const int64_t launches = c->launches;
@@ -997,6 +1066,7 @@ static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done
     c->graph_cur = c->cur;
     c->graph_blk = c->blk_x;
     c->graph_wy = c->warps_y;
+    c->graph_kind = c->sweep_kind;
   }
   const int per = (c->xrun ? 1 : 0) + (c->yrun ? 1 : 0);
   int done = 0;
@@ -1328,7 +1398,30 @@ int cliffs_gpu_status(cliffs_ctx* c, uint32_t* flags) {
   CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CK(cudaStreamSynchronize(c->stream));
   *flags = f;
-  return (f & CLIFFS_ST_NAN) ? CLIFFS_ERR_NAN : CLIFFS_OK;
+  if (f & CLIFFS_ST_NAN) return CLIFFS_ERR_NAN;
+  return (f & CLIFFS_ST_STALL) ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
+}
+
+int cliffs_gpu_set_sweep_kernel(cliffs_ctx* c, int32_t kind) {
+  if (!c || (kind != CLIFFS_SWEEP_TILED && kind != CLIFFS_SWEEP_STAGED)) return CLIFFS_ERR_ARG;
+  c->sweep_kind = kind;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_check_stage_timeout(cliffs_ctx* c, int32_t wait_ms) {
+  if (!c || wait_ms < 1 || wait_ms > 2000) return CLIFFS_ERR_ARG;
+  if (!c->have_state || !c->staged_ok || !c->xrun) return CLIFFS_ERR_STATE;
+  const SweepArgs A = sweep_args(c, 1, false, c->cur);  // writes copy 1 - cur, which stays unused
+  const StageCtl S{(unsigned long long)wait_ms * 1000000ull, 16u};
+  const int tiles = (A.n + kXTile - 1) / kXTile * A.nlines;
+  ++c->launches;
+  staged_x<<<std::min(tiles, c->grid_sx), kStagedThreads, 0, c->stream>>>(A, S);
+  CK(cudaGetLastError());
+  unsigned f = 0;
+  CK(cudaMemcpyAsync(&f, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return (f & ST_STALL) ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
 }
 
 int cliffs_gpu_sync(cliffs_ctx* c) {

@@ -92,6 +92,21 @@ __device__ __forceinline__ Geo<float> geo_at(const SweepArgs& A, int m, float al
   return r;
 }
 
+// Geometry of position m for the plain update: g0 is the line's uniform
+// geometry, already scaled by the row factor; a non-uniform line reads its
+// table.  Unlike geo_at there is no zeroing at the line ends: the plain update
+// only keeps cells with 2 <= m <= n-1, and the caller clamps m to 1..n.
+__device__ __forceinline__ Geo<float> geo_plain(const SweepArgs& A, int m, const Geo<float>& g0, float alpha,
+                                                float ialpha) {
+  Geo<float> r = g0;
+  if (!A.geo_uniform) {
+    const float4 g = __ldg(A.geo + (m - 1));
+    r = Geo<float>{g.x * ialpha, g.y * ialpha, g.z * ialpha, g.w * alpha, 0.f};
+  }
+  r.scl = A.scl ? __ldg(A.scl + (m - 1)) : 0.f;
+  return r;
+}
+
 // edge1 (cell 1, side 0) or edge2 (cell n, side 1) of line L.
 __device__ __forceinline__ EdgeVals<float> edge_vals(const SweepArgs& A, int L, int side) {
   if (!A.edges) return EdgeVals<float>{0.f, 0.f, 0.f};
@@ -190,6 +205,12 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   if (!isfinite(r.s + xo + yo)) atomicOr(A.status, ST_NAN);
 }
 
+template <int DIR, bool LOCAL, bool COH, bool TAIL = true>
+__device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
+                                            float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
+                                            float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
+                                            uint32_t* s_list, unsigned* s_n);
+
 // LOCAL: the block finishes its own listed cells after its fast cells (a
 // block-local list in shared memory); otherwise they go to the global
 // worklist for general_kernel.
@@ -217,8 +238,6 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     i0 = (bx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5)) * kCellsPerThread + 1;
   }
   const bool active = L <= A.nlines && i0 <= n;
-  const bool swept = active && L >= A.lo && L <= A.hi;
-  const Phys<float>& p = A.ph;
   // window w[0..5] = positions i0-1 .. i0+4 (u normal, v tangential); e
   // holds the surface state as loaded, then eta
   float d[6], e[6], u[6], v[6];
@@ -287,19 +306,38 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
       }
     }
   }
-  float H[6];
-#pragma unroll
-  for (int w = 0; w < 6; ++w) {  // surface state -> (eta, H); the stored form stays exact in one of them
-    H[w] = depth_of(e[w], d[w]);
-    e[w] = eta_of(e[w], d[w]);
-  }
+  sweep_cells<DIR, LOCAL, COH>(A, L, i0, active, q0, d, e, u, v, hm, vm, s_list, &s_n);
+}
+
+// The cells i0..i0+3 of line L from their loaded window: d depth, e surface
+// state, u normal and v tangential velocity at positions i0-1 .. i0+4, hm/vm
+// the max-wave values of the 4 cells (when fused).  Updates and stores them;
+// cells that need the full wet/dry rules go to the block's list s_list
+// (LOCAL: finished by the whole block after a __syncthreads) or to the
+// global worklist.  q0 is the first cell's index (x-sweep).  The whole block
+// calls it.  TAIL = false leaves the block's list to the caller, who must
+// finish it after a barrier (the fast stores come first).
+template <int DIR, bool LOCAL, bool COH, bool TAIL>
+__device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
+                                            float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
+                                            float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
+                                            uint32_t* s_list, unsigned* s_n) {
+  const int n = A.n;
+  const bool swept = active && L >= A.lo && L <= A.hi;
+  const Phys<float>& p = A.ph;
   // os: new surface state of cells i0..i0+3, initially the state as loaded
   float os[kCellsPerThread], ou[kCellsPerThread], ov[kCellsPerThread];
 #pragma unroll
   for (int r = 0; r < kCellsPerThread; ++r) {
-    os[r] = d[r + 1] < 0.f ? H[r + 1] : e[r + 1];
+    os[r] = e[r + 1];
     ou[r] = u[r + 1];
     ov[r] = v[r + 1];
+  }
+  float H[6];
+#pragma unroll
+  for (int w = 0; w < 6; ++w) {  // surface state -> (eta, H); the stored form stays exact in one of them
+    H[w] = e[w] + fmaxf(d[w], 0.f);  // depth_of and eta_of without a branch
+    e[w] = e[w] - fminf(d[w], 0.f);
   }
   unsigned need = 0u;  // bit r: cell i0+r goes to the general path
   if (swept) {  // lines not swept are copied through
@@ -314,8 +352,9 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     bool sup = false;  // a supercritical cell (|u| > c) in the window
 #pragma unroll
     for (int w = 0; w < 6; ++w) {
-      const int k = i0 - 1 + w;
-      wet[w] = (k >= 1 && k <= n) && H[w] > p.ground;
+      // in range or not: the window of a cell that can take the plain update
+      // (2 <= k <= n-1) is; the rare branch below applies the range
+      wet[w] = H[w] > p.ground;
       c[w] = fsqrt_pos(p.g * fmaxf(H[w], p.ground));
       sup = sup || fabsf(u[w]) > c[w];
     }
@@ -327,6 +366,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     // between wet neighbours, and no transcritical point can occur (a
     // transcritical point needs a supercritical neighbour).
     unsigned rest = 0u;  // bit r: cell i0+r is not a plain interior cell
+    const Geo<float> g0{A.geo0.x * ialpha, A.geo0.y * ialpha, A.geo0.z * ialpha, A.geo0.w * alpha, 0.f};
 #pragma unroll
     for (int r = 0; r < kCellsPerThread; ++r) {
       const int k = i0 + r;
@@ -337,13 +377,15 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
       const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
       float cn;
       const OutCell<float> o = interior_update<float, false>(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w],
-                                                             geo_at(A, k, alpha, ialpha), p, &cn);
+                                                             geo_plain(A, min(k, n), g0, alpha, ialpha), p, &cn);
       os[r] = plain ? o.s : os[r];
       ou[r] = plain ? o.u : ou[r];
       ov[r] = plain ? o.v : ov[r];
       if (!plain && k <= n) rest |= 1u << r;
     }
     if (rest) {  // line ends, shorelines, dry cells, supercritical flow
+#pragma unroll
+      for (int w = 0; w < 6; ++w) wet[w] = wet[w] && i0 - 1 + w >= 1 && i0 - 1 + w <= n;  // positions 1..n only
 #pragma unroll
       for (int r = 0; r < kCellsPerThread; ++r) {
         if (!((rest >> r) & 1u)) continue;
@@ -379,7 +421,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
 #pragma unroll
     for (int r = 0; r < kCellsPerThread; ++r)
       if (active && ((need >> r) & 1u))
-        s_list[atomicAdd(&s_n, 1u)] = (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1);
+        s_list[atomicAdd(s_n, 1u)] = (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1);
   } else {
 #pragma unroll
     for (int r = 0; r < kCellsPerThread; ++r)
@@ -426,9 +468,9 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     }
   }
   if (bad) atomicOr(A.status, ST_NAN);
-  if (LOCAL) {
+  if (LOCAL && TAIL) {
     __syncthreads();  // the block's fast values are stored; its listed cells overwrite theirs
-    const unsigned cnt = s_n;
+    const unsigned cnt = *s_n;
     for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) general_store<DIR, COH>(A, s_list[t]);
   }
 }

@@ -36,12 +36,13 @@ enum {
   CLIFFS_ERR_NOMEM = -4,      /* device allocation failed */
   CLIFFS_ERR_STATE = -5,      /* call out of order (e.g. no state uploaded) */
   CLIFFS_ERR_DEVICE = -6,     /* no usable sm_103 device */
-  CLIFFS_ERR_TIMEOUT = -7     /* a device-side wait ran out (batch barrier) */
+  CLIFFS_ERR_TIMEOUT = -7     /* a device-side wait ran out (batch barrier, sweep stage) */
 };
 
 /* status bits reported by cliffs_gpu_status() */
 enum {
-  CLIFFS_ST_NAN = 1u          /* a sweep produced a non-finite value */
+  CLIFFS_ST_NAN = 1u,         /* a sweep produced a non-finite value */
+  CLIFFS_ST_STALL = 2u        /* a staged sweep's shared-memory stage wait ran out */
 };
 
 typedef struct cliffs_ctx cliffs_ctx;
@@ -197,7 +198,8 @@ int cliffs_gpu_feed_child(cliffs_ctx *ctx, int32_t id, double cuke,
                           int32_t *arrived, double *uvq_w, double *uvq_e,
                           double *uvq_s, double *uvq_n);
 
-/* Sticky status bits (CLIFFS_ST_*) since the last call; synchronises. */
+/* Sticky status bits (CLIFFS_ST_*) since the last call; synchronises.
+ * Returns CLIFFS_ERR_NAN or CLIFFS_ERR_TIMEOUT when the matching bit is set. */
 int cliffs_gpu_status(cliffs_ctx *ctx, uint32_t *flags);
 /* Block until queued work on the context's stream is done. */
 int cliffs_gpu_sync(cliffs_ctx *ctx);
@@ -220,8 +222,28 @@ int cliffs_gpu_set_graph_steps(cliffs_ctx *ctx, int32_t k);
 
 /* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
  * and warps per block of the y-sweep kernel (<= 8).  0 keeps the current
- * value.  Results do not depend on the tiling. */
+ * value.  Results do not depend on the tiling.  Applies to the tiled sweep
+ * kernels. */
 int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
+
+/* The sweep kernels, two choices with identical results:
+ * - CLIFFS_SWEEP_TILED (the default): one block per tile, loads straight into
+ *   registers.
+ * - CLIFFS_SWEEP_STAGED: persistent kernels, one resident grid walking the
+ *   tiles.  Each block's window loads arrive in shared memory by bulk copies
+ *   (TMA), one tile ahead of the compute.  On GB300 it is the slower of the
+ *   two, by 3 % (y-sweep) to 30 % (x-sweep).
+ * A context whose tensor maps could not be made runs the tiled kernels
+ * whichever is chosen. */
+enum { CLIFFS_SWEEP_TILED = 0, CLIFFS_SWEEP_STAGED = 1 };
+int cliffs_gpu_set_sweep_kernel(cliffs_ctx *ctx, int32_t kind);
+/* Failure-detection check of the staged kernels' stage waits: one staged
+ * x-sweep whose waits expect 16 bytes more than the copies bring, each wait
+ * limited to wait_ms (1..2000).  Expected result: CLIFFS_ERR_TIMEOUT, read by
+ * the host, with the device usable afterwards.  The state is unchanged: the
+ * sweep writes the other state copy, which is not taken.
+ * CLIFFS_ERR_STATE without a state, an x-sweep or the staged kernels. */
+int cliffs_gpu_check_stage_timeout(cliffs_ctx *ctx, int32_t wait_ms);
 
 /* One sweep without any device allocation, for callers that cannot allocate
  * device memory: an application that gives the solver a fixed memory budget
