@@ -476,7 +476,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
 }
 
 template <int DIR, bool LOCAL>
-__global__ void __launch_bounds__(256, 3) fast_kernel(const SweepArgs A) {
+__global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
   sweep_tile<DIR, LOCAL, false>(A, blockIdx.x, blockIdx.y);
 }
 
