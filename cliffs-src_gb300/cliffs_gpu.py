@@ -71,6 +71,33 @@ PERSISTENT, GRAPH = 0, 1
 TILED, STAGED = 0, 1  # cliffs_gpu_set_sweep_kernel
 
 
+class _Pinned:
+    """Owner of one pinned host allocation (cliffs_gpu_host_alloc), freed
+    when the last array viewing it goes."""
+
+    def __init__(self, nbytes):
+        self.L = load()
+        self.ptr = ctypes.c_void_p()
+        _chk(self.L.cliffs_gpu_host_alloc(max(nbytes, 1), ctypes.byref(self.ptr)), "host_alloc")
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                self.L.cliffs_gpu_host_free(self.ptr)
+        except Exception:
+            pass
+
+
+def pinned(shape, dtype=np.float64):
+    """A numpy array in pinned host memory, for the asynchronous outputs."""
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape))
+    owner = _Pinned(count * dtype.itemsize)
+    buf = (ctypes.c_char * max(count * dtype.itemsize, 1)).from_address(owner.ptr.value)
+    buf._owner = owner  # the array's base keeps the allocation alive
+    return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape)
+
+
 class CliffsError(RuntimeError):
     def __init__(self, code, what):
         self.code = code
@@ -102,6 +129,15 @@ SIGNATURES = {
     "cliffs_gpu_runup": ([_V, ctypes.POINTER(Runup)], ctypes.c_int),
     "cliffs_gpu_nest_add": ([_V, ctypes.POINTER(NestDesc), _ip], ctypes.c_int),
     "cliffs_gpu_feed_child": ([_V, _I, _D, _ip, _dp, _dp, _dp, _dp], ctypes.c_int),
+    "cliffs_gpu_get_sea_state_async": ([_V, _I, _I, _fp, _fp, _fp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_gpu_get_gauges_async": ([_V, _I, _ip, _ip, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int64)],
+                                    ctypes.c_int),
+    "cliffs_gpu_feed_child_async": ([_V, _I, _D, _ip, _dp, _dp, _dp, _dp, ctypes.POINTER(ctypes.c_int64)],
+                                    ctypes.c_int),
+    "cliffs_gpu_output_wait": ([_V, ctypes.c_int64], ctypes.c_int),
+    "cliffs_gpu_output_done": ([_V, ctypes.c_int64, _ip], ctypes.c_int),
+    "cliffs_gpu_host_alloc": ([ctypes.c_int64, ctypes.POINTER(_V)], ctypes.c_int),
+    "cliffs_gpu_host_free": ([_V], None),
     "cliffs_gpu_status": ([_V, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     "cliffs_gpu_sync": ([_V], ctypes.c_int),
     "cliffs_gpu_profile": ([_V, _I], ctypes.c_int),
@@ -383,6 +419,44 @@ class GpuGrid:
         r = _chk(self.L.cliffs_gpu_feed_child(self.h, nid, float(cuke), ctypes.byref(a),
                                               _p(w), _p(e), _p(s), _p(n)), "feed_child")
         return bool(a.value), ((w, e, s, n) if r == 1 else None)
+
+    # -- asynchronous outputs --------------------------------------------------------
+    def sea_state_async(self, lonsub, latsub, out):
+        """Queue a screenshot into out = (h, u, v), float32 arrays (pinned:
+        pinned()); returns the ticket for wait()."""
+        h, u, v = out
+        t = ctypes.c_int64()
+        _chk(self.L.cliffs_gpu_get_sea_state_async(self.h, int(lonsub), int(latsub), _p(h, _fp), _p(u, _fp),
+                                                   _p(v, _fp), ctypes.byref(t)), "get_sea_state_async")
+        return t.value
+
+    def gauges_async(self, I, J, out):
+        """Queue a gauge record into out = (eta, u, v), float64 arrays."""
+        I = np.ascontiguousarray(I, np.int32)
+        J = np.ascontiguousarray(J, np.int32)
+        eta, u, v = out
+        t = ctypes.c_int64()
+        _chk(self.L.cliffs_gpu_get_gauges_async(self.h, len(I), _p(I, _ip), _p(J, _ip), _p(eta), _p(u), _p(v),
+                                                ctypes.byref(t)), "get_gauges_async")
+        return t.value
+
+    def feed_child_async(self, nest, cuke, out):
+        """Queue a feed record: out = (arrived int32 (1,), w, e (3, nn), s, n
+        (3, mm)), float64; arrived[0] = 1 when the call produced a record."""
+        nid, _ = nest
+        a, w, e, s, n = out
+        t = ctypes.c_int64()
+        _chk(self.L.cliffs_gpu_feed_child_async(self.h, nid, float(cuke), _p(a, _ip), _p(w), _p(e), _p(s), _p(n),
+                                                ctypes.byref(t)), "feed_child_async")
+        return t.value
+
+    def wait(self, ticket):
+        _chk(self.L.cliffs_gpu_output_wait(self.h, int(ticket)), "output_wait")
+
+    def done(self, ticket):
+        d = ctypes.c_int32()
+        _chk(self.L.cliffs_gpu_output_done(self.h, int(ticket), ctypes.byref(d)), "output_done")
+        return bool(d.value)
 
     # -- profiling / tuning -------------------------------------------------------
     def profile(self, enable=True):

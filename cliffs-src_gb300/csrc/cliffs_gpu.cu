@@ -5,6 +5,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -33,7 +34,21 @@ struct Nest {
   cliffs_nest_desc d;
   int32_t *WE_ny = nullptr, *SN_nx = nullptr;
   double *WE_cy = nullptr, *SN_cx = nullptr;
+  // the footprint of the arrival test: parent columns i1..i2, rows k1..k2
+  int32_t i1 = 0, i2 = 0, k1 = 0, k2 = 0;
+  int* d_arr = nullptr;  // arrival flag on the device, sticky (the asynchronous feed)
 };
+
+// One asynchronous output: a device buffer the conversion kernels write and a
+// second stream copies to the caller's host buffers, and the events that
+// order the two.
+struct OutSlot {
+  void* dbuf = nullptr;
+  size_t cap = 0;
+  cudaEvent_t conv = nullptr, done = nullptr;
+  bool used = false;
+};
+constexpr int kOutSlots = 8;
 
 struct ProfPair {
   cudaEvent_t a, b;
@@ -130,6 +145,14 @@ struct cliffs_ctx {
   int grid_sx = 0, grid_sy = 0;  // resident blocks of staged_x / staged_y
   unsigned long long stage_ns = 2000000000ull;  // limit of one stage wait
   int graph_kind = -1;
+  // asynchronous outputs: a copy stream and a ring of slots; ticket k uses
+  // slot k % kOutSlots.  Gauge indices stay on the device between calls.
+  cudaStream_t cpy = nullptr;
+  OutSlot outs[kOutSlots];
+  int64_t out_next = 0;
+  int32_t* g_ij = nullptr;
+  int g_n = 0, g_cap = 0;
+  std::vector<int32_t> g_host;
   bool prof = false;
   std::vector<ProfPair> prof_pending;
   double prof_ms[2] = {0, 0};
@@ -324,7 +347,8 @@ __global__ void k_runup(int nx, int ny, int pitch, const float* __restrict__ dep
 __global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
                           const float* __restrict__ dep, const float* __restrict__ srf,
                           const float* __restrict__ xu, const float* __restrict__ yv,
-                          double hmin, double cuke, double g, int* flag) {
+                          double hmin, double cuke, double g, int* flag, bool sticky) {
+  if (sticky && *(volatile int*)flag) return;  // arrived at an earlier call
   const int ni = ii2 - ii1 + 1, nk = kk2 - kk1 + 1;
   const long long total = (long long)ni * nk;
   const double tenth = (double)0.1f;
@@ -368,8 +392,13 @@ __global__ void k_feed_child(int mm, int nn, int W_nx, int E_nx, int S_ny, int N
                              const double* __restrict__ SN_cx, int pitch, const float* __restrict__ dep,
                              const float* __restrict__ srf, const float* __restrict__ xu,
                              const float* __restrict__ yv, double hmin, double g, double* w_out,
-                             double* e_out, double* s_out, double* n_out) {
+                             double* e_out, double* s_out, double* n_out, const int* gate, int* gate_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gate) {  // the asynchronous feed: no record before the wave reaches the child
+    const int open = *gate;
+    if (t == 0) *gate_out = open;  // the flag as this record saw it, for the host
+    if (!open) return;
+  }
   if (t < 2 * nn) {  // west / east: parent columns (ii, ii+1), rows kk, kk+1
     const int side = t / nn, i = t % nn;
     const int ii = side == 0 ? W_nx : E_nx;
@@ -798,7 +827,16 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
     cudaFree(n.WE_cy);
     cudaFree(n.SN_nx);
     cudaFree(n.SN_cx);
+    cudaFree(n.d_arr);
   }
+  if (c->cpy) cudaStreamSynchronize(c->cpy);
+  for (auto& o : c->outs) {
+    if (o.dbuf) cudaFree(o.dbuf);
+    if (o.conv) cudaEventDestroy(o.conv);
+    if (o.done) cudaEventDestroy(o.done);
+  }
+  if (c->g_ij) cudaFree(c->g_ij);
+  if (c->cpy) cudaStreamDestroy(c->cpy);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -1328,8 +1366,16 @@ int cliffs_gpu_nest_add(cliffs_ctx* c, const cliffs_nest_desc* d, int32_t* id) {
     if (!inside_x(d->SN_nx[k])) return CLIFFS_ERR_ARG;
   Nest n;
   n.d = *d;
-  if (dalloc(&n.WE_ny, d->nn) || dalloc(&n.WE_cy, d->nn) || dalloc(&n.SN_nx, d->mm) || dalloc(&n.SN_cx, d->mm))
+  // footprint of the arrival test: parent rows WE_ny(1)..WE_ny(nn)+1,
+  // columns SN_nx(1)..SN_nx(mm)+1
+  n.k1 = d->WE_ny[0];
+  n.k2 = d->WE_ny[d->nn - 1] + 1;
+  n.i1 = d->SN_nx[0];
+  n.i2 = d->SN_nx[d->mm - 1] + 1;
+  if (dalloc(&n.WE_ny, d->nn) || dalloc(&n.WE_cy, d->nn) || dalloc(&n.SN_nx, d->mm) || dalloc(&n.SN_cx, d->mm) ||
+      dalloc(&n.d_arr, 1))
     return CLIFFS_ERR_NOMEM;
+  CK(cudaMemset(n.d_arr, 0, sizeof(int)));
   CK(cudaMemcpy(n.WE_ny, d->WE_ny, d->nn * 4, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(n.WE_cy, d->WE_cy, d->nn * 8, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(n.SN_nx, d->SN_nx, d->mm * 4, cudaMemcpyHostToDevice));
@@ -1350,18 +1396,10 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
   const Nest& n = c->nests[id];
   const int st = c->cur;
   if (!*arrived) {
-    // footprint: parent rows WE_ny(1)..WE_ny(nn)+1, columns SN_nx(1)..SN_nx(mm)+1
-    int32_t k1, k2, i1, i2;
-    CK(cudaMemcpy(&k1, n.WE_ny, 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&k2, n.WE_ny + n.d.nn - 1, 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&i1, n.SN_nx, 4, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&i2, n.SN_nx + n.d.mm - 1, 4, cudaMemcpyDeviceToHost));
-    k2 += 1;
-    i2 += 1;
     CK(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
     ++c->launches;
-    k_arrival<<<152, 256, 0, c->stream>>>(i1, i2, k1, k2, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st],
-                                          c->ground, cuke, kGrav, c->d_flag);
+    k_arrival<<<152, 256, 0, c->stream>>>(n.i1, n.i2, n.k1, n.k2, c->pitch, c->dep, c->srf[st], c->xu[st],
+                                          c->yv[st], c->ground, cuke, kGrav, c->d_flag, false);
     CK(cudaGetLastError());
     int f = 0;
     CK(cudaMemcpyAsync(&f, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1369,6 +1407,9 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
     if (f) *arrived = 1;
   }
   if (!*arrived) return 0;
+  // the asynchronous feed starts from the same arrival: the flag's low byte
+  // to 1 (the int was zeroed at nest_add and only ever goes to 1)
+  CK(cudaMemsetAsync(n.d_arr, 1, 1, c->stream));
   if (!w || !e || !s || !nn_out) return CLIFFS_ERR_ARG;
   const int mm = n.d.mm, nn = n.d.nn;
   double* buf = nullptr;
@@ -1378,7 +1419,8 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
   ++c->launches;
   k_feed_child<<<(threads + 127) / 128, 128, 0, c->stream>>>(
       mm, nn, n.d.W_nx, n.d.E_nx, n.d.S_ny, n.d.N_ny, n.d.W_cx, n.d.E_cx, n.d.S_cy, n.d.N_cy, n.WE_ny, n.WE_cy,
-      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn);
+      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn,
+      nullptr, nullptr);
   int r = CLIFFS_OK;
   if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && (cudaMemcpyAsync(w, dw, 3 * nn * 8, cudaMemcpyDeviceToHost, c->stream) ||
@@ -1389,6 +1431,177 @@ int cliffs_gpu_feed_child(cliffs_ctx* c, int32_t id, double cuke, int32_t* arriv
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   cudaFree(buf);
   return r ? r : 1;
+}
+
+// ---------------------------------------------------------------------------
+// Asynchronous outputs.
+
+namespace {
+
+// The next output slot, with a device buffer of at least `bytes`.  The
+// context's stream first waits until the slot's previous copy has left it.
+int out_slot(cliffs_ctx* c, size_t bytes, OutSlot** slot, int64_t* ticket) {
+  if (!c->cpy) {
+    CK(cudaStreamCreateWithFlags(&c->cpy, cudaStreamNonBlocking));
+    for (auto& o : c->outs) {
+      CK(cudaEventCreateWithFlags(&o.conv, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
+    }
+  }
+  OutSlot& o = c->outs[c->out_next % kOutSlots];
+  if (o.cap < bytes) {
+    if (o.used) CK(cudaEventSynchronize(o.done));
+    if (o.dbuf) cudaFree(o.dbuf);
+    o.dbuf = nullptr;
+    o.cap = 0;
+    if (cudaMalloc(&o.dbuf, bytes) != cudaSuccess) return CLIFFS_ERR_NOMEM;
+    o.cap = bytes;
+  } else if (o.used) {
+    CK(cudaStreamWaitEvent(c->stream, o.done, 0));
+  }
+  o.used = true;
+  *slot = &o;
+  *ticket = c->out_next++;
+  return CLIFFS_OK;
+}
+
+struct HostCopy {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
+// After the conversion kernels on the context's stream: the copies to the
+// host, on the copy stream behind them.
+int out_copy(cliffs_ctx* c, OutSlot& o, std::initializer_list<HostCopy> copies) {
+  CK(cudaEventRecord(o.conv, c->stream));
+  CK(cudaStreamWaitEvent(c->cpy, o.conv, 0));
+  for (const HostCopy& h : copies)
+    if (h.bytes) CK(cudaMemcpyAsync(h.dst, h.src, h.bytes, cudaMemcpyDeviceToHost, c->cpy));
+  CK(cudaEventRecord(o.done, c->cpy));
+  return CLIFFS_OK;
+}
+
+}  // namespace
+
+int cliffs_gpu_get_sea_state_async(cliffs_ctx* c, int32_t lonsub, int32_t latsub, float* h, float* u, float* v,
+                                   int64_t* ticket) {
+  if (!c || lonsub < 1 || latsub < 1 || !h || !u || !v || !ticket) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const int nxs = (c->nx - 1) / lonsub + 1, nys = (c->ny - 1) / latsub + 1;
+  const size_t n = (size_t)nxs * nys;
+  OutSlot* o = nullptr;
+  int64_t tk = 0;
+  int r = out_slot(c, 3 * n * sizeof(float), &o, &tk);
+  if (r) return r;
+  float* a = (float*)o->dbuf;
+  const int s = c->cur;
+  ++c->launches;
+  k_sea_state<<<grid2(nxs, nys), 128, 0, c->stream>>>(nxs, nys, c->pitch, lonsub, latsub, c->dep, c->srf[s],
+                                                      c->xu[s], c->yv[s], (float)c->ground, a, a + n, a + 2 * n);
+  CK(cudaGetLastError());
+  r = out_copy(c, *o, {{h, a, n * 4}, {u, a + n, n * 4}, {v, a + 2 * n, n * 4}});
+  if (r) return r;
+  *ticket = tk;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_get_gauges_async(cliffs_ctx* c, int32_t n, const int32_t* I, const int32_t* J, double* eta,
+                                double* u, double* v, int64_t* ticket) {
+  if (!c || n < 1 || !I || !J || !eta || !u || !v || !ticket) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  for (int k = 0; k < n; ++k)
+    if (I[k] < 1 || I[k] > c->nx || J[k] < 1 || J[k] > c->ny) return CLIFFS_ERR_ARG;
+  // the indices stay on the device; a new set goes up (synchronously) once
+  const bool same = n == c->g_n && std::equal(I, I + n, c->g_host.begin()) &&
+                    std::equal(J, J + n, c->g_host.begin() + n);
+  if (!same) {
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->g_cap < n) {
+      if (c->g_ij) cudaFree(c->g_ij);
+      c->g_ij = nullptr;
+      c->g_cap = 0;
+      if (dalloc(&c->g_ij, 2 * (size_t)n)) return CLIFFS_ERR_NOMEM;
+      c->g_cap = n;
+    }
+    c->g_host.assign(I, I + n);
+    c->g_host.insert(c->g_host.end(), J, J + n);
+    CK(cudaMemcpy(c->g_ij, c->g_host.data(), 2 * (size_t)n * 4, cudaMemcpyHostToDevice));
+    c->g_n = n;
+  }
+  OutSlot* o = nullptr;
+  int64_t tk = 0;
+  int r = out_slot(c, 3 * (size_t)n * sizeof(double), &o, &tk);
+  if (r) return r;
+  double* out = (double*)o->dbuf;
+  const int s = c->cur;
+  ++c->launches;
+  k_gauges<<<(n + 127) / 128, 128, 0, c->stream>>>(n, c->g_ij, c->g_ij + n, c->pitch, c->dep, c->srf[s], c->xu[s],
+                                                   c->yv[s], (float)c->ground, out);
+  CK(cudaGetLastError());
+  r = out_copy(c, *o, {{eta, out, (size_t)n * 8}, {u, out + n, (size_t)n * 8}, {v, out + 2 * n, (size_t)n * 8}});
+  if (r) return r;
+  *ticket = tk;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_feed_child_async(cliffs_ctx* c, int32_t id, double cuke, int32_t* arrived, double* w, double* e,
+                                double* s, double* nn_out, int64_t* ticket) {
+  if (!c || !arrived || !w || !e || !s || !nn_out || !ticket || id < 0 || id >= (int32_t)c->nests.size())
+    return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  const Nest& n = c->nests[id];
+  const int mm = n.d.mm, nn = n.d.nn;
+  const size_t rec = 6 * (size_t)(mm + nn);
+  OutSlot* o = nullptr;
+  int64_t tk = 0;
+  int r = out_slot(c, rec * sizeof(double) + sizeof(double), &o, &tk);
+  if (r) return r;
+  double* buf = (double*)o->dbuf;
+  double *dw = buf, *de = buf + 3 * (size_t)nn, *ds = buf + 6 * (size_t)nn, *dn = ds + 3 * (size_t)mm;
+  int* gate = (int*)(buf + rec);
+  const int st = c->cur;
+  c->launches += 2;
+  // the arrival test leaves at once when an earlier call found the wave
+  k_arrival<<<152, 256, 0, c->stream>>>(n.i1, n.i2, n.k1, n.k2, c->pitch, c->dep, c->srf[st], c->xu[st],
+                                        c->yv[st], c->ground, cuke, kGrav, n.d_arr, true);
+  CK(cudaGetLastError());
+  const int threads = 2 * (mm + nn);
+  k_feed_child<<<(threads + 127) / 128, 128, 0, c->stream>>>(
+      mm, nn, n.d.W_nx, n.d.E_nx, n.d.S_ny, n.d.N_ny, n.d.W_cx, n.d.E_cx, n.d.S_cy, n.d.N_cy, n.WE_ny, n.WE_cy,
+      n.SN_nx, n.SN_cx, c->pitch, c->dep, c->srf[st], c->xu[st], c->yv[st], c->ground, kGrav, dw, de, ds, dn,
+      n.d_arr, gate);
+  CK(cudaGetLastError());
+  r = out_copy(c, *o,
+               {{w, dw, 3 * (size_t)nn * 8}, {e, de, 3 * (size_t)nn * 8}, {s, ds, 3 * (size_t)mm * 8},
+                {nn_out, dn, 3 * (size_t)mm * 8}, {arrived, gate, sizeof(int32_t)}});
+  if (r) return r;
+  *ticket = tk;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_output_wait(cliffs_ctx* c, int64_t ticket) {
+  if (!c || ticket < 0 || ticket >= c->out_next) return CLIFFS_ERR_ARG;
+  // a later output of the same slot follows this one on the copy stream
+  CK(cudaEventSynchronize(c->outs[ticket % kOutSlots].done));
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_output_done(cliffs_ctx* c, int64_t ticket, int32_t* done) {
+  if (!c || !done || ticket < 0 || ticket >= c->out_next) return CLIFFS_ERR_ARG;
+  const cudaError_t q = cudaEventQuery(c->outs[ticket % kOutSlots].done);
+  if (q != cudaSuccess && q != cudaErrorNotReady) return CLIFFS_ERR_CUDA;
+  *done = q == cudaSuccess ? 1 : 0;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_host_alloc(int64_t bytes, void** p) {
+  if (!p || bytes < 1) return CLIFFS_ERR_ARG;
+  return cudaHostAlloc(p, (size_t)bytes, cudaHostAllocDefault) == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_NOMEM;
+}
+
+void cliffs_gpu_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 int cliffs_gpu_status(cliffs_ctx* c, uint32_t* flags) {

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <deque>
 #include <fstream>
 #include <memory>
 #include <sstream>
@@ -401,51 +402,122 @@ int run(const Case& c, const std::string& casename, const std::string& outprefix
   Outputs o = open_outputs(c, casename, outprefix, log);
   double t = c.t0;
   const int ng = c.p.ngages;
-  std::vector<float> hs((size_t)o.nxsub * o.nysub), us(hs.size()), vs(hs.size());
-  std::vector<double> ge(ng), gu(ng), gv(ng);
   std::vector<float> me(cells), mv(cells);
-  auto sea = [&]() {
-    check(cliffs_gpu_get_sea_state(ctx, c.p.lonsub, c.p.latsub, hs.data(), us.data(), vs.data()), "sea_state");
-    write_sea(o, hs.data(), us.data(), vs.data(), t, log);
-  };
-  auto gages = [&]() {
-    check(cliffs_gpu_get_gauges(ctx, ng, c.p.gage_i.data(), c.p.gage_j.data(), ge.data(), gu.data(), gv.data()),
-          "gauges");
-    write_gage_record(*o.gages, ng, ge.data(), gu.data(), gv.data(), t);
-  };
   auto maxwave = [&]() {
     check(cliffs_gpu_get_maxwave(ctx, me.data(), mv.data()), "maxwave");
     write_max(o, me.data(), mv.data(), cells);
   };
-  std::vector<int32_t> arrived(c.nests.size(), 0);
-  std::vector<std::vector<double>> fw(c.nests.size()), fe(c.nests.size()), fs(c.nests.size()), fn(c.nests.size());
-  for (size_t k = 0; k < c.nests.size(); ++k) {
-    fw[k].resize(3 * (size_t)c.nests[k].nn);
-    fe[k].resize(3 * (size_t)c.nests[k].nn);
-    fs[k].resize(3 * (size_t)c.nests[k].mm);
-    fn[k].resize(3 * (size_t)c.nests[k].mm);
+  // Screenshots, gauge records and child feed records are asynchronous
+  // outputs: queued on the device in order with the steps, copied to pinned
+  // host slots behind them, and written to their files once the copy has
+  // landed.  The loop runs up to kDepth records of a kind ahead of the files;
+  // a kind whose slots are all in flight writes its oldest record first.
+  constexpr int kDepth = 3;
+  enum Kind { kSea = 0, kGage = 1, kFeed = 2 };
+  struct Pending {
+    int64_t ticket;
+    double t;
+    int kind, child, slot;
+  };
+  std::deque<Pending> queue;
+  std::vector<void*> pinned;
+  auto host = [&](size_t bytes) {
+    void* p = nullptr;
+    check(cliffs_gpu_host_alloc((int64_t)std::max<size_t>(bytes, 8), &p), "host_alloc");
+    pinned.push_back(p);
+    return p;
+  };
+  struct PinnedGuard {
+    std::vector<void*>& v;
+    ~PinnedGuard() {
+      for (void* p : v) cliffs_gpu_host_free(p);
+    }
+  } pinned_guard{pinned};
+  const size_t nsub = (size_t)o.nxsub * o.nysub;
+  float* sea_buf = o.sea.empty() ? nullptr : (float*)host(kDepth * 3 * nsub * sizeof(float));
+  double* gage_buf = ng >= 1 ? (double*)host(kDepth * 3 * (size_t)ng * sizeof(double)) : nullptr;
+  std::vector<double*> feed_buf;
+  std::vector<int32_t*> feed_arr;
+  for (const auto& n : c.nests) {
+    feed_buf.push_back((double*)host(kDepth * 6 * (size_t)(n.mm + n.nn) * sizeof(double)));
+    feed_arr.push_back((int32_t*)host(kDepth * sizeof(int32_t)));
   }
+  std::vector<int> in_flight(2 + c.nests.size(), 0), next_slot(2 + c.nests.size(), 0);
+  std::vector<int32_t> arrived(c.nests.size(), 0);
+  auto write_front = [&]() {
+    const Pending p = queue.front();
+    queue.pop_front();
+    check(cliffs_gpu_output_wait(ctx, p.ticket), "output_wait");
+    if (p.kind == kSea) {
+      const float* b = sea_buf + (size_t)p.slot * 3 * nsub;
+      write_sea(o, b, b + nsub, b + 2 * nsub, p.t, log);
+    } else if (p.kind == kGage) {
+      const double* b = gage_buf + (size_t)p.slot * 3 * ng;
+      write_gage_record(*o.gages, ng, b, b + ng, b + 2 * ng, p.t);
+    } else {
+      const int k = p.child, mm = c.nests[k].mm, nn = c.nests[k].nn;
+      if (feed_arr[k][p.slot]) {  // feed_children_grid.f: a record once the wave is in the footprint
+        if (!arrived[k]) {
+          arrived[k] = 1;
+          std::ostringstream m;
+          m << "reached child grid " << k + 1 << " at " << p.t << "sec";
+          log.line(m.str());
+        }
+        const double* b = feed_buf[k] + (size_t)p.slot * 6 * (mm + nn);
+        write_feed(o.feeds[k], b, b + 3 * (size_t)nn, b + 6 * (size_t)nn, b + 6 * (size_t)nn + 3 * (size_t)mm,
+                   mm, nn, p.t);
+      }
+    }
+    --in_flight[p.kind == kFeed ? 2 + p.child : p.kind];
+  };
+  // a free slot of kind index q: the oldest records are written until one is
+  auto slot_for = [&](int q) {
+    while (in_flight[q] >= kDepth) write_front();
+    ++in_flight[q];
+    const int s = next_slot[q];
+    next_slot[q] = (s + 1) % kDepth;
+    return s;
+  };
+  auto sea = [&]() {
+    const int s = slot_for(kSea);
+    float* b = sea_buf + (size_t)s * 3 * nsub;
+    int64_t tk = 0;
+    check(cliffs_gpu_get_sea_state_async(ctx, c.p.lonsub, c.p.latsub, b, b + nsub, b + 2 * nsub, &tk),
+          "sea_state");
+    queue.push_back({tk, t, kSea, 0, s});
+  };
+  auto gages = [&]() {
+    const int s = slot_for(kGage);
+    double* b = gage_buf + (size_t)s * 3 * ng;
+    int64_t tk = 0;
+    check(cliffs_gpu_get_gauges_async(ctx, ng, c.p.gage_i.data(), c.p.gage_j.data(), b, b + ng, b + 2 * ng, &tk),
+          "gauges");
+    queue.push_back({tk, t, kGage, 0, s});
+  };
   auto feed = [&]() {  // feed_children_grid.f
     for (size_t k = 0; k < c.nests.size(); ++k) {
-      const int32_t was = arrived[k];
-      const int r = cliffs_gpu_feed_child(ctx, nest_id[k], c.p.cuke, &arrived[k], fw[k].data(), fe[k].data(),
-                                          fs[k].data(), fn[k].data());
-      check(r, "feed_child");
-      if (arrived[k] && !was) {
-        std::ostringstream m;
-        m << "reached child grid " << k + 1 << " at " << t << "sec";
-        log.line(m.str());
-      }
-      if (r == 1)
-        write_feed(o.feeds[k], fw[k].data(), fe[k].data(), fs[k].data(), fn[k].data(), c.nests[k].mm,
-                   c.nests[k].nn, t);
+      const int s = slot_for(2 + (int)k);
+      const int mm = c.nests[k].mm, nn = c.nests[k].nn;
+      double* b = feed_buf[k] + (size_t)s * 6 * (mm + nn);
+      int64_t tk = 0;
+      check(cliffs_gpu_feed_child_async(ctx, nest_id[k], c.p.cuke, feed_arr[k] + s, b, b + 3 * (size_t)nn,
+                                        b + 6 * (size_t)nn, b + 6 * (size_t)nn + 3 * (size_t)mm, &tk),
+            "feed_child");
+      queue.push_back({tk, t, kFeed, (int)k, s});
     }
+  };
+  auto status = [&](int istep) {
+    uint32_t flags = 0;
+    const int st = cliffs_gpu_status(ctx, &flags);
+    if (st == CLIFFS_ERR_NAN || (flags & CLIFFS_ST_NAN))
+      throw std::runtime_error("non-finite state by step " + std::to_string(istep));
+    check(st, "status");
   };
   // cliffs_main.f:255-297: the initial screenshot, gauge record and child feed
   if (!o.sea.empty()) sea();
   if (ng >= 1) gages();
   if (!c.nests.empty()) feed();
-  // cliffs_main.f:300-378: advance to the next output event, then write
+  // cliffs_main.f:300-378: advance to the next output event, then output
   const int total = c.p.steps_total;
   auto next_event = [&](int istep) {
     int nxt = total;
@@ -470,16 +542,16 @@ int run(const Case& c, const std::string& casename, const std::string& outprefix
       log.line("bndr feed ended at step " + std::to_string(istep + 1));
       break;
     }
-    uint32_t flags = 0;
-    const int st = cliffs_gpu_status(ctx, &flags);
-    if (st == CLIFFS_ERR_NAN || (flags & CLIFFS_ST_NAN))
-      throw std::runtime_error("non-finite state by step " + std::to_string(istep));
-    check(st, "status");
     if (!c.nests.empty() && istep % c.p.bndout == 0) feed();
     if (!o.sea.empty() && istep % c.p.seaout == 0) sea();
     if (ng >= 1 && istep % c.p.gout == 0) gages();
-    if (istep % c.p.maxout == 0) maxwave();
+    if (istep % c.p.maxout == 0) {  // synchronises: the status word is read here
+      status(istep);
+      maxwave();
+    }
   }
+  while (!queue.empty()) write_front();
+  status(istep);
   maxwave();  // cliffs_main.f:380
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   std::ostringstream m;

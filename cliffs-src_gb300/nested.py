@@ -79,7 +79,7 @@ def nest_tables(x, y, xn, yn):
 
 def _records(recs, times):
     """Feed records in set_feed's layout: tinput (nt), west/east (nt, 3, ny),
-    south/north (nt, 3, nx)."""
+    south/north (nt, 3, nx), from a list of (w, e, s, n) records."""
     return (np.asarray(times, np.float64), np.stack([r[0] for r in recs]), np.stack([r[1] for r in recs]),
             np.stack([r[2] for r in recs]), np.stack([r[3] for r in recs]))
 
@@ -88,7 +88,10 @@ def run_level(case, source, t_end, feed=None, child=None, cuke=0.001, bndout=3, 
     """One level: the grid at rest, the source as a bottom deformation, then
     steps to t_end in chunks of bndout steps.  feed: the records of this level
     (from its parent), child: the next level's case, whose records this level
-    produces.  Gauge records every gout steps.  Returns (result, child_feed)."""
+    produces.  Gauge records every gout steps.  Feed and gauge records are
+    asynchronous outputs into pinned host memory, so the loop never waits for
+    the device; they are collected at the end.  Returns (result, child_feed)."""
+    cg = pkg.cliffs_gpu
     g = pkg.GpuGrid.from_case(case)
     t0 = 0.0
     if feed is not None:
@@ -104,49 +107,67 @@ def run_level(case, source, t_end, feed=None, child=None, cuke=0.001, bndout=3, 
         g.t.value = t0
     g.add_source(case["xcrd"], case["ycrd"], **source)
     nest = g.nest_add(nest_tables(case["xcrd"], case["ycrd"], child["xcrd"], child["ycrd"])) if child else None
-    I, J = case["gauges"]
-    gt, ge, gu, gv = [], [], [], []
-    recs, rtimes = [], []
-    arrived = False
     total = max(0, int(np.floor((t_end - t0) / case["dt"] + 1e-9)))
+    step = bndout if nest is not None else gout
+    if feed is None and step >= 2:
+        g.set_graph_steps(min(step, 16))  # plain steps between outputs replay from graphs
+    I, J = case["gauges"]
+    ng = len(I)
+    n_g = total // gout + 1
+    gbuf = cg.pinned((n_g, 3, ng))
+    gt = []
+    if nest is not None:
+        mm, nn = nest[1]
+        n_f = total // bndout + 1
+        fbuf = {k: cg.pinned((n_f, 3, m)) for k, m in (("w", nn), ("e", nn), ("s", mm), ("n", mm))}
+        farr = cg.pinned((n_f,), np.int32)
+        ft = []
+    last = -1
     g.sync()
     w0 = time.perf_counter()
     done = 0
 
     def outputs():
-        nonlocal arrived
+        nonlocal last
         if nest is not None and done % bndout == 0:
-            arrived, rec = g.feed_child(nest, cuke, arrived)
-            if rec is not None:
-                recs.append(rec)
-                rtimes.append(g.time)
+            k = len(ft)
+            last = g.feed_child_async(nest, cuke, (farr[k:k + 1], fbuf["w"][k], fbuf["e"][k], fbuf["s"][k],
+                                                   fbuf["n"][k]))
+            ft.append(g.time)
         if done % gout == 0:
-            e_, u_, v_ = g.gauges(I, J)
+            k = len(gt)
+            last = g.gauges_async(I, J, (gbuf[k, 0], gbuf[k, 1], gbuf[k, 2]))
             gt.append(g.time)
-            ge.append(e_)
-            gu.append(u_)
-            gv.append(v_)
 
     outputs()
     ended = False
     while done < total and not ended:
-        k = min(total - done, bndout - done % bndout if nest is not None else gout - done % gout,
-                gout - done % gout)
+        k = min(total - done, step - done % step, gout - done % gout)
         got, ended = g.step(k)
         done += got
         if got == k:
             outputs()
-    me, mv = g.maxwave()
-    g.sync()
+    me, mv = g.maxwave()  # synchronises: every output above is done after it
+    if last >= 0:
+        g.wait(last)
     wall = time.perf_counter() - w0
     r, flags = g.status()
+    child_feed = None
+    if nest is not None:
+        got_rec = np.flatnonzero(farr[:len(ft)] == 1)
+        if len(got_rec):
+            child_feed = (np.asarray(ft)[got_rec], fbuf["w"][got_rec].copy(), fbuf["e"][got_rec].copy(),
+                          fbuf["s"][got_rec].copy(), fbuf["n"][got_rec].copy())
+    k = len(gt)
     res = dict(name=case["name"], shape=list(case["dep"].shape), dt=case["dt"], t0=t0, t_end=g.time, steps=done,
                feed_ended=bool(ended), wall_s=wall, cell_updates_per_s=case["dep"].size * done / max(wall, 1e-12),
-               status=r, flags=flags, launches=g.launches(), records_out=len(recs),
+               status=r, flags=flags, launches=g.launches(),
+               records_out=0 if child_feed is None else len(child_feed[0]),
                land_wetted=int(((case["dep"] < 0) & (case["dep"] > -900.0) & (me > -1e30)).sum()),
-               maxe=me, maxv=mv, gauges=dict(t=np.array(gt), eta=np.array(ge), u=np.array(gu), v=np.array(gv)))
+               maxe=me, maxv=mv, gauges=dict(t=np.array(gt), eta=gbuf[:k, 0].copy(), u=gbuf[:k, 1].copy(),
+                                             v=gbuf[:k, 2].copy()))
     g.close()
-    return res, (_records(recs, rtimes) if recs else None)
+    return res, child_feed
 
 
 def run_chain(levels, source, hours, cuke=0.001, bndout=3, gout=10):

@@ -199,11 +199,19 @@ def solve(params, base, steps, chunk=512):
 class Norm:
     """Inputs to [-1, 1]; gauge maxima as standardised log(max + 0.01),
     weighted x4 so that the 64 gauges weigh as much as the 1024 map cells;
-    map cells standardised."""
+    map cells standardised.
+
+    per_amp: targets per metre of source amplitude (max / amp, window / amp).
+    Offshore the response is close to linear in the amplitude, so the network
+    then learns the shape of the response rather than its scale."""
 
     GW = 4.0
 
-    def __init__(self, G, P):
+    def __init__(self, G, P, params=None, per_amp=False):
+        self.per_amp = per_amp
+        if per_amp:
+            a = params[:, 2:3]
+            G, P = G / a, P / a
         lg = np.log(G + 0.01)
         self.gm, self.gs = lg.mean(0), lg.std(0) + 1e-6
         self.pm, self.ps = P.mean(0), P.std(0) + 1e-3
@@ -216,12 +224,18 @@ class Norm:
         z[:, 2] = 2.0 * (la - np.log(LO[2])) / (np.log(HI[2]) - np.log(LO[2])) - 1.0
         return np.hstack([z[:, :5], np.cos(params[:, 5:6]), np.sin(params[:, 5:6]), z[:, 6:]])
 
-    def t(self, G, P):
+    def t(self, G, P, params=None):
+        if self.per_amp:
+            a = params[:, 2:3]
+            G, P = G / a, P / a
         return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, (P - self.pm) / self.ps])
 
-    def back(self, Y):
+    def back(self, Y, params=None):
         g = np.exp(Y[:, :NGAUGES] / self.GW * self.gs + self.gm) - 0.01
         p = Y[:, NGAUGES:] * self.ps + self.pm
+        if self.per_amp:
+            a = params[:, 2:3]
+            g, p = g * a, p * a
         return np.maximum(g, 0.0), np.maximum(p, 0.0)
 
 
@@ -249,8 +263,8 @@ class Ensemble:
         batch = max(16, min(batch, len(X) // 16 * 16))
         return [net.train(X, T, epochs, batch, lr, seed + 7 * k, weight_decay) for k, net in enumerate(self.nets)]
 
-    def predict(self, X, norm):
-        outs = [norm.back(net.predict(X)) for net in self.nets]
+    def predict(self, X, norm, params=None):
+        outs = [norm.back(net.predict(X), params) for net in self.nets]
         G = np.stack([o[0] for o in outs])  # (members, n, 64)
         P = np.stack([o[1] for o in outs])
         return G.mean(0), P.mean(0), G
@@ -291,10 +305,9 @@ def calibrate_gate(sp, rel, mask, target):
     return float(best)
 
 
-def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256):
-    """Data from the batched solver, the ensemble trained on n_train - n_val
-    runs, its gate calibrated on the n_val others, judged on n_test held-out
-    runs against the solver."""
+def make_data(n_train=4096, n_test=256, steps=2000, seed=0):
+    """The solver runs of the study: n_train training runs (the first n_val of
+    them calibrate the gate) and n_test held-out runs."""
     base = base_grid(seed)
     Xall = sample_params(n_train, seed + 1)
     Xte = sample_params(n_test, seed + 2)
@@ -302,20 +315,32 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0,
     Gall, Pall, _, t_data, bad_tr = solve(Xall, base, steps)
     t_gen = time.perf_counter() - t0
     Gte, Pte, Fte, t_test_solve, bad_te = solve(Xte, base, steps)
+    return dict(base=base, steps=steps, Xall=Xall, Gall=Gall, Pall=Pall, Xte=Xte, Gte=Gte, Pte=Pte, Fte=Fte,
+                t_gen=t_gen, t_data=t_data, t_test_solve=t_test_solve, bad=int(bad_tr + bad_te))
+
+
+def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=False, width=512, depth=3,
+                  members=4, single=None):
+    """Train the ensemble on the training runs, calibrate its gate on the
+    validation split, judge it on the held-out runs against the solver.
+    single: seconds of one one-at-a-time solve (measured here when None)."""
+    base, steps = D["base"], D["steps"]
+    Xall, Gall, Pall, Xte, Gte, Fte = D["Xall"], D["Gall"], D["Pall"], D["Xte"], D["Gte"], D["Fte"]
+    n_test = len(Xte)
     Xtr, Gtr, Ptr = Xall[n_val:], Gall[n_val:], Pall[n_val:]
     Xva, Gva = Xall[:n_val], Gall[:n_val]
-    norm = Norm(Gtr, Ptr)
-    ens = Ensemble(seed=seed)
+    norm = Norm(Gtr, Ptr, Xtr, per_amp=per_amp)
+    ens = Ensemble(members=members, width=width, depth=depth, seed=seed)
     t0 = time.perf_counter()
-    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Ptr), epochs)
+    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Ptr, Xtr), epochs)
     t_train = time.perf_counter() - t0
     # the gate, from the validation split
-    Gv, _, Gvm = ens.predict(norm.x(Xva), norm)
+    Gv, _, Gvm = ens.predict(norm.x(Xva), norm, Xva)
     rel_v, mask_v, _ = gauge_errors(Gv, Gva)
     thr = calibrate_gate(spread(Gvm), rel_v, mask_v, target)
     # the surrogate path on the test split: ensemble prediction, then the gate
     t0 = time.perf_counter()
-    Gp, Pp, Gm = ens.predict(norm.x(Xte), norm)
+    Gp, Pp, Gm = ens.predict(norm.x(Xte), norm, Xte)
     sp = spread(Gm)
     accept = sp <= thr
     t_pred = time.perf_counter() - t0
@@ -323,20 +348,22 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0,
     rel_acc = rel[accept[:, None] & mask]
     win_err = np.abs(upsample(Pp) - Fte)  # m, on the full 128 x 128 window
     # one-at-a-time solves of a few test scenarios: the method without the surrogate
-    n_single = min(16, n_test)
-    L = base["xcrd"][-1]
-    t_single = 0.0
-    for p in Xte[:n_single]:
-        g = pkg.GpuGrid.from_case(dict(base, H0=base["dep"]))
-        g.add_source(base["xcrd"], base["ycrd"], **source_of(p, L))
-        g.sync()
-        t1 = time.perf_counter()
-        g.step(steps)
-        g.maxwave()
-        t_single += time.perf_counter() - t1
-        g.close()
-    per_single = t_single / n_single
-    per_batch = t_test_solve / n_test
+    if single is None:
+        n_single = min(16, n_test)
+        L = base["xcrd"][-1]
+        t_single = 0.0
+        for p in Xte[:n_single]:
+            g = pkg.GpuGrid.from_case(dict(base, H0=base["dep"]))
+            g.add_source(base["xcrd"], base["ycrd"], **source_of(p, L))
+            g.sync()
+            t1 = time.perf_counter()
+            g.step(steps)
+            g.maxwave()
+            t_single += time.perf_counter() - t1
+            g.close()
+        single = t_single / n_single
+    per_single = single
+    per_batch = D["t_test_solve"] / n_test
     # the rejected scenarios go to the batched solver, as one batch, timed
     # whole (grid set-up, sources, steps, max-wave download)
     rej = np.flatnonzero(~accept)
@@ -349,8 +376,8 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0,
         assert np.array_equal(Gfb, Gte[rej])  # batching does not change a run
     t_gated = t_pred + t_fb
     res = dict(train=len(Xtr), validation=n_val, test=n_test, steps=steps, epochs=epochs, target=target,
-               nonfinite_runs=int(bad_tr + bad_te),
-               data_seconds=round(t_gen, 2), solver_seconds_train=round(t_data, 2),
+               per_amp=per_amp, width=width, depth=depth, members=members, nonfinite_runs=D["bad"],
+               data_seconds=round(D["t_gen"], 2), solver_seconds_train=round(D["t_data"], 2),
                train_seconds=round(t_train, 2),
                final_loss=[round(float(l[-1]), 5) for l in losses],
                first_loss=[round(float(l[0]), 5) for l in losses],
@@ -373,6 +400,14 @@ def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0,
     return res
 
 
+def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=False):
+    """Data from the batched solver, the ensemble trained on n_train - n_val
+    runs, its gate calibrated on the n_val others, judged on n_test held-out
+    runs against the solver."""
+    D = make_data(n_train, n_test, steps, seed)
+    return fit_and_judge(D, epochs=epochs, target=target, seed=seed, n_val=n_val, per_amp=per_amp)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=4096)
@@ -381,9 +416,10 @@ def main():
     ap.add_argument("--epochs", type=int, default=1500)
     ap.add_argument("--target", type=float, default=0.045)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--per-amp", action="store_true")
     a = ap.parse_args()
     pkg.build.build()
-    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed)), flush=True)
+    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=a.per_amp)), flush=True)
 
 
 if __name__ == "__main__":

@@ -198,6 +198,40 @@ int cliffs_gpu_feed_child(cliffs_ctx *ctx, int32_t id, double cuke,
                           int32_t *arrived, double *uvq_w, double *uvq_e,
                           double *uvq_s, double *uvq_n);
 
+/* Asynchronous outputs (no reference counterpart: the reference writes each
+ * record before it steps on).
+ * - The conversion runs on the context's stream, in order with the steps.
+ * - The copy to the caller's host buffers runs on a second stream behind it,
+ *   overlapping the steps that follow.  No call synchronises the device.
+ * - The buffers hold the record once cliffs_gpu_output_wait(ticket) has
+ *   returned, or cliffs_gpu_output_done reports it.  They must stay allocated
+ *   until then, and be pinned (cliffs_gpu_host_alloc) for the copy to
+ *   overlap.
+ * - Up to 8 outputs are in flight per context. A ninth waits on the device,
+ *   not the host, for the copy of the first.
+ * Per call:
+ * - sea_state: as cliffs_gpu_get_sea_state.
+ * - gauges: as cliffs_gpu_get_gauges, n >= 1. The indices stay on the device
+ *   until a call passes others.
+ * - feed_child: as cliffs_gpu_feed_child, with the arrival flag kept on the
+ *   device. *arrived gets 1 when this call produced a record (the wave has
+ *   reached the child), else 0 and the record buffers hold nothing. */
+int cliffs_gpu_get_sea_state_async(cliffs_ctx *ctx, int32_t lonsub,
+                                   int32_t latsub, float *hsub, float *usub,
+                                   float *vsub, int64_t *ticket);
+int cliffs_gpu_get_gauges_async(cliffs_ctx *ctx, int32_t n, const int32_t *I,
+                                const int32_t *J, double *eta, double *u,
+                                double *v, int64_t *ticket);
+int cliffs_gpu_feed_child_async(cliffs_ctx *ctx, int32_t id, double cuke,
+                                int32_t *arrived, double *uvq_w,
+                                double *uvq_e, double *uvq_s, double *uvq_n,
+                                int64_t *ticket);
+int cliffs_gpu_output_wait(cliffs_ctx *ctx, int64_t ticket);
+int cliffs_gpu_output_done(cliffs_ctx *ctx, int64_t ticket, int32_t *done);
+/* Pinned host memory for the asynchronous outputs. */
+int cliffs_gpu_host_alloc(int64_t bytes, void **p);
+void cliffs_gpu_host_free(void *p);
+
 /* Sticky status bits (CLIFFS_ST_*) since the last call; synchronises.
  * Returns CLIFFS_ERR_NAN or CLIFFS_ERR_TIMEOUT when the matching bit is set. */
 int cliffs_gpu_status(cliffs_ctx *ctx, uint32_t *flags);
