@@ -207,7 +207,7 @@ class Norm:
 
     GW = 4.0
 
-    def __init__(self, G, P, params=None, per_amp=False):
+    def __init__(self, G, P, params=None, per_amp=True):
         self.per_amp = per_amp
         if per_amp:
             a = params[:, 2:3]
@@ -319,7 +319,7 @@ def make_data(n_train=4096, n_test=256, steps=2000, seed=0):
                 t_gen=t_gen, t_data=t_data, t_test_solve=t_test_solve, bad=int(bad_tr + bad_te))
 
 
-def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=False, width=512, depth=3,
+def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True, width=512, depth=3,
                   members=4, single=None):
     """Train the ensemble on the training runs, calibrate its gate on the
     validation split, judge it on the held-out runs against the solver.
@@ -400,7 +400,7 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=False
     return res
 
 
-def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=False):
+def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True):
     """Data from the batched solver, the ensemble trained on n_train - n_val
     runs, its gate calibrated on the n_val others, judged on n_test held-out
     runs against the solver."""
@@ -416,10 +416,11 @@ def main():
     ap.add_argument("--epochs", type=int, default=1500)
     ap.add_argument("--target", type=float, default=0.045)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--per-amp", action="store_true")
+    ap.add_argument("--no-per-amp", action="store_true", help="targets in metres, not per metre of amplitude")
     a = ap.parse_args()
     pkg.build.build()
-    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=a.per_amp)), flush=True)
+    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=not a.no_per_amp)),
+          flush=True)
 
 
 if __name__ == "__main__":
