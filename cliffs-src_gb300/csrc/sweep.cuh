@@ -205,6 +205,56 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   if (!isfinite(r.s + xo + yo)) atomicOr(A.status, ST_NAN);
 }
 
+// The cells of a thread that the plain update does not cover (bits of
+// `rest`, cells i0+r of line L): line ends, shorelines, dry cells,
+// supercritical flow.  d, e (eta), u (normal), v (tangential), H, c are the
+// window at positions i0-1 .. i0+4; wet as computed for the plain update
+// (without the line's range, applied here).  A line end next to a wet cell
+// takes the open or forced edge update in place; a dry cell at the zero state
+// between dry neighbours stays as it is; every other cell is returned for the
+// general path (bit r).
+__device__ __forceinline__ unsigned rest_cells(const SweepArgs& A, int L, int i0, unsigned rest, const float (&d)[6],
+                                               const float (&e)[6], const float (&u)[6], const float (&v)[6],
+                                               const float (&H)[6], const float (&c)[6], const bool (&wet_in)[6],
+                                               float ialpha, float (&os)[kCellsPerThread],
+                                               float (&ou)[kCellsPerThread], float (&ov)[kCellsPerThread]) {
+  const int n = A.n;
+  const Phys<float>& p = A.ph;
+  unsigned need = 0u;
+  bool wet[6];
+#pragma unroll
+  for (int w = 0; w < 6; ++w) wet[w] = wet_in[w] && i0 - 1 + w >= 1 && i0 - 1 + w <= n;  // positions 1..n only
+#pragma unroll
+  for (int r = 0; r < kCellsPerThread; ++r) {
+    if (!((rest >> r) & 1u)) continue;
+    const int k = i0 + r;
+    const int w = r + 1;
+    if ((r == 0 && k == 1 && wet[w] && wet[w + 1]) ||
+        (r == kCellsPerThread - 1 && k == n && wet[w - 1] && wet[w])) {
+      // line end next to a wet cell: no flooding reaches it; the open or
+      // forced edge update (cliffs.f:287-329), or the cell as it is.  Only
+      // the thread's first and last cell can take it here (one copy each in
+      // the unrolled loop); other line ends go to the general path.
+      const EdgeVals<float> ev = edge_vals(A, L, k == 1 ? 0 : 1);
+      if (ev.eta + d[w] > p.ground) {
+        const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
+        float cn;
+        if (k == 1) {
+          const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
+          edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], os[r]);
+        } else {
+          const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
+          edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r], os[r]);
+        }
+      }
+    } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
+      need |= 1u << r;
+    }
+    // else: dry, zero state: unchanged whether or not the line holds water
+  }
+  return need;
+}
+
 template <int DIR, bool LOCAL, bool COH, bool TAIL = true>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
@@ -383,39 +433,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
       ov[r] = plain ? o.v : ov[r];
       if (!plain && k <= n) rest |= 1u << r;
     }
-    if (rest) {  // line ends, shorelines, dry cells, supercritical flow
-#pragma unroll
-      for (int w = 0; w < 6; ++w) wet[w] = wet[w] && i0 - 1 + w >= 1 && i0 - 1 + w <= n;  // positions 1..n only
-#pragma unroll
-      for (int r = 0; r < kCellsPerThread; ++r) {
-        if (!((rest >> r) & 1u)) continue;
-        const int k = i0 + r;
-        const int w = r + 1;
-        if ((r == 0 && k == 1 && wet[w] && wet[w + 1]) ||
-            (r == kCellsPerThread - 1 && k == n && wet[w - 1] && wet[w])) {
-          // line end next to a wet cell: no flooding reaches it; the open or
-          // forced edge update (cliffs.f:287-329), or the cell as it is.
-          // Only the thread's first and last cell can take it here (one copy
-          // each in the unrolled loop); other line ends go to the general path.
-          const EdgeVals<float> ev = edge_vals(A, L, k == 1 ? 0 : 1);
-          if (ev.eta + d[w] > p.ground) {
-            const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
-            float cn;
-            if (k == 1) {
-              const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
-              edge_left(j, b, ev, A.inv_dx1 * ialpha, A.scl ? A.scl[0] : 0.f, p, cn, ou[r], ov[r], os[r]);
-            } else {
-              const CellState<float> a{u[w - 1], c[w - 1], e[w - 1], d[w - 1], v[w - 1], H[w - 1]};
-              edge_right(a, j, ev, A.inv_dxn1 * ialpha, A.scl ? A.scl[n - 1] : 0.f, p, cn, ou[r], ov[r],
-                         os[r]);
-            }
-          }
-        } else if (!(!wet[w] && !wet[w - 1] && !wet[w + 1] && H[w] == 0.f && u[w] == 0.f && v[w] == 0.f)) {
-          need |= 1u << r;
-        }
-        // else: dry, zero state: unchanged whether or not the line holds water
-      }
-    }
+    if (rest) need = rest_cells(A, L, i0, rest, d, e, u, v, H, c, wet, ialpha, os, ou, ov);
   }
   if (LOCAL) {
 #pragma unroll
