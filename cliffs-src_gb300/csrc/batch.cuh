@@ -62,7 +62,7 @@ __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int s
     __syncthreads();  // the previous tile is done with sA and its shared list
     if (threadIdx.x == 0) sA = B.args[2 * k + DIR];
     __syncthreads();
-    sweep_tile<DIR, true, COH>(sA, local % g, local / g);
+    sweep_tile<DIR, true, COH, true>(sA, local % g, local / g);
   }
 }
 
