@@ -1,11 +1,11 @@
 """A nested chain on the GPU (nested.run_chain) against the same chain replayed
 on the oracle: a spherical master and two children at refinement 3, each fed
 by its parent's edge records (feed_children_grid.f, get_boundary_feed.f),
-runup on every level.
+runup on the innermost level and walls on the others.
 
 The chain is the benchmark's nested configuration at a tenth of the size
-(nested.SMALL: a 432 x 216 master at 5/6 degree, children of 60^2 and 90^2,
-a +3/-1 m dipole source 2000 km offshore), 3 hours of model time.  Every
+(nested.SMALL: a 432 x 216 master at 1/12 degree, children of 60^2 and 90^2,
+a +3/-1 m dipole source 400 km offshore), 3 hours of model time.  Every
 level is compared on its own: the start time and record count, the gauge
 series, and the max-wave fields.  Tolerances are those of test_gpu_parity.py:
 elevation 1e-4 of the source amplitude, velocities 2e-4 m/s.
