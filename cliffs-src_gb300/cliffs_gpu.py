@@ -69,6 +69,7 @@ class BatchPlan(ctypes.Structure):
 
 PERSISTENT, GRAPH = 0, 1
 TILED, STAGED = 0, 1  # cliffs_gpu_set_sweep_kernel
+LATTICE_SURFACE, LATTICE_BOTTOM, LATTICE_XVEL, LATTICE_YVEL = 0, 1, 2, 3  # cliffs_gpu_apply_lattice
 
 
 class _Pinned:
@@ -150,6 +151,7 @@ SIGNATURES = {
     "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
     "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
+    "cliffs_gpu_apply_lattice": ([_V, _dp, _dp, _I, _I, _dp, _dp, _dp, _I], ctypes.c_int),
     "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),
     "cliffs_batch_destroy": ([_V], None),
     "cliffs_batch_set_plan": ([_V, ctypes.POINTER(BatchPlan)], ctypes.c_int),
@@ -319,6 +321,15 @@ class GpuGrid:
                        float(dipole), float(rise_time), int(bool(bottom)))
         _chk(self.L.cliffs_gpu_add_source(self.h, _p(_f64(x)), _p(_f64(y)), ctypes.byref(d)),
              "add_source")
+
+    def apply_lattice(self, x, y, xq, yq, q, target):
+        """apply_initial_conditions.f on the device (cliffs_gpu_apply_lattice):
+        lattice q (len(yq), len(xq)) at xq, yq added to target (LATTICE_*)."""
+        q = _f64(q)
+        xq = _f64(np.atleast_1d(xq))
+        yq = _f64(np.atleast_1d(yq))
+        _chk(self.L.cliffs_gpu_apply_lattice(self.h, _p(_f64(x)), _p(_f64(y)), len(xq), len(yq), _p(xq), _p(yq),
+                                             _p(q), int(target)), "apply_lattice")
 
     def set_feed(self, tinput, west=None, east=None, south=None, north=None, irec=1, freeze=True):
         arr = [_f64(a) for a in (tinput, west, east, south, north)]

@@ -482,6 +482,46 @@ __global__ void k_source(int nx, int ny, int pitch, const double* __restrict__ x
   q[(size_t)j * pitch + i] = i < nx ? (float)source_at(S, x[i], y[j]) : 0.f;
 }
 
+// apply_initial_conditions.f:7-70 on the device: the bilinear value of a
+// lattice q (nxq x nyq, x fastest) at every grid node.  The host has placed
+// the grid's columns and rows in the lattice (pinpoint): ii/jj 1-based, -1
+// for a node outside it, xc/yc the weights of the lower lattice node.  A
+// lattice one node wide along an axis interpolates along the other only.
+__global__ void k_lattice(int nx, int ny, int pitch, const int32_t* __restrict__ ii, const double* __restrict__ xc,
+                          const int32_t* __restrict__ jj, const double* __restrict__ yc, int nxq, int nyq,
+                          const double* __restrict__ q, float* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= pitch || j >= ny) return;
+  double v = 0.0;
+  if (i < nx) {
+    auto Q = [&](int a, int b) { return q[(size_t)(b - 1) * nxq + (a - 1)]; };
+    if (nxq > 2 && nyq > 2) {
+      const int a = ii[i], b = jj[j];
+      if (a > 0 && b > 0) {
+        const double x = xc[i], y = yc[j];
+        v = (Q(a, b) * x + Q(a + 1, b) * (1 - x)) * y + (Q(a, b + 1) * x + Q(a + 1, b + 1) * (1 - x)) * (1 - y);
+      }
+    } else if (nyq == 1 && nxq > 2) {
+      const int a = ii[i];
+      if (a > 0) v = Q(a, 1) * xc[i] + Q(a + 1, 1) * (1 - xc[i]);
+    } else if (nxq == 1 && nyq > 2) {
+      const int b = jj[j];
+      if (b > 0) v = Q(1, b) * yc[j] + Q(1, b + 1) * (1 - yc[j]);
+    }
+  }
+  out[(size_t)j * pitch + i] = (float)v;
+}
+
+// A field q (pitched FP32) added to the velocity component u (or v).
+__global__ void k_add_field(int nx, int ny, int pitch, float* f, const float* __restrict__ q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= nx || j >= ny) return;
+  const size_t k = (size_t)j * pitch + i;
+  f[k] += q[k];
+}
+
 // The surface rises by (w_now - w_prev) q where water stands; a dry cell takes
 // the water column dep + w_now q once that exceeds ground, as the initial
 // surface deformation of cliffs_main.f:209-213 does before the celerity
@@ -922,6 +962,40 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   return r;
 }
 
+namespace {
+
+// The bottom rises by q (device, pitched FP32) under the standing water
+// column (cliffs_main.f:205-208).  The FP64 depth the context keeps moves on
+// the host; the device depth becomes its rounding.  Synchronises.
+int move_bottom(cliffs_ctx* c, const float* q) {
+  const size_t cells = (size_t)c->pitch * c->ny;
+  std::vector<float> hq(cells), hd(cells, 0.f);
+  CK(cudaMemcpyAsync(hq.data(), q, cells * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int j = 0; j < c->ny; ++j)
+    for (int i = 0; i < c->nx; ++i) {
+      double& d = c->dep64[(size_t)j * c->nx + i];
+      d -= (double)hq[(size_t)j * c->pitch + i];
+      hd[(size_t)j * c->pitch + i] = (float)d;
+    }
+  float* dnew = nullptr;
+  if (dalloc(&dnew, cells)) return CLIFFS_ERR_NOMEM;
+  int r = CLIFFS_OK;
+  if (cudaMemcpyAsync(dnew, hd.data(), cells * sizeof(float), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    ++c->launches;
+    k_move_bottom<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dnew, c->srf[c->cur]);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(c->dep, dnew, cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream))
+      r = CLIFFS_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  cudaFree(dnew);
+  return r;
+}
+
+}  // namespace
+
 int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd, const cliffs_source* src) {
   if (!c || !xcrd || !ycrd || !src) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
@@ -930,7 +1004,7 @@ int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd,
     return CLIFFS_ERR_ARG;
   const size_t cells = (size_t)c->pitch * c->ny;
   double *dx = nullptr, *dy = nullptr;
-  float *q = nullptr, *dnew = nullptr;
+  float* q = nullptr;
   int r = CLIFFS_OK;
   if (dalloc(&dx, (size_t)c->nx) || dalloc(&dy, (size_t)c->ny) || dalloc(&q, cells)) r = CLIFFS_ERR_NOMEM;
   if (!r && (cudaMemcpyAsync(dx, xcrd, c->nx * sizeof(double), cudaMemcpyHostToDevice, c->stream) ||
@@ -943,28 +1017,7 @@ int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd,
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
   if (!r && src->bottom) {
-    // the FP64 depth moves on the host, the device depth is its rounding
-    std::vector<float> hq(cells), hd(cells, 0.f);
-    if (cudaMemcpyAsync(hq.data(), q, cells * sizeof(float), cudaMemcpyDeviceToHost, c->stream) ||
-        cudaStreamSynchronize(c->stream))
-      r = CLIFFS_ERR_CUDA;
-    for (int j = 0; !r && j < c->ny; ++j)
-      for (int i = 0; i < c->nx; ++i) {
-        double& d = c->dep64[(size_t)j * c->nx + i];
-        d -= (double)hq[(size_t)j * c->pitch + i];
-        hd[(size_t)j * c->pitch + i] = (float)d;
-      }
-    if (!r && (dalloc(&dnew, cells) ||
-               cudaMemcpyAsync(dnew, hd.data(), cells * sizeof(float), cudaMemcpyHostToDevice, c->stream)))
-      r = CLIFFS_ERR_CUDA;
-    if (!r) {
-      ++c->launches;
-      k_move_bottom<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dnew,
-                                                                c->srf[c->cur]);
-      if (cudaGetLastError() != cudaSuccess ||
-          cudaMemcpyAsync(c->dep, dnew, cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream))
-        r = CLIFFS_ERR_CUDA;
-    }
+    r = move_bottom(c, q);
   } else if (!r && src->rise_time == 0) {
     ++c->launches;
     k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur], q,
@@ -981,7 +1034,93 @@ int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd,
   cudaFree(dx);
   cudaFree(dy);
   if (q) cudaFree(q);
-  if (dnew) cudaFree(dnew);
+  return r;
+}
+
+namespace {
+
+// NestedGrid.f:129-148: the 1-based ip with xx(ip) <= xp <= xx(ip+1) by
+// bisection, and the weight of xx(ip).
+void pinpoint_host(const double* xx, int n, double xp, int32_t* ip_out, double* cp) {
+  int ip = 1, ipp = n;
+  while (ip + 2 <= ipp) {
+    const int med = (ip + ipp) / 2;
+    if (xp > xx[med - 1])
+      ip = med;
+    else
+      ipp = med;
+  }
+  *ip_out = ip;
+  *cp = n > 1 ? (xx[ip] - xp) / (xx[ip] - xx[ip - 1]) : 0.5;
+}
+
+}  // namespace
+
+int cliffs_gpu_apply_lattice(cliffs_ctx* c, const double* xcrd, const double* ycrd, int32_t nxq, int32_t nyq,
+                             const double* xq, const double* yq, const double* q, int32_t target) {
+  if (!c || !xcrd || !ycrd || !q || nxq < 1 || nyq < 1 || (nxq > 1 && !xq) || (nyq > 1 && !yq)) return CLIFFS_ERR_ARG;
+  if (target < CLIFFS_LATTICE_SURFACE || target > CLIFFS_LATTICE_YVEL) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if (c->rise_on) return CLIFFS_ERR_STATE;  // a source still rising owns the surface
+  // apply_initial_conditions.f: lattices narrower than 3 nodes along both
+  // axes, or 2 along one, leave the field as it is
+  if (!((nxq > 2 && nyq > 2) || (nyq == 1 && nxq > 2) || (nxq == 1 && nyq > 2))) return CLIFFS_OK;
+  for (int k = 1; k < nxq; ++k)
+    if (!(xq[k] > xq[k - 1])) return CLIFFS_ERR_ARG;
+  for (int k = 1; k < nyq; ++k)
+    if (!(yq[k] > yq[k - 1])) return CLIFFS_ERR_ARG;
+  // the grid's columns and rows in the lattice, on the host (O(nx + ny))
+  const double zero = 0.1e-20;
+  std::vector<int32_t> ii(c->nx, -1), jj(c->ny, -1);
+  std::vector<double> xc(c->nx, 0.0), yc(c->ny, 0.0);
+  if (nxq > 2) {
+    const double x1 = xq[0] - zero, x2 = xq[nxq - 1] + zero;
+    for (int i = 0; i < c->nx; ++i)
+      if (xcrd[i] >= x1 && xcrd[i] <= x2) pinpoint_host(xq, nxq, xcrd[i], &ii[i], &xc[i]);
+  }
+  if (nyq > 2) {
+    const double y1 = yq[0] - zero, y2 = yq[nyq - 1] + zero;
+    for (int j = 0; j < c->ny; ++j)
+      if (ycrd[j] >= y1 && ycrd[j] <= y2) pinpoint_host(yq, nyq, ycrd[j], &jj[j], &yc[j]);
+  }
+  const size_t cells = (size_t)c->pitch * c->ny;
+  int32_t *dii = nullptr, *djj = nullptr;
+  double *dxc = nullptr, *dyc = nullptr, *dq = nullptr;
+  float* f = nullptr;
+  int r = CLIFFS_OK;
+  if (dalloc(&dii, (size_t)c->nx) || dalloc(&djj, (size_t)c->ny) || dalloc(&dxc, (size_t)c->nx) ||
+      dalloc(&dyc, (size_t)c->ny) || dalloc(&dq, (size_t)nxq * nyq) || dalloc(&f, cells))
+    r = CLIFFS_ERR_NOMEM;
+  if (!r && (cudaMemcpy(dii, ii.data(), c->nx * 4, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(djj, jj.data(), c->ny * 4, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dxc, xc.data(), c->nx * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dyc, yc.data(), c->ny * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dq, q, (size_t)nxq * nyq * 8, cudaMemcpyHostToDevice)))
+    r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    ++c->launches;
+    k_lattice<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, dii, dxc, djj, dyc, nxq, nyq,
+                                                              dq, f);
+    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  }
+  if (!r) {
+    if (target == CLIFFS_LATTICE_BOTTOM) {
+      r = move_bottom(c, f);
+    } else if (target == CLIFFS_LATTICE_SURFACE) {
+      ++c->launches;
+      k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur], f,
+                                                                1.f, 0.f, (float)c->ground);
+      if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+    } else {
+      ++c->launches;
+      float* u = target == CLIFFS_LATTICE_XVEL ? c->xu[c->cur] : c->yv[c->cur];
+      k_add_field<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, u, f);
+      if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+    }
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
+  for (void* p : {(void*)dii, (void*)djj, (void*)dxc, (void*)dyc, (void*)dq, (void*)f})
+    if (p) cudaFree(p);
   return r;
 }
 

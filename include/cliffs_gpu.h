@@ -138,6 +138,24 @@ typedef struct cliffs_source {
 int cliffs_gpu_add_source(cliffs_ctx *ctx, const double *xcrd, const double *ycrd,
                           const cliffs_source *src);
 
+/* apply_initial_conditions.f:7-70 on the device.  A lattice of nxq x nyq
+ * values q (x fastest) at ascending coordinates xq (nxq), yq (nyq) is
+ * interpolated bilinearly onto the grid nodes xcrd (nx), ycrd (ny) that lie
+ * within it, and the result is added to the target field.  A lattice one
+ * node wide along an axis interpolates along the other axis only; one two
+ * nodes wide, or narrower along both axes, changes nothing.  Targets:
+ * - SURFACE: the water column, as the initial surface deformation of
+ *   cliffs_main.f:209-213.  A dry node floods once its depth exceeds ground.
+ * - BOTTOM: the bottom rises by q under the water column (quake = 1,
+ *   cliffs_main.f:205-208).
+ * - XVEL, YVEL: the velocity components (get_initial_state.f's uinput,
+ *   vinput).
+ * Call after cliffs_gpu_set_initial; synchronises. */
+enum { CLIFFS_LATTICE_SURFACE = 0, CLIFFS_LATTICE_BOTTOM = 1, CLIFFS_LATTICE_XVEL = 2, CLIFFS_LATTICE_YVEL = 3 };
+int cliffs_gpu_apply_lattice(cliffs_ctx *ctx, const double *xcrd, const double *ycrd,
+                             int32_t nxq, int32_t nyq, const double *xq, const double *yq,
+                             const double *q, int32_t target);
+
 /* Boundary forcing (get_boundary_feed.f): nt records at times tinput(nt);
  * west/east (ny,3,nt) and south/north (nx,3,nt) hold (u, v, eta) per edge
  * node, either pair may be NULL when that sweep does not run.  irec is the
