@@ -72,6 +72,18 @@ TILED, STAGED = 0, 1  # cliffs_gpu_set_sweep_kernel
 LATTICE_SURFACE, LATTICE_BOTTOM, LATTICE_XVEL, LATTICE_YVEL = 0, 1, 2, 3  # cliffs_gpu_apply_lattice
 
 
+def depth_ssl(dep, alpha=2.0, depmin=0.1):
+    """The depth_ssl tool's limiter (cliffs_depth_ssl) on a copy of dep
+    (ny, nx); returns (adjusted depth, per-passage counts (24,), status)."""
+    b = np.array(dep, dtype=np.float64, order="C", copy=True)
+    counts = np.zeros(24, np.int32)
+    st = ctypes.c_int32()
+    ny, nx = b.shape
+    _chk(load().cliffs_depth_ssl(nx, ny, _p(b), float(alpha), float(depmin), _p(counts, _ip), ctypes.byref(st)),
+         "depth_ssl")
+    return b, counts, st.value
+
+
 class _Pinned:
     """Owner of one pinned host allocation (cliffs_gpu_host_alloc), freed
     when the last array viewing it goes."""
@@ -150,6 +162,7 @@ SIGNATURES = {
     "cliffs_gpu_set_sweep_kernel": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
+    "cliffs_depth_ssl": ([_I, _I, _dp, _D, _D, _ip, _ip], ctypes.c_int),
     "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
     "cliffs_gpu_apply_lattice": ([_V, _dp, _dp, _I, _I, _dp, _dp, _dp, _I], ctypes.c_int),
     "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),

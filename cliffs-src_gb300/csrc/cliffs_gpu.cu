@@ -13,6 +13,7 @@
 #include "../../include/cliffs_gpu.h"
 #include "batch.cuh"
 #include "staged.cuh"
+#include "depth_ssl.cuh"
 
 using namespace cliffs;
 
@@ -1121,6 +1122,53 @@ int cliffs_gpu_apply_lattice(cliffs_ctx* c, const double* xcrd, const double* yc
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   for (void* p : {(void*)dii, (void*)djj, (void*)dxc, (void*)dyc, (void*)dq, (void*)f})
     if (p) cudaFree(p);
+  return r;
+}
+
+int cliffs_depth_ssl(int32_t nx, int32_t ny, double* dep, double alpha, double depmin, int32_t* counts,
+                     int32_t* status) {
+  if (nx < 1 || ny < 1 || !dep || !counts || !status || !(alpha > 0) || !(depmin > 0)) return CLIFFS_ERR_ARG;
+  int dev = 0;
+  int r = check_device(&dev);
+  if (r) return r;
+  const size_t n = (size_t)nx * ny;
+  double* b = nullptr;
+  unsigned* cnt = nullptr;
+  if (dalloc(&b, n) || dalloc(&cnt, 1)) {
+    if (b) cudaFree(b);
+    return CLIFFS_ERR_NOMEM;
+  }
+  for (int k = 0; k < 24; ++k) counts[k] = 0;
+  *status = 0;
+  const double alp2 = alpha * alpha;
+  auto passage = [&](int phase, unsigned* nodes) {
+    if (cudaMemset(cnt, 0, sizeof(unsigned)) != cudaSuccess) return CLIFFS_ERR_CUDA;
+    if (phase == 0) {
+      k_depth_ssl<0, 0><<<(nx + 127) / 128, 128>>>(nx, ny, b, alpha, alp2, depmin, cnt);
+      k_depth_ssl<0, 1><<<(ny + 127) / 128, 128>>>(nx, ny, b, alpha, alp2, depmin, cnt);
+    } else {
+      k_depth_ssl<1, 0><<<(nx + 127) / 128, 128>>>(nx, ny, b, alpha, alp2, depmin, cnt);
+      k_depth_ssl<1, 1><<<(ny + 127) / 128, 128>>>(nx, ny, b, alpha, alp2, depmin, cnt);
+    }
+    if (cudaGetLastError() != cudaSuccess) return CLIFFS_ERR_CUDA;
+    if (cudaMemcpy(nodes, cnt, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) return CLIFFS_ERR_CUDA;
+    return CLIFFS_OK;
+  };
+  if (cudaMemcpy(b, dep, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  // up to 12 passages per phase, each ending early once no node moves
+  for (int phase = 0; phase < 2 && !r; ++phase) {
+    unsigned nodes = 0;
+    for (int itry = 0; itry < 12 && !r; ++itry) {
+      r = passage(phase, &nodes);
+      if (r) break;
+      counts[12 * phase + itry] = (int32_t)nodes;
+      if (nodes == 0) break;
+    }
+    if (!r && nodes != 0) *status |= 1 << phase;
+  }
+  if (!r && cudaMemcpy(dep, b, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  cudaFree(b);
+  cudaFree(cnt);
   return r;
 }
 

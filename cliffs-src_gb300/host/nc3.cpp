@@ -320,6 +320,11 @@ void Writer::put_att_text(int varid, const std::string& name, const std::string&
   (varid < 0 ? gatts_ : vars_.at(varid).atts).push_back(std::move(a));
 }
 
+void Writer::put_att(int varid, const Attr& a) {
+  if (!defining_) throw Error("nc3: put_att after enddef");
+  (varid < 0 ? gatts_ : vars_.at(varid).atts).push_back(a);
+}
+
 void Writer::enddef() {
   if (!defining_) return;
   auto header = [&](int version) {

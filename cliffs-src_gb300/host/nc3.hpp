@@ -65,6 +65,7 @@ class Reader {
   const Var& var(int id) const { return vars_.at(id); }
   int var_id(const std::string& name) const;  // -1 when absent
   int64_t numrecs() const { return numrecs_; }
+  const std::vector<Attr>& global_atts() const { return gatts_; }
   // Number of values of a variable (all records for a record variable).
   int64_t var_count(int id) const;
   // All values of a variable converted to double, in C order.
@@ -97,6 +98,7 @@ class Writer {
   int def_dim(const std::string& name, int64_t len);  // len 0: unlimited
   int def_var(const std::string& name, Type type, const std::vector<int>& dims);
   void put_att_text(int varid, const std::string& name, const std::string& text);  // varid -1: global
+  void put_att(int varid, const Attr& a);  // an attribute as read, any type (nf_copy_att)
   void enddef();
   // A fixed variable, all values (C order), converted to the variable's type.
   void put_var(int varid, const double* v, int64_t n);

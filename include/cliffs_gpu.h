@@ -372,6 +372,25 @@ int cliffs_batch_check_barrier_timeout(cliffs_batch *b, int32_t wait_ms);
 /* Kernels the batch has launched (a persistent launch counts once). */
 int cliffs_batch_launch_count(const cliffs_batch *b, int64_t *n);
 
+/* Offline tool: depth_ssl (depth_ssl/depth_ssl.f:222-362, setSSLim) on the
+ * device.  It limits depth ratios between neighbouring nodes, for the
+ * stability of VTCS-2.  dep (nx*ny, x fastest, FP64, > 0 water) is changed in
+ * place.  Two phases, each of up to 12 passages along every column and then
+ * every row:
+ * - open water: a node whose sqrt(depth) differs from a neighbour's by more
+ *   than the ratio alpha, with all three nodes at least depmin deep, takes
+ *   the mean of its neighbours' sqrt(depth);
+ * - coastlines: a wet node with land on exactly one side is made at least
+ *   (its wet neighbour's depth) / alpha^2 deep.
+ * The reference's defaults are alpha = 2, depmin = 0.1 m; its interactive
+ * bounds are 1.5 <= alpha <= 2.5.  counts[24] gets the nodes adjusted per
+ * passage (open water, then coastlines; 0 after a phase's last).
+ * *status = bit 0 / bit 1 when a phase was still adjusting at its 12th
+ * passage (the reference's "processing is not complete").  Results are
+ * bit-identical to the sequential FP64 scan. */
+int cliffs_depth_ssl(int32_t nx, int32_t ny, double *dep, double alpha, double depmin,
+                     int32_t *counts, int32_t *status);
+
 const char *cliffs_gpu_strerror(int code);
 
 #ifdef __cplusplus

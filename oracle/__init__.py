@@ -84,6 +84,8 @@ def lib():
         L.orc_apply_ic.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp,
                                    ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
         L.orc_pinpoint.argtypes = [_dp, ctypes.c_int, ctypes.c_double, _ip, _dp]
+        L.orc_depth_ssl.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double, _ip]
+        L.orc_depth_ssl.restype = ctypes.c_int
         L.orc_metrics.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   _dp, _dp, _dp, _dp, _dp]
         L.orc_nest_tables.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int,
@@ -136,6 +138,16 @@ def apply_ic(xq, yq, qq, xp, yp, pp):
     assert pp.flags.c_contiguous and pp.dtype == np.float64
     lib().orc_apply_ic(len(xq), len(yq), _p(xq), _p(yq), _p(qq),
                        len(xp), len(yp), _p(xp), _p(yp), _p(pp))
+
+
+def depth_ssl(dep, alpha=2.0, depmin=0.1):
+    """depth_ssl/depth_ssl.f:222-362 (setSSLim) on a copy of dep (ny, nx);
+    returns (adjusted depth, per-passage counts (24,), status)."""
+    b = np.array(dep, dtype=np.float64, order="C", copy=True)
+    counts = np.zeros(24, np.int32)
+    ny, nx = b.shape
+    st = lib().orc_depth_ssl(nx, ny, _p(b), float(alpha), float(depmin), _p(counts, _ip))
+    return b, counts, st
 
 
 class NestTables:

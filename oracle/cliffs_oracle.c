@@ -926,3 +926,92 @@ void orc_gauges(const orc_grid *g, int n, const int32_t *I, const int32_t *J,
     v[k] = g->yvel[p];
   }
 }
+
+/* depth_ssl/depth_ssl.f:222-362 (setSSLim): node-wise limits on the depth
+ * ratio of neighbouring nodes, for the stability of VTCS-2.  b (nx*ny, x
+ * fastest) is changed in place.  Up to 12 passages of open-water smoothing:
+ * along every column, then every row, a node whose celerity-like sqrt(depth)
+ * differs from a neighbour's by more than the ratio alpha, with all three
+ * nodes at least depmin deep, takes the mean of its neighbours' sqrt(depth)
+ * (the scan runs in place along the line, so a node sees its updated left
+ * neighbour).  Then up to 12 passages at coastlines: a wet node with land on
+ * exactly one side is made at least (its wet neighbour's depth) / alpha^2
+ * deep.  counts[0..11] and counts[12..23] get the nodes adjusted per
+ * passage (0 after the last).  Returns 0, or 1 (open water) | 2 (coasts)
+ * when a phase ended with nodes still adjusted in its last passage. */
+int orc_depth_ssl(int nx, int ny, double *b, double alpha, double depmin, int32_t *counts) {
+  const int nm = nx > ny ? nx : ny;
+  double *q = (double *)malloc(sizeof(double) * (size_t)nm);
+  double *p = (double *)malloc(sizeof(double) * (size_t)nm);
+  int *land = (int *)malloc(sizeof(int) * (size_t)nm);
+  int status = 0;
+  for (int k = 0; k < 24; ++k) counts[k] = 0;
+  /* one line: `len` nodes at stride `st` from b + off */
+  int nodes = 0;
+  for (int itry = 1; itry <= 12; ++itry) {
+    nodes = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+      const int lines = dir == 0 ? nx : ny, len = dir == 0 ? ny : nx;
+      for (int L = 0; L < lines; ++L) {
+        double *row = dir == 0 ? b + L : b + (size_t)L * nx;
+        const size_t st = dir == 0 ? (size_t)nx : 1;
+        for (int j = 0; j < len; ++j) {
+          q[j] = row[j * st];
+          p[j] = q[j];
+          land[j] = 0;
+          if (q[j] < depmin)
+            land[j] = 1;
+          else
+            q[j] = sqrt(q[j]);
+        }
+        for (int j = 1; j < len - 1; ++j) {
+          if (!(land[j - 1] || land[j] || land[j + 1])) {
+            const double c1 = q[j + 1] / q[j];
+            const double c2 = q[j - 1] / q[j];
+            if (c1 > alpha || c2 > alpha) {
+              q[j] = (q[j - 1] + q[j + 1]) / 2;
+              p[j] = q[j] * q[j];
+              nodes++;
+            }
+          }
+        }
+        for (int j = 0; j < len; ++j) row[j * st] = p[j];
+      }
+    }
+    counts[itry - 1] = nodes;
+    if (nodes == 0) break;
+  }
+  if (nodes != 0) status |= 1;
+  const double alp2 = alpha * alpha;
+  for (int itry = 1; itry <= 12; ++itry) {
+    nodes = 0;
+    for (int dir = 0; dir < 2; ++dir) {
+      const int lines = dir == 0 ? nx : ny, len = dir == 0 ? ny : nx;
+      for (int L = 0; L < lines; ++L) {
+        double *row = dir == 0 ? b + L : b + (size_t)L * nx;
+        const size_t st = dir == 0 ? (size_t)nx : 1;
+        for (int j = 0; j < len; ++j) {
+          q[j] = row[j * st];
+          land[j] = q[j] < depmin;
+        }
+        for (int j = 1; j < len - 1; ++j) {
+          if (!land[j] && ((land[j + 1] && !land[j - 1]) || (!land[j + 1] && land[j - 1]))) {
+            const double dep = land[j + 1] ? q[j - 1] : q[j + 1];
+            if (dep / q[j] > alp2) {
+              q[j] = dep / alp2;
+              nodes++;
+            }
+          }
+        }
+        for (int j = 0; j < len; ++j) row[j * st] = q[j];
+      }
+    }
+    counts[12 + itry - 1] = nodes;
+    if (nodes == 0) break;
+  }
+  if (nodes != 0) status |= 2;
+  free(q);
+  free(p);
+  free(land);
+  return status;
+}

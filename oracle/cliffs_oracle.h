@@ -128,6 +128,11 @@ void orc_sea_state(const orc_grid *g, int lonsub, int latsub, float *hsub,
 void orc_gauges(const orc_grid *g, int n, const int32_t *I, const int32_t *J,
                 double *eta, double *u, double *v);
 
+/* depth_ssl/depth_ssl.f:222-362 (setSSLim), in place on b (nx*ny, x fastest);
+ * counts[24]: nodes adjusted per passage, open water then coastlines.
+ * Returns 0, or 1 | 2 when a phase was still adjusting at its 12th passage. */
+int orc_depth_ssl(int nx, int ny, double *b, double alpha, double depmin, int32_t *counts);
+
 #ifdef __cplusplus
 }
 #endif
