@@ -3,8 +3,9 @@ driver executable above it.
 
 nvcc compiles csrc/cliffs_gpu.cu for sm_103a only (GB300) into
 _lib/libcliffs_gpu.so; g++ compiles host/*.cpp (the Cliffs driver with its
-NetCDF classic I/O) into _lib/cliffs_gb300, and the depth_ssl tool into
-_lib/depth_ssl_gb300, both linked against that library.
+NetCDF classic I/O) into _lib/cliffs_gb300, and the offline tools depth_ssl
+and ComputeBoundaryInput into _lib/depth_ssl_gb300 and _lib/cmpboundary_gb300,
+all linked against that library.
 Both stay in the source tree.  No torch, no cmake.
 """
 import glob
@@ -17,9 +18,10 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libcliffs_gpu.so")
 SRC = [os.path.join(HERE, "csrc", "cliffs_gpu.cu"), os.path.join(HERE, "csrc", "mlp.cu")]
 DRIVER = os.path.join(LIBDIR, "cliffs_gb300")
-TOOL = os.path.join(LIBDIR, "depth_ssl_gb300")  # the depth_ssl tool
-TOOL_SRC = [os.path.join(HERE, "host", "depth_ssl_main.cpp"), os.path.join(HERE, "host", "nc3.cpp")]
-HOST_SRC = sorted(p for p in glob.glob(os.path.join(HERE, "host", "*.cpp")) if p != TOOL_SRC[0])
+# the offline tools: executable -> its main source (each linked with nc3.cpp)
+TOOLS = {os.path.join(LIBDIR, "depth_ssl_gb300"): os.path.join(HERE, "host", "depth_ssl_main.cpp"),
+         os.path.join(LIBDIR, "cmpboundary_gb300"): os.path.join(HERE, "host", "cmpboundary_main.cpp")}
+HOST_SRC = sorted(p for p in glob.glob(os.path.join(HERE, "host", "*.cpp")) if p not in TOOLS.values())
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,21 +38,23 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Build the library, then the driver; returns the library's path."""
     lib = build_lib(force, verbose)
     build_driver(force)
-    build_tool(force)
+    for exe, main in TOOLS.items():
+        build_tool(exe, main, force)
     return lib
 
 
-def build_tool(force: bool = False) -> str:
-    deps = TOOL_SRC + glob.glob(os.path.join(HERE, "host", "*.hpp")) + [LIB, os.path.join(ROOT, "include", "cliffs_gpu.h")]
-    if not force and os.path.exists(TOOL):
-        if os.path.getmtime(TOOL) >= max(os.path.getmtime(p) for p in deps):
-            return TOOL
-    tmp = TOOL + ".tmp"
-    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", *TOOL_SRC, "-L" + LIBDIR, "-lcliffs_gpu",
+def build_tool(exe: str, main: str, force: bool = False) -> str:
+    src = [main, os.path.join(HERE, "host", "nc3.cpp")]
+    deps = src + glob.glob(os.path.join(HERE, "host", "*.hpp")) + [LIB, os.path.join(ROOT, "include", "cliffs_gpu.h")]
+    if not force and os.path.exists(exe):
+        if os.path.getmtime(exe) >= max(os.path.getmtime(p) for p in deps):
+            return exe
+    tmp = exe + ".tmp"
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-Wextra", *src, "-L" + LIBDIR, "-lcliffs_gpu",
            "-Wl,-rpath,$ORIGIN", "-o", tmp]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, TOOL)
-    return TOOL
+    os.replace(tmp, exe)
+    return exe
 
 
 def build_driver(force: bool = False) -> str:

@@ -84,6 +84,46 @@ def depth_ssl(dep, alpha=2.0, depmin=0.1):
     return b, counts, st.value
 
 
+def _nest_desc(t):
+    """A cliffs_nest_desc of a tables dict; returns it with the arrays it points to."""
+    keep = [np.ascontiguousarray(t["WE_ny"], np.int32), _f64(t["WE_cy"]), np.ascontiguousarray(t["SN_nx"], np.int32),
+            _f64(t["SN_cx"])]
+    d = NestDesc(mm=len(keep[2]), nn=len(keep[0]), W_nx=int(t["W_nx"]), E_nx=int(t["E_nx"]), S_ny=int(t["S_ny"]),
+                 N_ny=int(t["N_ny"]), W_cx=float(t["W_cx"]), E_cx=float(t["E_cx"]), S_cy=float(t["S_cy"]),
+                 N_cy=float(t["N_cy"]), WE_ny=_p(keep[0], _ip), WE_cy=_p(keep[1]), SN_nx=_p(keep[2], _ip),
+                 SN_cx=_p(keep[3]))
+    return d, keep
+
+
+def boundary_scan(cube, cuke):
+    """scan4wave.f on the device (cliffs_boundary_scan): cube (nt, ny, nx)
+    float32, the target's footprint; the first 1-based record above cuke in
+    magnitude, or nt + 1 (any result >= nt is no signal)."""
+    c = np.ascontiguousarray(cube, np.float32)
+    nt, ny, nx = c.shape
+    first = ctypes.c_int32()
+    _chk(load().cliffs_boundary_scan(nx, ny, nt, _p(c, _fp), float(cuke), ctypes.byref(first)), "boundary_scan")
+    return first.value
+
+
+def boundary_edges(tables, cubes, scale=1.0):
+    """InterpolateOntoBndr.f on the device (cliffs_boundary_edges): the edge
+    records of a target grid from the footprint cubes (u, v, eta), each
+    (nt, ny, nx) float32.  Returns west, east (nt, 3, nn), south, north
+    (nt, 3, mm)."""
+    d, keep = _nest_desc(tables)
+    nt = cubes[0].shape[0]
+    mm, nn = d.mm, d.nn
+    w, e = np.zeros((nt, 3, nn)), np.zeros((nt, 3, nn))
+    s, n = np.zeros((nt, 3, mm)), np.zeros((nt, 3, mm))
+    for ival, cube in enumerate(cubes, start=1):
+        c = np.ascontiguousarray(cube, np.float32)
+        _, ny, nx = c.shape
+        _chk(load().cliffs_boundary_edges(ctypes.byref(d), nx, ny, nt, _p(c, _fp), float(scale), ival, _p(w), _p(e),
+                                          _p(s), _p(n)), "boundary_edges")
+    return w, e, s, n
+
+
 class _Pinned:
     """Owner of one pinned host allocation (cliffs_gpu_host_alloc), freed
     when the last array viewing it goes."""
@@ -163,6 +203,9 @@ SIGNATURES = {
     "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
     "cliffs_depth_ssl": ([_I, _I, _dp, _D, _D, _ip, _ip], ctypes.c_int),
+    "cliffs_boundary_scan": ([_I, _I, _I, _fp, _D, _ip], ctypes.c_int),
+    "cliffs_boundary_edges": ([ctypes.POINTER(NestDesc), _I, _I, _I, _fp, _D, _I, _dp, _dp, _dp, _dp],
+                              ctypes.c_int),
     "cliffs_gpu_add_source": ([_V, _dp, _dp, ctypes.POINTER(SourceDesc)], ctypes.c_int),
     "cliffs_gpu_apply_lattice": ([_V, _dp, _dp, _I, _I, _dp, _dp, _dp, _I], ctypes.c_int),
     "cliffs_batch_create": ([ctypes.POINTER(_V), _I, ctypes.POINTER(_V)], ctypes.c_int),

@@ -14,6 +14,7 @@
 #include "batch.cuh"
 #include "staged.cuh"
 #include "depth_ssl.cuh"
+#include "boundary.cuh"
 
 using namespace cliffs;
 
@@ -1169,6 +1170,82 @@ int cliffs_depth_ssl(int32_t nx, int32_t ny, double* dep, double alpha, double d
   if (!r && cudaMemcpy(dep, b, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = CLIFFS_ERR_CUDA;
   cudaFree(b);
   cudaFree(cnt);
+  return r;
+}
+
+int cliffs_boundary_scan(int32_t nx, int32_t ny, int32_t nt, const float* cube, double cuke, int32_t* first) {
+  if (nx < 1 || ny < 1 || nt < 1 || !cube || !first) return CLIFFS_ERR_ARG;
+  int dev = 0;
+  int r = check_device(&dev);
+  if (r) return r;
+  const size_t n = (size_t)nx * ny * nt;
+  float *d = nullptr, *hi = nullptr, *lo = nullptr;
+  if (dalloc(&d, n) || dalloc(&hi, (size_t)nt) || dalloc(&lo, (size_t)nt)) r = CLIFFS_ERR_NOMEM;
+  std::vector<float> h(nt), l(nt);
+  if (!r && cudaMemcpy(d, cube, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    k_boundary_scan<<<nt, 256>>>(nx, ny, d, hi, lo);
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(h.data(), hi, nt * 4, cudaMemcpyDeviceToHost) ||
+        cudaMemcpy(l.data(), lo, nt * 4, cudaMemcpyDeviceToHost))
+      r = CLIFFS_ERR_CUDA;
+  }
+  if (!r) {  // scan4wave.f: the first record above cuke, nt + 1 when none
+    int it = 1;
+    while (it <= nt && !((double)h[it - 1] > cuke || (double)l[it - 1] > cuke)) ++it;
+    *first = it;
+  }
+  for (void* p : {(void*)d, (void*)hi, (void*)lo})
+    if (p) cudaFree(p);
+  return r;
+}
+
+int cliffs_boundary_edges(const cliffs_nest_desc* t, int32_t nx, int32_t ny, int32_t nt, const float* cube,
+                          double scale, int32_t ival, double* west, double* east, double* south, double* north) {
+  if (!t || !cube || !west || !east || !south || !north || nx < 2 || ny < 2 || nt < 1 || ival < 1 || ival > 3 ||
+      t->mm < 1 || t->nn < 1 || !t->WE_ny || !t->WE_cy || !t->SN_nx || !t->SN_cx)
+    return CLIFFS_ERR_ARG;
+  // every lattice column and row the interpolation reads lies in the cube
+  for (int i = 0; i < t->nn; ++i) {
+    const int kk = t->WE_ny[i] - t->WE_ny[0] + 1;
+    if (kk < 1 || kk + 1 > ny) return CLIFFS_ERR_ARG;
+  }
+  for (int i = 0; i < t->mm; ++i) {
+    const int kk = t->SN_nx[i] - t->SN_nx[0] + 1;
+    if (kk < 1 || kk + 1 > nx) return CLIFFS_ERR_ARG;
+  }
+  int dev = 0;
+  int r = check_device(&dev);
+  if (r) return r;
+  const int mm = t->mm, nn = t->nn;
+  const size_t n = (size_t)nx * ny * nt, rw = (size_t)3 * nn * nt, rs = (size_t)3 * mm * nt;
+  float* d = nullptr;
+  int32_t *we = nullptr, *sn = nullptr;
+  double *wc = nullptr, *sc = nullptr, *out = nullptr;
+  if (dalloc(&d, n) || dalloc(&we, (size_t)nn) || dalloc(&sn, (size_t)mm) || dalloc(&wc, (size_t)nn) ||
+      dalloc(&sc, (size_t)mm) || dalloc(&out, 2 * rw + 2 * rs))
+    r = CLIFFS_ERR_NOMEM;
+  double *dw = out, *de = out + rw, *ds = out + 2 * rw, *dn = out + 2 * rw + rs;
+  // the other components of the records stay as the caller has them
+  if (!r && (cudaMemcpy(d, cube, n * 4, cudaMemcpyHostToDevice) || cudaMemcpy(we, t->WE_ny, nn * 4, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(sn, t->SN_nx, mm * 4, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(wc, t->WE_cy, nn * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(sc, t->SN_cx, mm * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dw, west, rw * 8, cudaMemcpyHostToDevice) || cudaMemcpy(de, east, rw * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(ds, south, rs * 8, cudaMemcpyHostToDevice) ||
+             cudaMemcpy(dn, north, rs * 8, cudaMemcpyHostToDevice)))
+    r = CLIFFS_ERR_CUDA;
+  if (!r) {
+    const long long work = (long long)(nn + mm) * nt;
+    k_boundary_edges<<<(unsigned)((work + 127) / 128), 128>>>(nx, ny, nt, d, (float)scale, ival, mm, nn, t->W_cx,
+                                                               t->E_cx, t->S_cy, t->N_cy, we, wc, sn, sc, dw, de, ds,
+                                                               dn);
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpy(west, dw, rw * 8, cudaMemcpyDeviceToHost) ||
+        cudaMemcpy(east, de, rw * 8, cudaMemcpyDeviceToHost) || cudaMemcpy(south, ds, rs * 8, cudaMemcpyDeviceToHost) ||
+        cudaMemcpy(north, dn, rs * 8, cudaMemcpyDeviceToHost))
+      r = CLIFFS_ERR_CUDA;
+  }
+  for (void* p : {(void*)d, (void*)we, (void*)sn, (void*)wc, (void*)sc, (void*)out})
+    if (p) cudaFree(p);
   return r;
 }
 

@@ -391,6 +391,31 @@ int cliffs_batch_launch_count(const cliffs_batch *b, int64_t *n);
 int cliffs_depth_ssl(int32_t nx, int32_t ny, double *dep, double alpha, double depmin,
                      int32_t *counts, int32_t *status);
 
+/* Offline tool: ComputeBoundaryInput (cmpboundary/cmpboundary.f:44-190) on
+ * the device.  It builds the edge forcing records of a target grid
+ * (get_boundary_feed.f's input) from a coarse sea-state cube.  The caller
+ * cuts the cube to the target's footprint in the source lattice: columns
+ * W_nx .. E_nx+1, rows S_ny .. N_ny+1 of the tables (cliffs_nest_desc, with
+ * pinpoint of the target's coordinates in the source's), x fastest, then
+ * rows, then records.  Values below -1e10 count as missing (0).
+ * - scan (scan4wave.f): *first gets the first 1-based record whose largest
+ *   value or largest negated value exceeds cuke, or nt + 1 when none does.
+ *   As in the reference, *first >= nt counts as no signal (a first signal
+ *   at the last record included); the caller decides what follows.
+ * - edges (InterpolateOntoBndr.f:6-38): component ival (1 u, 2 v, 3 eta) of
+ *   the records west/east (nn,3,nt) and south/north (mm,3,nt), Fortran order.
+ *   Each value is first linear across the edge, between the lattice columns
+ *   (rows) that straddle it, then linear along the edge.  Values are taken
+ *   times scale first, as a single-precision product (1 for metres, 0.01
+ *   for centimetres, get_sea_state.f).  The other components are left as
+ *   passed.
+ * Results are bit-identical to the sequential FP64 computation. */
+int cliffs_boundary_scan(int32_t nx, int32_t ny, int32_t nt, const float *cube, double cuke,
+                         int32_t *first);
+int cliffs_boundary_edges(const cliffs_nest_desc *tables, int32_t nx, int32_t ny, int32_t nt,
+                          const float *cube, double scale, int32_t ival, double *west,
+                          double *east, double *south, double *north);
+
 const char *cliffs_gpu_strerror(int code);
 
 #ifdef __cplusplus

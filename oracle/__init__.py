@@ -86,6 +86,10 @@ def lib():
         L.orc_pinpoint.argtypes = [_dp, ctypes.c_int, ctypes.c_double, _ip, _dp]
         L.orc_depth_ssl.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double, _ip]
         L.orc_depth_ssl.restype = ctypes.c_int
+        L.orc_boundary_scan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp, ctypes.c_double]
+        L.orc_boundary_scan.restype = ctypes.c_int
+        L.orc_boundary_edges.argtypes = [N, ctypes.c_int, ctypes.c_int, ctypes.c_int, _fp, ctypes.c_double,
+                                         ctypes.c_int, _dp, _dp, _dp, _dp]
         L.orc_metrics.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   _dp, _dp, _dp, _dp, _dp]
         L.orc_nest_tables.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int,
@@ -148,6 +152,32 @@ def depth_ssl(dep, alpha=2.0, depmin=0.1):
     ny, nx = b.shape
     st = lib().orc_depth_ssl(nx, ny, _p(b), float(alpha), float(depmin), _p(counts, _ip))
     return b, counts, st
+
+
+def boundary_scan(cube, cuke):
+    """cmpboundary/scan4wave.f on a footprint cube (nt, ny, nx) of float32:
+    the first 1-based record above cuke in magnitude, or nt + 1 (the
+    reference counts any result >= nt as no signal)."""
+    c = np.ascontiguousarray(cube, dtype=np.float32)
+    nt, ny, nx = c.shape
+    return lib().orc_boundary_scan(nx, ny, nt, _p(c, _fp), float(cuke))
+
+
+def boundary_edges(tables, cubes, scale=1.0):
+    """cmpboundary/InterpolateOntoBndr.f:6-38: the edge records of a target
+    grid (NestTables of its coordinates in the source lattice) from the
+    footprint cubes (u, v, eta), each (nt, ny, nx) float32.  Returns west,
+    east (nt, 3, nn) and south, north (nt, 3, mm)."""
+    nt = cubes[0].shape[0]
+    mm, nn = tables.mm, tables.nn
+    w, e = np.zeros((nt, 3, nn)), np.zeros((nt, 3, nn))
+    s, n = np.zeros((nt, 3, mm)), np.zeros((nt, 3, mm))
+    for ival, cube in enumerate(cubes, start=1):
+        c = np.ascontiguousarray(cube, dtype=np.float32)
+        _, ny, nx = c.shape
+        lib().orc_boundary_edges(ctypes.byref(tables.s), nx, ny, nt, _p(c, _fp), float(scale), ival,
+                                 _p(w), _p(e), _p(s), _p(n))
+    return w, e, s, n
 
 
 class NestTables:

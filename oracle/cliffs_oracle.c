@@ -1015,3 +1015,72 @@ int orc_depth_ssl(int nx, int ny, double *b, double alpha, double depmin, int32_
   free(land);
   return status;
 }
+
+/* cmpboundary/scan4wave.f: the first record (1-based) of a sea-state cube
+ * (nx*ny*nt, x fastest; the target footprint) with a value above cuke or
+ * below -cuke, values below -1e10 counting as 0; nt + 1 when there is none
+ * (the loop index after a DO loop that ran out).  The reference reports "no
+ * signal above treshold" for any result >= nt. */
+int orc_boundary_scan(int nx, int ny, int nt, const float *sea, double cuke) {
+  const double nanum = -1.0e+10;
+  int it;
+  for (it = 1; it <= nt; ++it) {
+    const float *s = sea + (size_t)(it - 1) * nx * ny;
+    double mx = -INFINITY, mn = -INFINITY;
+    for (size_t k = 0; k < (size_t)nx * ny; ++k) {
+      const double v = s[k] < nanum ? 0.0 : (double)s[k];
+      if (v > mx) mx = v;
+      if (-v > mn) mn = -v;
+    }
+    if (mx > cuke) break;
+    if (mn > cuke) break;
+  }
+  return it;
+}
+
+/* One value of the sea-state cube, 1-based (i, j, k), as get_sea_state.f
+ * leaves it: below -1e10 as 0, then scaled. */
+static double orc_sea_value(const float *sea, int nx, int ny, int i, int j, int k, double nanum, double scale) {
+  float v = sea[(size_t)(i - 1) + (size_t)(j - 1) * nx + (size_t)(k - 1) * nx * ny];
+  if (v < nanum) v = 0.0f;
+  if (scale != 1.0) v = v * (float)scale; /* sea = 0.01*sea: a real*4 product */
+  return (double)v;
+}
+
+/* cmpboundary/InterpolateOntoBndr.f:6-38 with get_sea_state.f: the edge
+ * records of a target grid from a sea-state cube (nx*ny*nt floats, x
+ * fastest, the footprint from lattice column W_nx and row S_ny), values below
+ * -1e10 as 0, times scale (1 for metres, 0.01 for centimetres).  Component
+ * ival (1 u, 2 v, 3 eta) of west/east (nn,3,nt) and south/north (mm,3,nt),
+ * Fortran order (node fastest).  t is the nest's table (orc_nest). */
+void orc_boundary_edges(const orc_nest *t, int nx, int ny, int nt, const float *sea, double scale, int ival,
+                        double *west, double *east, double *south, double *north) {
+  const double nanum = -1.0e+10;
+#define SEA(i, j, k) orc_sea_value(sea, nx, ny, (i), (j), (k), nanum, scale)
+  const int mm = t->mm, nn = t->nn;
+  for (int k = 1; k <= nt; ++k) {
+    for (int i = 1; i <= nn; ++i) {
+      const int kk = t->WE_ny[i - 1] - t->WE_ny[0] + 1;
+      const double cc = t->WE_cy[i - 1];
+      const double w1 = t->W_cx * SEA(1, kk, k) + (1 - t->W_cx) * SEA(2, kk, k);
+      const double w2 = t->W_cx * SEA(1, kk + 1, k) + (1 - t->W_cx) * SEA(2, kk + 1, k);
+      const double e1 = t->E_cx * SEA(nx - 1, kk, k) + (1 - t->E_cx) * SEA(nx, kk, k);
+      const double e2 = t->E_cx * SEA(nx - 1, kk + 1, k) + (1 - t->E_cx) * SEA(nx, kk + 1, k);
+      const size_t o = (size_t)(i - 1) + (size_t)(ival - 1) * nn + (size_t)(k - 1) * 3 * nn;
+      west[o] = cc * w1 + (1 - cc) * w2;
+      east[o] = cc * e1 + (1 - cc) * e2;
+    }
+    for (int i = 1; i <= mm; ++i) {
+      const int kk = t->SN_nx[i - 1] - t->SN_nx[0] + 1;
+      const double cc = t->SN_cx[i - 1];
+      const double s1 = t->S_cy * SEA(kk, 1, k) + (1 - t->S_cy) * SEA(kk, 2, k);
+      const double s2 = t->S_cy * SEA(kk + 1, 1, k) + (1 - t->S_cy) * SEA(kk + 1, 2, k);
+      const double n1 = t->N_cy * SEA(kk, ny - 1, k) + (1 - t->N_cy) * SEA(kk, ny, k);
+      const double n2 = t->N_cy * SEA(kk + 1, ny - 1, k) + (1 - t->N_cy) * SEA(kk + 1, ny, k);
+      const size_t o = (size_t)(i - 1) + (size_t)(ival - 1) * mm + (size_t)(k - 1) * 3 * mm;
+      south[o] = cc * s1 + (1 - cc) * s2;
+      north[o] = cc * n1 + (1 - cc) * n2;
+    }
+  }
+#undef SEA
+}

@@ -133,6 +133,14 @@ void orc_gauges(const orc_grid *g, int n, const int32_t *I, const int32_t *J,
  * Returns 0, or 1 | 2 when a phase was still adjusting at its 12th passage. */
 int orc_depth_ssl(int nx, int ny, double *b, double alpha, double depmin, int32_t *counts);
 
+/* cmpboundary/scan4wave.f on a footprint cube (nx*ny*nt floats, x fastest):
+ * the first 1-based record above cuke in magnitude, or nt + 1. */
+int orc_boundary_scan(int nx, int ny, int nt, const float *sea, double cuke);
+/* cmpboundary/InterpolateOntoBndr.f:6-38: component ival (1 u, 2 v, 3 eta) of
+ * the edge records from the footprint cube, scaled by scale. */
+void orc_boundary_edges(const orc_nest *t, int nx, int ny, int nt, const float *sea, double scale, int ival,
+                        double *west, double *east, double *south, double *north);
+
 #ifdef __cplusplus
 }
 #endif

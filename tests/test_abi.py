@@ -20,7 +20,7 @@ def _declared():
     names = []
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
-        names += re.findall(r"\b(cliffs_(?:gpu|batch|mlp|depth)_\w+)\s*\(", src)
+        names += re.findall(r"\b(cliffs_(?:gpu|batch|mlp|depth|boundary)_\w+)\s*\(", src)
     return sorted(set(names))
 
 
