@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <initializer_list>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -147,6 +148,9 @@ struct cliffs_ctx {
   int grid_sx = 0, grid_sy = 0;  // resident blocks of staged_x / staged_y
   unsigned long long stage_ns = 2000000000ull;  // limit of one stage wait
   int graph_kind = -1;
+  // fast-kernel sweeps launched as programmatic dependents of the previous
+  // sweep (CLIFFS_PDL=0 in the environment at context creation turns it off)
+  bool pdl = true;
   // asynchronous outputs: a copy stream and a ring of slots; ticket k uses
   // slot k % kOutSlots.  Gauge indices stay on the device between calls.
   cudaStream_t cpy = nullptr;
@@ -608,6 +612,23 @@ SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
   return A;
 }
 
+// One fast-kernel sweep on the context's stream, a programmatic dependent of
+// the previous launch when c->pdl is set.
+template <int DIR>
+cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArgs& A) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = c->pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true>, A);
+}
+
 int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
                  int flen, int irec, double cc) {
   SweepArgs A = sweep_args(c, iu, fuse_max, c->cur);
@@ -644,12 +665,12 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     const int cells = c->blk_x * kCellsPerThread;
     const dim3 grid((A.n + cells - 1) / cells, A.nlines);
     ++c->launches;
-    fast_kernel<0, true><<<grid, c->blk_x, 0, c->stream>>>(A);
+    CK(launch_fast<0>(c, grid, (unsigned)c->blk_x, A));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
     ++c->launches;
-    fast_kernel<1, true><<<grid, 32 * c->warps_y, 0, c->stream>>>(A);
+    CK(launch_fast<1>(c, grid, (unsigned)(32 * c->warps_y), A));
   }
   CK(cudaGetLastError());
   if (c->prof) {
@@ -741,6 +762,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   if (r) return r;
   cliffs_ctx* c = new cliffs_ctx();
   c->dev = dev;
+  if (const char* e = getenv("CLIFFS_PDL")) c->pdl = std::strcmp(e, "0") != 0;
   c->nx = d->nx;
   c->ny = d->ny;
   c->pitch = (d->nx + 31) / 32 * 32;

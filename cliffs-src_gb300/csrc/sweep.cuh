@@ -496,8 +496,15 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
   }
 }
 
+// Launched with programmatic stream serialization, consecutive sweeps
+// overlap their launch: this grid lets the next one be scheduled once all of
+// its own blocks have started, and waits for the previous grid to complete
+// (its stores visible) before any load or store of the state.  Without the
+// launch attribute both instructions are no-ops.
 template <int DIR, bool LOCAL>
 __global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   sweep_tile<DIR, LOCAL, false>(A, blockIdx.x, blockIdx.y);
 }
 
