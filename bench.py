@@ -147,21 +147,29 @@ def config_dict(case, impl_note):
             "parallelism": "replicas only (one independent grid per GPU)", "impl": impl_note}
 
 
-def cpu_baseline(case, steps, threads):
-    """The CPU restatement (oracle) timed on a bounded sample of the workload."""
-    import oracle
-    from tests.runners import oracle_model
+def cpu_baseline(case, steps, threads, f32=True):
+    """The CPU restatement (oracle) timed on a bounded sample of the workload;
+    with f32, also the same source built in FP32 (like for like with the FP32
+    GPU path), reported under "f32"."""
+    import oracle  # noqa: F401
+    from tests.runners import oracle_model, oracle_model32
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    m = oracle_model(case)
-    m.step(1)  # warm-up
-    t0 = time.perf_counter()
-    m.step(steps)
-    dt = time.perf_counter() - t0
     cells = case["dep"].size
-    val = cells * steps / dt / 1e6
-    return {"value": round(val, 3), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
+
+    def timed(m):
+        m.step(1)  # warm-up
+        t0 = time.perf_counter()
+        m.step(steps)
+        return cells * steps / (time.perf_counter() - t0) / 1e6
+
+    val = timed(oracle_model(case))
+    line = {"value": round(val, 3), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
             "sample": f"{case['dep'].shape[1]}x{case['dep'].shape[0]} grid, {steps} time steps after 1 warm-up step, "
                       f"OpenMP over lines ({threads} threads), FP64"}
+    if f32:
+        line["f32"] = {"value": round(timed(oracle_model32(case)), 3), "unit": "Mcell-updates/s",
+                       "sample": "the same steps with the same source built in FP32 (orc_real = float)"}
+    return line
 
 
 def run_reference(args):
@@ -174,7 +182,7 @@ def run_reference(args):
     import oracle  # noqa: F401  (builds/loads the CPU restatement)
     case = workload(args.workload)
     steps = max(1, min(args.steps, 300))
-    cb = cpu_baseline(case, steps, threads)
+    cb = cpu_baseline(case, steps, threads, f32=False)
     line = {"metric": "Mcell-updates/s", "value": cb["value"], "unit": "Mcell-updates/s",
             "n_gpus": args.gpus, "steps": steps, "warmup": 1,
             "ms_per_step": round(1e3 * case["dep"].size / (cb["value"] * 1e6), 3), "higher_is_better": True,

@@ -16,7 +16,7 @@ import os
 
 import numpy as np
 
-from .build import LIB, build
+from .build import LIB, LIB32, build
 
 GRAV = 9.800000190734863   # (double)9.8f, global_modules.f:17
 PI = 3.1415927410125732    # (double)3.1415926536f
@@ -332,3 +332,76 @@ class Model:
         if r < 0:
             raise MemoryError("orc_feed_child")
         return bool(a.value), (w, e, s, n) if r == 1 else None
+
+
+# -- FP32 variant of the time loop (a timed CPU baseline, not a checker) -----
+
+class OrcGrid32(ctypes.Structure):
+    """orc_grid of the FP32 build (orc_real = float)."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("dep", _fp), ("cel", _fp), ("xvel", _fp), ("yvel", _fp),
+                ("hmax", _fp), ("velmax", _fp),
+                ("s1", _fp), ("s2", _fp), ("zeta", _fp),
+                ("ground", ctypes.c_float), ("crough", ctypes.c_float),
+                ("dt", ctypes.c_float), ("celmin", ctypes.c_float),
+                ("edge1", _fp), ("edge2", _fp), ("mx", ctypes.c_int32),
+                ("xrun", ctypes.c_int32), ("yrun", ctypes.c_int32),
+                ("ii1", ctypes.c_int32), ("ii2", ctypes.c_int32),
+                ("jj1", ctypes.c_int32), ("jj2", ctypes.c_int32),
+                ("seg_overflow", ctypes.c_int32)]
+
+
+_lib32 = None
+
+
+def lib32():
+    global _lib32
+    if _lib32 is None:
+        if not os.path.exists(LIB32):
+            build()
+        L = ctypes.CDLL(LIB32)
+        G = ctypes.POINTER(OrcGrid32)
+        L.orc_run.argtypes = [G, ctypes.POINTER(OrcFeed), _dp, ctypes.c_int, ctypes.c_int]
+        L.orc_run.restype = ctypes.c_int
+        L.orc_celerity.argtypes = [_fp, ctypes.c_int64, ctypes.c_float]
+        L.orc_celerity.restype = ctypes.c_float
+        _lib32 = L
+    return _lib32
+
+
+class Model32:
+    """The time loop of Model in FP32 (the same source built with
+    orc_real = float): plain steps without forcing, for timing only."""
+
+    def __init__(self, dep, s1, s2, zeta, *, ground, crough, dt, cel=None, xvel=None, yvel=None):
+        L = lib32()
+        f32 = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32).copy()
+        self.dep = f32(dep)
+        ny, nx = self.dep.shape
+        self.cel = self.dep.copy() if cel is None else f32(cel)
+        self.celmin = L.orc_celerity(_p(self.cel, _fp), self.cel.size, float(ground))
+        self.xvel = np.zeros((ny, nx), np.float32) if xvel is None else f32(xvel)
+        self.yvel = np.zeros((ny, nx), np.float32) if yvel is None else f32(yvel)
+        self.hmax = np.zeros((ny, nx), np.float32)
+        self.velmax = np.zeros((ny, nx), np.float32)
+        self.s1, self.s2, self.zeta = f32(s1), f32(s2), f32(zeta)
+        xrun, yrun = nx > 2, ny > 2
+        ii1, ii2 = (2, nx - 1) if xrun else (1, 1)
+        jj1, jj2 = (2, ny - 1) if yrun else (1, 1)
+        mx = max(ny if xrun else 1, nx if yrun else 1)
+        self.edge1 = np.zeros((3, mx), np.float32)
+        self.edge2 = np.zeros((3, mx), np.float32)
+        q = lambda a: _p(a, _fp)
+        self.g = OrcGrid32(nx=nx, ny=ny, dep=q(self.dep), cel=q(self.cel), xvel=q(self.xvel), yvel=q(self.yvel),
+                           hmax=q(self.hmax), velmax=q(self.velmax), s1=q(self.s1), s2=q(self.s2),
+                           zeta=q(self.zeta), ground=float(ground), crough=float(crough), dt=float(dt),
+                           celmin=self.celmin, edge1=q(self.edge1), edge2=q(self.edge2), mx=mx,
+                           xrun=int(xrun), yrun=int(yrun), ii1=ii1, ii2=ii2, jj1=jj1, jj2=jj2, seg_overflow=0)
+        self.t = ctypes.c_double(0.0)
+        self.istep = 0
+
+    def step(self, nsteps=1):
+        done = lib32().orc_run(ctypes.byref(self.g), ctypes.cast(None, ctypes.POINTER(OrcFeed)),
+                               ctypes.byref(self.t), self.istep + 1, int(nsteps))
+        self.istep += done
+        return done

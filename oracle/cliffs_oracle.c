@@ -13,8 +13,9 @@
  */
 #include "cliffs_oracle.h"
 
-#include <math.h>
 #include <stdlib.h>
+#include <tgmath.h> /* sqrt, fabs, ... of the argument's type: float in the FP32 variant */
+#undef I            /* complex.h's imaginary unit, which tgmath.h brings in */
 #include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -25,22 +26,22 @@
 /* Automatic arrays of subroutine cliffs (cliffs.f:24-33), 1-based. */
 typedef struct {
   int cap;
-  double *h, *pp, *qq, *vv, *dx, *scl, *depth, *Pinv, *Qinv, *v, *u;
-  double *hf, *uf, *vf; /* flood-modified copies, local-rule variant */
+  orc_real *h, *pp, *qq, *vv, *dx, *scl, *depth, *Pinv, *Qinv, *v, *u;
+  orc_real *hf, *uf, *vf; /* flood-modified copies, local-rule variant */
   int *lghost, *rghost;
   unsigned char *land, *newland, *R, *L;
-  double *pqvdL, *pqvdR; /* (4, cap) */
+  orc_real *pqvdL, *pqvdR; /* (4, cap) */
 } line_scratch;
 
 static int scratch_init(line_scratch *s, int n) {
   memset(s, 0, sizeof(*s));
   s->cap = n + 2;
   const size_t m = (size_t)s->cap;
-  double **d[] = {&s->h,    &s->pp,   &s->qq, &s->vv, &s->dx, &s->scl,
+  orc_real **d[] = {&s->h,    &s->pp,   &s->qq, &s->vv, &s->dx, &s->scl,
                   &s->depth, &s->Pinv, &s->Qinv, &s->v, &s->u, &s->hf,
                   &s->uf,   &s->vf};
   for (size_t k = 0; k < sizeof(d) / sizeof(d[0]); ++k) {
-    *d[k] = (double *)calloc(m, sizeof(double));
+    *d[k] = (orc_real *)calloc(m, sizeof(orc_real));
     if (!*d[k]) return -1;
   }
   s->lghost = (int *)calloc(m, sizeof(int));
@@ -52,8 +53,8 @@ static int scratch_init(line_scratch *s, int n) {
   /* The reference dimensions pqvdL/pqvdR(4,99) and writes them at index kseg
    * without a bound (cliffs.f:26).  The oracle sizes them by the line length
    * and reports kseg > 99 through orc_grid.seg_overflow instead. */
-  s->pqvdL = (double *)calloc(4 * m, sizeof(double));
-  s->pqvdR = (double *)calloc(4 * m, sizeof(double));
+  s->pqvdL = (orc_real *)calloc(4 * m, sizeof(orc_real));
+  s->pqvdR = (orc_real *)calloc(4 * m, sizeof(orc_real));
   if (!s->lghost || !s->rghost || !s->land || !s->newland || !s->R || !s->L ||
       !s->pqvdL || !s->pqvdR)
     return -1;
@@ -61,7 +62,7 @@ static int scratch_init(line_scratch *s, int n) {
 }
 
 static void scratch_free(line_scratch *s) {
-  double *d[] = {s->h,    s->pp,   s->qq,   s->vv, s->dx, s->scl, s->depth,
+  orc_real *d[] = {s->h,    s->pp,   s->qq,   s->vv, s->dx, s->scl, s->depth,
                  s->Pinv, s->Qinv, s->v,    s->u,  s->hf, s->uf,  s->vf};
   for (size_t k = 0; k < sizeof(d) / sizeof(d[0]); ++k) free(d[k]);
   free(s->lghost);
@@ -125,26 +126,26 @@ static void scatter(orc_grid *g, int iu, int irw, int n, const line_scratch *s) 
 /* cliffs.f:175-251: VTCS-2 update of interior cell i given its left (1) and
  * right (2) neighbour states.  Writes pp(i), qq(i), vv(i). */
 static inline void vtcs2_cell(const orc_grid *g, line_scratch *s, int i,
-                              double p1, double q1, double v1, double d1,
-                              double p2, double q2, double v2, double d2) {
-  const double grav = ORC_GRAV;
-  const double ground = g->ground, crough = g->crough, dt = g->dt;
-  double uj = s->u[i];
-  double vj = s->v[i];
-  double hj = s->h[i] * s->h[i] / grav;
+                              orc_real p1, orc_real q1, orc_real v1, orc_real d1,
+                              orc_real p2, orc_real q2, orc_real v2, orc_real d2) {
+  const orc_real grav = ORC_GRAV;
+  const orc_real ground = g->ground, crough = g->crough, dt = g->dt;
+  orc_real uj = s->u[i];
+  orc_real vj = s->v[i];
+  orc_real hj = s->h[i] * s->h[i] / grav;
   /* Almost Manning (cliffs.f:204) */
-  double cc = grav * crough * uj * sqrt((uj * uj + vj * vj) / hj) / hj;
-  double pj = s->Pinv[i];
-  double qj = s->Qinv[i];
-  double sphr = (pj - qj) * (pj + qj) * s->scl[i];
-  double fm = s->dx[i - 1];
-  double fp = s->dx[i];
-  double dtx = dt / (fm + fp);
-  double dj = s->depth[i];
-  double dpj = grav * (d2 - dj);
-  double dpm = grav * (dj - d1);
+  orc_real cc = grav * crough * uj * sqrt((uj * uj + vj * vj) / hj) / hj;
+  orc_real pj = s->Pinv[i];
+  orc_real qj = s->Qinv[i];
+  orc_real sphr = (pj - qj) * (pj + qj) * s->scl[i];
+  orc_real fm = s->dx[i - 1];
+  orc_real fp = s->dx[i];
+  orc_real dtx = dt / (fm + fp);
+  orc_real dj = s->depth[i];
+  orc_real dpj = grav * (d2 - dj);
+  orc_real dpm = grav * (dj - d1);
   int water = (dj > ground) && (d1 > ground) && (d2 > ground);
-  double ej, e2, e1, Qpj, Qjm, Qsum;
+  orc_real ej, e2, e1, Qpj, Qjm, Qsum;
 
   ej = 3 * pj + qj;
   e2 = 3 * p2 + q2;
@@ -178,15 +179,15 @@ static inline void vtcs2_cell(const orc_grid *g, line_scratch *s, int i,
 
 /* cliffs.f:287-329: open / forced edges. */
 static void edges(const orc_grid *g, int iu, int irw, int n, line_scratch *s) {
-  const double grav = ORC_GRAV;
-  const double ground = g->ground, dt = g->dt;
+  const orc_real grav = ORC_GRAV;
+  const orc_real ground = g->ground, dt = g->dt;
   const int mx = g->mx;
-  const double *e1 = g->edge1, *e2 = g->edge2;
-  double flood = e1[(size_t)(irw - 1) + 2 * (size_t)mx] + s->depth[1];
+  const orc_real *e1 = g->edge1, *e2 = g->edge2;
+  orc_real flood = e1[(size_t)(irw - 1) + 2 * (size_t)mx] + s->depth[1];
   if (!s->newland[1] && !s->newland[2] && (flood > ground)) {
-    double pj = s->Pinv[1], qj = s->Qinv[1], p2 = s->Pinv[2], q2 = s->Qinv[2];
-    double sphr = (pj - qj) * (pj + qj) * s->scl[1];
-    double Qpj = (3 * (q2 + qj) + p2 + pj) * (q2 - qj) / 8 -
+    orc_real pj = s->Pinv[1], qj = s->Qinv[1], p2 = s->Pinv[2], q2 = s->Qinv[2];
+    orc_real sphr = (pj - qj) * (pj + qj) * s->scl[1];
+    orc_real Qpj = (3 * (q2 + qj) + p2 + pj) * (q2 - qj) / 8 -
                  grav * (s->depth[2] - s->depth[1]);
     s->qq[1] = qj - dt * (Qpj / s->dx[1] + sphr);
     s->pp[1] = e1[(size_t)(irw - 1) + (size_t)(iu - 1) * mx] + 2 * sqrt(grav * flood);
@@ -199,9 +200,9 @@ static void edges(const orc_grid *g, int iu, int irw, int n, line_scratch *s) {
   }
   flood = s->depth[n] + e2[(size_t)(irw - 1) + 2 * (size_t)mx];
   if (!s->newland[n - 1] && !s->newland[n] && (flood > ground)) {
-    double pj = s->Pinv[n], qj = s->Qinv[n], p1 = s->Pinv[n - 1], q1 = s->Qinv[n - 1];
-    double sphr = (pj - qj) * (pj + qj) * s->scl[n];
-    double Qjm = (3 * (p1 + pj) + q1 + qj) * (pj - p1) / 8 -
+    orc_real pj = s->Pinv[n], qj = s->Qinv[n], p1 = s->Pinv[n - 1], q1 = s->Qinv[n - 1];
+    orc_real sphr = (pj - qj) * (pj + qj) * s->scl[n];
+    orc_real Qjm = (3 * (p1 + pj) + q1 + qj) * (pj - p1) / 8 -
                  grav * (s->depth[n] - s->depth[n - 1]);
     s->pp[n] = pj - dt * (Qjm / s->dx[n - 1] - sphr);
     s->qq[n] = e2[(size_t)(irw - 1) + (size_t)(iu - 1) * mx] - 2 * sqrt(grav * flood);
@@ -216,15 +217,15 @@ static void edges(const orc_grid *g, int iu, int irw, int n, line_scratch *s) {
 
 /* cliffs.f:17-346, verbatim: the serial segment scan. */
 static void line_scan(orc_grid *g, int iu, int irw, line_scratch *s) {
-  const double grav = ORC_GRAV;
-  const double ground = g->ground, celmin = g->celmin;
-  const double sqr2 = ORC_SQR2;
+  const orc_real grav = ORC_GRAV;
+  const orc_real ground = g->ground, celmin = g->celmin;
+  const orc_real sqr2 = ORC_SQR2;
   const int n = gather(g, iu, irw, s);
-  double *h = s->h, *u = s->u, *v = s->v, *depth = s->depth;
+  orc_real *h = s->h, *u = s->u, *v = s->v, *depth = s->depth;
   int *lghost = s->lghost, *rghost = s->rghost;
   unsigned char *land = s->land, *newland = s->newland;
   int water, kseg, k1, k2, i, j, k, i1, i2;
-  double flood;
+  orc_real flood;
 
   for (i = 1; i <= n; ++i) {
     lghost[i] = 0;
@@ -352,7 +353,7 @@ static void line_scan(orc_grid *g, int iu, int irw, line_scratch *s) {
     i2 = rghost[k] - 1;
     if (i1 > i2) continue;
     for (i = i1; i <= i2; ++i) {
-      double p1, q1, v1, d1, p2, q2, v2, d2;
+      orc_real p1, q1, v1, d1, p2, q2, v2, d2;
       if (i == i1) {
         p1 = PQ(s->pqvdL, 1, k);
         q1 = PQ(s->pqvdL, 2, k);
@@ -424,11 +425,11 @@ static void line_scan(orc_grid *g, int iu, int irw, line_scratch *s) {
  * untouched.  The arithmetic per cell is the reference's, so results must be
  * bit-identical to line_scan; the equivalence tests check that. */
 static void line_local(orc_grid *g, int iu, int irw, line_scratch *s) {
-  const double grav = ORC_GRAV;
-  const double ground = g->ground, celmin = g->celmin;
-  const double sqr2 = ORC_SQR2;
+  const orc_real grav = ORC_GRAV;
+  const orc_real ground = g->ground, celmin = g->celmin;
+  const orc_real sqr2 = ORC_SQR2;
   const int n = gather(g, iu, irw, s);
-  double *h = s->h, *u = s->u, *v = s->v, *depth = s->depth;
+  orc_real *h = s->h, *u = s->u, *v = s->v, *depth = s->depth;
   unsigned char *land = s->land, *ew = s->newland, *R = s->R, *L = s->L;
   int any = 0;
 
@@ -440,14 +441,14 @@ static void line_local(orc_grid *g, int iu, int irw, line_scratch *s) {
   for (int i = 1; i <= n; ++i) {
     R[i] = 0;
     if (i >= 2 && land[i] && !land[i - 1] && u[i - 1] >= 0) {
-      double flood = (h[i - 1] * h[i - 1]) / grav - depth[i - 1] + depth[i];
+      orc_real flood = (h[i - 1] * h[i - 1]) / grav - depth[i - 1] + depth[i];
       R[i] = flood > ground;
     }
   }
   for (int i = 1; i <= n; ++i) {
     L[i] = 0;
     if (i <= n - 1 && land[i] && !R[i] && !land[i + 1] && u[i + 1] <= 0) {
-      double flood = (h[i + 1] * h[i + 1]) / grav - depth[i + 1] + depth[i];
+      orc_real flood = (h[i + 1] * h[i + 1]) / grav - depth[i + 1] + depth[i];
       L[i] = flood > ground;
     }
   }
@@ -483,7 +484,7 @@ static void line_local(orc_grid *g, int iu, int irw, line_scratch *s) {
   }
   for (int i = 2; i <= n - 1; ++i) {
     if (!ew[i]) continue;
-    double p1, q1, v1, d1, p2, q2, v2, d2;
+    orc_real p1, q1, v1, d1, p2, q2, v2, d2;
     if (ew[i - 1]) {
       p1 = s->Pinv[i - 1];
       q1 = s->Qinv[i - 1];
@@ -573,7 +574,7 @@ void orc_sweep(orc_grid *g, int iu, int local) {
 void orc_maxwave_update(orc_grid *g) {
   const size_t n = (size_t)g->nx * (size_t)g->ny;
   for (size_t k = 0; k < n; ++k) {
-    double aa = g->cel[k];
+    orc_real aa = g->cel[k];
     if (aa > g->hmax[k]) g->hmax[k] = aa;
     aa = g->xvel[k] * g->xvel[k] + g->yvel[k] * g->yvel[k];
     if (aa > g->velmax[k]) g->velmax[k] = aa;
@@ -591,8 +592,8 @@ void orc_edges_lerp(orc_grid *g, const orc_feed *f, double t, int iu) {
     for (int j = 0; j < len; ++j) {
       size_t o0 = (size_t)j + (size_t)c * len + (size_t)(irec - 2) * rec;
       size_t o1 = (size_t)j + (size_t)c * len + (size_t)(irec - 1) * rec;
-      g->edge1[(size_t)j + (size_t)c * g->mx] = a[o0] * cc + a[o1] * (1 - cc);
-      g->edge2[(size_t)j + (size_t)c * g->mx] = b[o0] * cc + b[o1] * (1 - cc);
+      g->edge1[(size_t)j + (size_t)c * g->mx] = (orc_real)(a[o0] * cc + a[o1] * (1 - cc));
+      g->edge2[(size_t)j + (size_t)c * g->mx] = (orc_real)(b[o0] * cc + b[o1] * (1 - cc));
     }
 }
 
@@ -602,8 +603,8 @@ int orc_step(orc_grid *g, orc_feed *f, double *t, int istep) {
   while (f && f->bndr_input && *t >= f->tinput[f->irec - 1]) {
     if (f->irec == f->nt) {
       f->bndr_input = 0;
-      memset(g->edge1, 0, sizeof(double) * 3 * (size_t)g->mx);
-      memset(g->edge2, 0, sizeof(double) * 3 * (size_t)g->mx);
+      memset(g->edge1, 0, sizeof(orc_real) * 3 * (size_t)g->mx);
+      memset(g->edge2, 0, sizeof(orc_real) * 3 * (size_t)g->mx);
       f->ended_step = istep;
       if (f->freeze) return 1;
     } else {
@@ -633,7 +634,7 @@ void orc_wall(double *dep, int64_t n, double dwall) {
     if (dep[k] <= dwall) dep[k] = -999;
 }
 
-double orc_celerity(double *cel, int64_t n, double ground) {
+orc_real orc_celerity(orc_real *cel, int64_t n, orc_real ground) {
   for (int64_t k = 0; k < n; ++k) {
     if (cel[k] <= ground)
       cel[k] = 0;

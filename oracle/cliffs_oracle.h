@@ -16,6 +16,12 @@
  *
  * Arrays are column-major (x fastest) exactly like the Fortran module arrays:
  * element (i,j), 1-based, lives at [(i-1) + (j-1)*nx].
+ *
+ * The grid state and the time loop are written in orc_real: double for the
+ * oracle.  The same source built with -DORC_REAL=float and
+ * -fsingle-precision-constant is an FP32 variant of the CPU time loop, timed
+ * beside the FP64 one as a like-for-like baseline of the FP32 GPU path; it is
+ * not a checker.
  */
 #ifndef CLIFFS_ORACLE_H
 #define CLIFFS_ORACLE_H
@@ -24,6 +30,11 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+#ifndef ORC_REAL
+#define ORC_REAL double
+#endif
+typedef ORC_REAL orc_real;
 
 /* Fortran default-real literals widened to real*8 (global_modules.f:17, cliffs.f:34). */
 #define ORC_GRAV 9.800000190734863
@@ -36,13 +47,13 @@ extern "C" {
  * (global_modules.f:16-55). */
 typedef struct orc_grid {
   int32_t nx, ny;
-  double *dep, *cel, *xvel, *yvel; /* (nx,ny) */
-  double *hmax, *velmax;           /* (nx,ny) */
-  const double *s1;                /* (nx-1,ny), NULL when nx<=2 */
-  const double *s2;                /* (ny-1),   NULL when ny<=2 */
-  const double *zeta;              /* (ny),     NULL when ny<=2 */
-  double ground, crough, dt, celmin;
-  double *edge1, *edge2; /* (mx,3) each */
+  orc_real *dep, *cel, *xvel, *yvel; /* (nx,ny) */
+  orc_real *hmax, *velmax;           /* (nx,ny) */
+  const orc_real *s1;                /* (nx-1,ny), NULL when nx<=2 */
+  const orc_real *s2;                /* (ny-1),   NULL when ny<=2 */
+  const orc_real *zeta;              /* (ny),     NULL when ny<=2 */
+  orc_real ground, crough, dt, celmin;
+  orc_real *edge1, *edge2; /* (mx,3) each */
   int32_t mx;
   int32_t xrun, yrun, ii1, ii2, jj1, jj2; /* cliffs_main.f:140-164 */
   int32_t seg_overflow; /* out: a line had more than 99 wet segments */
@@ -85,7 +96,7 @@ int orc_run(orc_grid *g, orc_feed *f, double *t, int istep0, int nsteps);
 void orc_wall(double *dep, int64_t n, double dwall);
 /* cliffs_main.f:218-227: cel <- 0 if cel<=ground else sqrt(grav*cel);
  * returns celmin = sqrt(grav*ground). */
-double orc_celerity(double *cel, int64_t n, double ground);
+orc_real orc_celerity(orc_real *cel, int64_t n, orc_real ground);
 /* apply_initial_conditions.f:7-70 */
 void orc_apply_ic(int nx, int ny, const double *xq, const double *yq,
                   const double *qq, int kx, int ky, const double *xp,

@@ -18,6 +18,15 @@ def oracle_model(case):
                         t0=case.get("t0", 0.0))
 
 
+def oracle_model32(case):
+    """The FP32 variant of the oracle's time loop on a case (a timed baseline)."""
+    s1, s2, zeta = oracle.metrics(case["xcrd"], case["ycrd"], case["cartesian"])
+    if case.get("zeta") is not None:
+        zeta = case["zeta"]
+    return oracle.Model32(case["dep"], s1, s2, zeta, ground=case["ground"], crough=case["crough"], dt=case["dt"],
+                          cel=case["H0"], xvel=case.get("u0"), yvel=case.get("v0"))
+
+
 def gpu_grid(case):
     return pkg.GpuGrid.from_case(case)
 
