@@ -199,3 +199,72 @@ def test_tool_refusals(tmp_path):
     # help
     r = subprocess.run([_tool()], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "Help:" in r.stdout
+
+
+def test_pipeline_parent_screenshots_force_a_child(tmp_path):
+    """The reference's workflow for an externally forced grid, all of it on
+    the GPU: a coarse run writes its screenshots (cliffs_gb300), the edge
+    records of a finer target grid are built from them (cmpboundary_gb300,
+    bit-identical to the oracle on the files as written), and the target grid
+    runs forced by those files."""
+    from scipy.interpolate import RegularGridInterpolator
+    from scipy.io import netcdf_file
+
+    from tests import cases
+    driver = os.path.join(os.path.dirname(pkg.__file__), "_lib", "cliffs_gb300")
+    d = str(tmp_path / "parent") + "/"
+    c = cases.write_case(d, steps=240, seaout=20, gout=20, maxout=120, bndout=20, child=False, feed=False)
+    pout = str(tmp_path / "pout" / "run")
+    os.makedirs(os.path.dirname(pout))
+    r = subprocess.run([driver, pout, d, "0", "src", d + "params.txt"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    # the target: a 1/3 refinement of part of the parent, its bathymetry interpolated
+    x, y, dx = c["x"], c["y"], c["x"][1] - c["x"][0]
+    xn = np.arange(x[60] + 150.0, x[130], dx / 3)
+    yn = np.arange(y[40] + 90.0, y[110], dx / 3)
+    interp = RegularGridInterpolator((y, x), c["dep"])
+    Y, X = np.meshgrid(yn, xn, indexing="ij")
+    depn = interp(np.stack([Y.ravel(), X.ravel()], 1)).reshape(Y.shape).astype(np.float32)
+    cd = str(tmp_path / "child") + "/"
+    os.makedirs(cd)
+    cases._nc_grid(cd + "tgt.nc", xn, yn, depn)
+    r = subprocess.run([_tool(), pout + "_sea_h.nc", cd + "tgt.nc", cd + "bnd", "m"], input="0.001\n",
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    # the edge records against the oracle, from the screenshots as written
+    fields = {}
+    for k in "huv":
+        f = netcdf_file(f"{pout}_sea_{k}.nc", "r", mmap=False)
+        xs, ys, ts = f.variables["xxx"][:].copy(), f.variables["yyy"][:].copy(), f.variables["time"][:].copy()
+        fields[k] = f.variables[k + "a"][:].astype(np.float32)
+        f.close()
+    t = oracle.NestTables(xs, ys, xn, yn)
+    it = oracle.boundary_scan(_footprint(t, fields["h"]), 0.001)
+    assert 1 <= it < len(ts)
+    ref = oracle.boundary_edges(t, [_footprint(t, fields[k])[it - 1:] for k in "uvh"], 1.0)
+    for edge, want in zip(("west", "east", "south", "north"), ref):
+        f = netcdf_file(f"{cd}bnd_tgt_{edge}.nc", "r", mmap=False)
+        assert np.array_equal(f.variables["vals"][:], want), edge
+        assert np.array_equal(f.variables["time"][:], ts[it - 1:])
+        f.close()
+    # the target grid, forced by those files
+    new = {"time step (sec)": f"{c['dt'] / 3!r}", "total amount of steps": "300", "1 - to deform bottom": "0",
+           "N gages": "0"}
+    lines = []
+    for s in open(d + "params.txt").read().splitlines():
+        key = s.split("\t", 1)[-1]
+        lines.append(new[key] + "\t" + key if key in new else "tgt.nc" if s == "master.nc" else s)
+        if key == "N gages":
+            break
+    with open(cd + "params.txt", "w") as f:
+        f.write("\n".join(lines) + "\n")
+    cout = str(tmp_path / "cout" / "run")
+    os.makedirs(os.path.dirname(cout))
+    r = subprocess.run([driver, cout, cd, "bnd", "0", cd + "params.txt"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr + open(cout + "_log.txt").read()
+    f = netcdf_file(cout + "_maxwave.nc", "r", mmap=False)
+    me = f.variables["MaxE"][:]
+    f.close()
+    wet = me > -1e30
+    assert wet.mean() > 0.5 and np.isfinite(me[wet]).all() and np.abs(me[wet]).max() < 20.0
