@@ -35,8 +35,9 @@ sys.path.insert(0, ROOT)
 NX = NY = 2048
 DX = 100.0
 SEED = 0
-B_X = 28   # algorithmic bytes per cell, x-sweep: read dep,eta,u,v; write eta,u,v (FP32)
-B_Y = 44   # y-sweep with the fused max-wave: 28 + read/write hmax, velmax
+# algorithmic bytes per cell (FP32) of a two-dimensional step's sweeps
+B_X = 44   # x-sweep: read dep,eta,u,v; write eta,u,v; read/write hmax,velmax (the previous step's end state)
+B_Y = 28   # y-sweep: read dep,eta,u,v; write eta,u,v
 B_STEP = B_X + B_Y
 # Steps one run of the workload may take.  In the reference scheme (and the
 # FP64 oracle alike) an edge wave running along the east coast reaches the
@@ -306,9 +307,9 @@ def run_ours(args):
     peak, peak_kind = _peaks()
     kx, ky = prof["x_ms"], prof["y_ms"]
     if ky >= kx:
-        kname, kms, bpc = "y-sweep + fused max-wave: fast_kernel<1, true>", ky, B_Y
+        kname, kms, bpc = "y-sweep: fast_kernel<1, true, false>", ky, B_Y
     else:
-        kname, kms, bpc = "x-sweep: fast_kernel<0, true>", kx, B_X
+        kname, kms, bpc = "x-sweep + max-wave of the previous step's end state: fast_kernel<0, true, false>", kx, B_X
     achieved = bpc * cells / (kms / 1e3) / 1e9 if kms > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")

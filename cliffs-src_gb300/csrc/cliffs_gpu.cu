@@ -32,6 +32,12 @@ constexpr float kNan4 = -1.0e32f;             // global_modules.f:18
     cudaError_t e_ = (x);                         \
     if (e_ != cudaSuccess) return CLIFFS_ERR_CUDA; \
   } while (0)
+// a library status: returned when not CLIFFS_OK
+#define RET(x)             \
+  do {                     \
+    const int r_ = (x);    \
+    if (r_) return r_;     \
+  } while (0)
 
 struct Nest {
   cliffs_nest_desc d;
@@ -151,6 +157,12 @@ struct cliffs_ctx {
   // fast-kernel sweeps launched as programmatic dependents of the previous
   // sweep (CLIFFS_PDL=0 in the environment at context creation turns it off)
   bool pdl = true;
+  // max-wave bookkeeping of two-dimensional steps with the tiled kernels: the
+  // x-sweep folds in the state the previous step ended with, so the end state
+  // of the latest step is pending until the next x-sweep or a max_sync.
+  // fresh: the state is not the end of a step (initial, uploaded, a source
+  // added, after a single sweep) and is never folded in.
+  bool max_pending = false, max_fresh = true;
   // asynchronous outputs: a copy stream and a ring of slots; ticket k uses
   // slot k % kOutSlots.  Gauge indices stay on the device between calls.
   cudaStream_t cpy = nullptr;
@@ -614,7 +626,7 @@ SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
 
 // One fast-kernel sweep on the context's stream, a programmatic dependent of
 // the previous launch when c->pdl is set.
-template <int DIR>
+template <int DIR, bool MAXOUT>
 cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArgs& A) {
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -626,12 +638,21 @@ cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArg
   cfg.stream = c->stream;
   cfg.attrs = at;
   cfg.numAttrs = c->pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true>, A);
+  return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT>, A);
 }
 
-int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const double* fB,
+// Max-wave handling of one sweep: none, the update with its outputs (the last
+// sweep of a step in one dimension, or with the staged kernels), or the fold
+// of its input (the x-sweep of a two-dimensional step, tiled kernels).
+enum { MAXM_NONE = 0, MAXM_OUT = 1, MAXM_IN = 2 };
+
+int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double* fB,
                  int flen, int irec, double cc) {
-  SweepArgs A = sweep_args(c, iu, fuse_max, c->cur);
+  SweepArgs A = sweep_args(c, iu, maxm == MAXM_OUT, c->cur);
+  if (maxm == MAXM_IN && iu == 1) {
+    A.hmax_in = c->hmax;
+    A.velmax_in = c->velmax;
+  }
   const int o = 1 - c->cur;
   if (fA || fB) {
     float* eb = iu == 1 ? c->edge_x : c->edge_y;
@@ -665,12 +686,18 @@ int launch_sweep(cliffs_ctx* c, int iu, bool fuse_max, const double* fA, const d
     const int cells = c->blk_x * kCellsPerThread;
     const dim3 grid((A.n + cells - 1) / cells, A.nlines);
     ++c->launches;
-    CK(launch_fast<0>(c, grid, (unsigned)c->blk_x, A));
+    if (maxm == MAXM_OUT)
+      CK((launch_fast<0, true>(c, grid, (unsigned)c->blk_x, A)));
+    else
+      CK((launch_fast<0, false>(c, grid, (unsigned)c->blk_x, A)));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
     ++c->launches;
-    CK(launch_fast<1>(c, grid, (unsigned)(32 * c->warps_y), A));
+    if (maxm == MAXM_OUT)
+      CK((launch_fast<1, true>(c, grid, (unsigned)(32 * c->warps_y), A)));
+    else
+      CK((launch_fast<1, false>(c, grid, (unsigned)(32 * c->warps_y), A)));
   }
   CK(cudaGetLastError());
   if (c->prof) {
@@ -693,6 +720,41 @@ __global__ void k_maxwave_update(int nx, int ny, int pitch, const float* __restr
   if (eta > hmax[q]) hmax[q] = eta;
   const float s = xu[q] * xu[q] + yv[q] * yv[q];
   if (s > velmax[q]) velmax[q] = s;
+}
+
+// The end state of the latest step into the max-wave fields, if the next
+// x-sweep has not folded it in yet: before hmax/velmax are read or the state
+// is changed outside a step.
+int max_sync(cliffs_ctx* c) {
+  if (!c->max_pending) return CLIFFS_OK;
+  ++c->launches;
+  k_maxwave_update<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
+                                                              c->xu[c->cur], c->yv[c->cur], c->hmax, c->velmax);
+  CK(cudaGetLastError());
+  c->max_pending = false;
+  return CLIFFS_OK;
+}
+
+// The max-wave handling of the two sweeps of a step (see MAXM_*).
+void step_modes(const cliffs_ctx* c, int* mx, int* my) {
+  if (c->sweep_kind == CLIFFS_SWEEP_STAGED && c->staged_ok) {
+    *mx = c->yrun ? MAXM_NONE : MAXM_OUT;
+    *my = MAXM_OUT;
+  } else if (c->xrun && c->yrun) {
+    *mx = c->max_fresh ? MAXM_NONE : MAXM_IN;
+    *my = MAXM_NONE;
+  } else {
+    *mx = MAXM_OUT;
+    *my = MAXM_OUT;
+  }
+}
+
+// After a step: with the fold, its end state is pending.
+void step_done(cliffs_ctx* c) {
+  int mx, my;
+  step_modes(c, &mx, &my);
+  c->max_pending = my == MAXM_NONE && c->xrun && c->yrun;
+  c->max_fresh = false;
 }
 
 int flush_profile(cliffs_ctx* c) {
@@ -925,7 +987,10 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
     r = CLIFFS_ERR_CUDA;
   if (!r && xv && cudaMemcpyAsync(dx, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!r && !reset_max && c->have_state) r = max_sync(c);  // the replaced state's pending end state
   if (!r) {
+    c->max_pending = false;
+    c->max_fresh = true;
     c->cur = 0;
     ++c->launches;
     k_init_state<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(
@@ -1026,6 +1091,8 @@ int cliffs_gpu_add_source(cliffs_ctx* c, const double* xcrd, const double* ycrd,
   if (!(src->ax > 0) || !(src->ay > 0) || !(src->rise_time >= 0) || !std::isfinite(src->amp) ||
       !std::isfinite(src->dipole) || (src->bottom && src->rise_time > 0) || c->rise_on)
     return CLIFFS_ERR_ARG;
+  RET(max_sync(c));
+  if (src->rise_time == 0) c->max_fresh = true;  // the state changes outside a step
   const size_t cells = (size_t)c->pitch * c->ny;
   double *dx = nullptr, *dy = nullptr;
   float* q = nullptr;
@@ -1093,6 +1160,8 @@ int cliffs_gpu_apply_lattice(cliffs_ctx* c, const double* xcrd, const double* yc
     if (!(xq[k] > xq[k - 1])) return CLIFFS_ERR_ARG;
   for (int k = 1; k < nyq; ++k)
     if (!(yq[k] > yq[k - 1])) return CLIFFS_ERR_ARG;
+  RET(max_sync(c));
+  c->max_fresh = true;  // the state changes outside a step
   // the grid's columns and rows in the lattice, on the host (O(nx + ny))
   const double zero = 0.1e-20;
   std::vector<int32_t> ii(c->nx, -1), jj(c->ny, -1);
@@ -1372,9 +1441,12 @@ static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int r = CLIFFS_OK;
-    for (int s = 0; s < k && !r; ++s) {
-      if (c->xrun) r = launch_sweep(c, 1, !c->yrun, nullptr, nullptr, c->ny, 2, 0.0);
-      if (!r && c->yrun) r = launch_sweep(c, 2, true, nullptr, nullptr, c->nx, 2, 0.0);
+    for (int s = 0; s < k && !r; ++s) {  // every step alike: the state is not fresh here
+      int mx, my;
+      step_modes(c, &mx, &my);
+      if (c->xrun) r = launch_sweep(c, 1, mx, nullptr, nullptr, c->ny, 2, 0.0);
+      if (!r && c->yrun) r = launch_sweep(c, 2, my, nullptr, nullptr, c->nx, 2, 0.0);
+      step_done(c);
     }
     const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     c->launches = launches;  // captured, not launched
@@ -1411,52 +1483,73 @@ int cliffs_gpu_set_graph_steps(cliffs_ctx* c, int32_t k) {
   return CLIFFS_OK;
 }
 
+// One step of the time loop body (cliffs_main.f:304-355) with a launch per
+// sweep; CLIFFS_FEED_ENDED when the forcing ended with freeze (t advanced,
+// nothing swept).
+static int one_step(cliffs_ctx* c, double* t) {
+  *t = *t + c->dt;
+  // forcing record cursor (cliffs_main.f:305-315)
+  while (c->feed_on && *t >= c->tinput[c->irec - 1]) {
+    if (c->irec == c->nt) {
+      c->feed_on = false;
+      if (c->freeze) return CLIFFS_FEED_ENDED;
+    } else {
+      c->irec = c->irec + 1;
+    }
+  }
+  double cc = 0;
+  if (c->feed_on) cc = (c->tinput[c->irec - 1] - *t) / (c->tinput[c->irec - 1] - c->tinput[c->irec - 2]);
+  if (c->rise_on) {  // the rising source's share of this step
+    RET(max_sync(c));
+    c->max_fresh = true;  // the surface changes before the sweeps
+    c->rise_el += c->dt;
+    const double w = std::min(1.0, c->rise_el / c->rise_T);
+    ++c->launches;
+    k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
+                                                              c->rise_q, (float)w, (float)c->rise_w,
+                                                              (float)c->ground);
+    CK(cudaGetLastError());
+    c->rise_w = w;
+    if (w >= 1.0) c->rise_on = false;
+  }
+  int mx, my;
+  step_modes(c, &mx, &my);
+  if (c->xrun) {
+    int r = launch_sweep(c, 1, mx, c->feed_on ? c->fw : nullptr, c->feed_on ? c->fe : nullptr, c->ny, c->irec, cc);
+    if (r) return r;
+  }
+  if (c->yrun) {
+    int r = launch_sweep(c, 2, my, c->feed_on ? c->fs : nullptr, c->feed_on ? c->fn : nullptr, c->nx, c->irec, cc);
+    if (r) return r;
+  }
+  step_done(c);
+  return CLIFFS_OK;
+}
+
 int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_done) {
   if (!c || !t || nsteps < 0) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   if (steps_done) *steps_done = 0;
+  int done = 0;
+  if (c->max_fresh && nsteps > 0) {
+    // the first step from a fresh state folds nothing into the max-wave
+    // fields; the graphs' steps all fold in the previous step's end state
+    const int r = one_step(c, t);
+    if (r) return r;
+    done = 1;
+    if (steps_done) *steps_done = 1;
+  }
   int gdone = 0;
-  const int gr = graph_steps(c, nsteps, t, steps_done, &gdone);
+  const int gr = graph_steps(c, nsteps - done, t, steps_done, &gdone);
   if (gr) return gr;
-  nsteps -= gdone;
-  for (int s = 0; s < nsteps; ++s) {
-    *t = *t + c->dt;
-    // forcing record cursor (cliffs_main.f:305-315)
-    while (c->feed_on && *t >= c->tinput[c->irec - 1]) {
-      if (c->irec == c->nt) {
-        c->feed_on = false;
-        if (c->freeze) return CLIFFS_FEED_ENDED;
-      } else {
-        c->irec = c->irec + 1;
-      }
-    }
-    double cc = 0;
-    if (c->feed_on) cc = (c->tinput[c->irec - 1] - *t) / (c->tinput[c->irec - 1] - c->tinput[c->irec - 2]);
-    if (c->rise_on) {  // the rising source's share of this step
-      c->rise_el += c->dt;
-      const double w = std::min(1.0, c->rise_el / c->rise_T);
-      ++c->launches;
-      k_add_surface<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
-                                                                c->rise_q, (float)w, (float)c->rise_w,
-                                                                (float)c->ground);
-      CK(cudaGetLastError());
-      c->rise_w = w;
-      if (w >= 1.0) c->rise_on = false;
-    }
-    if (c->xrun) {
-      int r = launch_sweep(c, 1, !c->yrun, c->feed_on ? c->fw : nullptr, c->feed_on ? c->fe : nullptr, c->ny,
-                           c->irec, cc);
-      if (r) return r;
-    }
-    if (c->yrun) {
-      int r = launch_sweep(c, 2, true, c->feed_on ? c->fs : nullptr, c->feed_on ? c->fn : nullptr, c->nx,
-                           c->irec, cc);
-      if (r) return r;
-    }
-    if (steps_done) *steps_done = gdone + s + 1;
+  done += gdone;
+  for (; done < nsteps; ++done) {
+    const int r = one_step(c, t);
+    if (r) return r;
+    if (steps_done) *steps_done = done + 1;
     if (c->prof && c->prof_pending.size() > 4096) {
-      int r = flush_profile(c);
-      if (r) return r;
+      const int f = flush_profile(c);
+      if (f) return f;
     }
   }
   return CLIFFS_OK;
@@ -1469,13 +1562,15 @@ int cliffs_gpu_sweep(cliffs_ctx* c, int32_t iu) {
   if (!c->have_state) return CLIFFS_ERR_STATE;
   if ((iu == 1 && !c->xrun) || (iu == 2 && !c->yrun)) return CLIFFS_ERR_ARG;
   const int len = iu == 1 ? c->ny : c->nx;
+  RET(max_sync(c));
+  c->max_fresh = true;  // a half step: not a step's end state
   if (c->edges_static) {
     // static edge1/edge2, stored as two identical records: lerp weight 1
     const int mx = std::max(c->xrun ? c->ny : 1, c->yrun ? c->nx : 1);
     (void)len;
-    return launch_sweep(c, iu, false, c->edge_s[0], c->edge_s[1], mx, 2, 1.0);
+    return launch_sweep(c, iu, MAXM_NONE, c->edge_s[0], c->edge_s[1], mx, 2, 1.0);
   }
-  return launch_sweep(c, iu, false, nullptr, nullptr, len, 2, 1.0);
+  return launch_sweep(c, iu, MAXM_NONE, nullptr, nullptr, len, 2, 1.0);
 }
 
 int cliffs_gpu_set_edges(cliffs_ctx* c, const double* edge1, const double* edge2) {
@@ -1499,6 +1594,7 @@ int cliffs_gpu_set_edges(cliffs_ctx* c, const double* edge1, const double* edge2
 int cliffs_gpu_maxwave_update(cliffs_ctx* c) {
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
+  c->max_pending = false;  // the update below folds the current state in
   ++c->launches;
   k_maxwave_update<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->srf[c->cur],
                                                               c->xu[c->cur], c->yv[c->cur], c->hmax, c->velmax);
@@ -1508,6 +1604,7 @@ int cliffs_gpu_maxwave_update(cliffs_ctx* c) {
 
 int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
   if (!c || !me || !mv) return CLIFFS_ERR_ARG;
+  RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
   float *a = nullptr, *b = nullptr;
   int r = CLIFFS_OK;
@@ -1528,6 +1625,7 @@ int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
 
 int cliffs_gpu_get_max_raw(cliffs_ctx* c, double* hm, double* vm) {
   if (!c) return CLIFFS_ERR_ARG;
+  RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
   double *a = nullptr, *b = nullptr;
   int r = CLIFFS_OK;
@@ -1605,6 +1703,7 @@ int cliffs_gpu_get_gauges(cliffs_ctx* c, int32_t n, const int32_t* I, const int3
 int cliffs_gpu_runup(cliffs_ctx* c, cliffs_runup* o) {
   if (!c || !o) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
+  RET(max_sync(c));
   const int blocks = 304;
   if (c->red_cap < 4 * blocks) {
     if (c->red) cudaFree(c->red);
@@ -2281,6 +2380,15 @@ static int batch_rising_steps(cliffs_batch* b, int* nsteps) {
 
 int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
   if (!b || nsteps < 0) return CLIFFS_ERR_ARG;
+  // the batched kernels update the max-wave fields with each step's end
+  // state: a step a context took alone is folded in first
+  for (cliffs_ctx* c : b->ctx)
+    if (c->max_pending) {
+      RET(max_sync(c));
+      CK(cudaStreamSynchronize(c->stream));
+    }
+  if (nsteps > 0)
+    for (cliffs_ctx* c : b->ctx) c->max_fresh = false;
   int r = batch_rising_steps(b, &nsteps);
   if (r) return r;
   if (nsteps == 0) return CLIFFS_OK;

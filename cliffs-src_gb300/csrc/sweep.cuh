@@ -40,6 +40,10 @@ struct SweepArgs {
   float* yv_o;
   float* hmax;    // max eta, nullptr when the max-wave update is not fused
   float* velmax;  // max u^2+v^2
+  // x-sweep of a two-dimensional step: the max-wave fields updated with the
+  // sweep's INPUT, the state the previous step ended with (nullptr: not)
+  float* hmax_in;
+  float* velmax_in;
   const float4* geo;  // per position m: 1/dx(m-1), 1/dx(m), dt/(dx(m-1)+dx(m)), dx(m)-dx(m-1)
   int geo_uniform;    // every interior position has geo0
   float4 geo0;
@@ -254,7 +258,7 @@ __device__ __forceinline__ unsigned rest_cells(const SweepArgs& A, int L, int i0
   return need;
 }
 
-template <int DIR, bool LOCAL, bool COH, bool TAIL = true, bool SHARED_ARGS = false>
+template <int DIR, bool LOCAL, bool COH, bool TAIL = true, bool SHARED_ARGS = false, bool MAXOUT = true>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
@@ -265,8 +269,9 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
 // worklist for general_kernel.
 // One tile of a sweep: the block's cells at block coordinates (bx, by) of the
 // sweep's grid (x: (columns / (4 * blockDim.x), rows); y: (rows / (4 * warps),
-// columns / 32)).  The whole block calls it.
-template <int DIR, bool LOCAL, bool COH, bool SHARED_ARGS = false>
+// columns / 32)).  The whole block calls it.  MAXOUT = false leaves out the
+// max-wave update of the outputs (A.hmax is then ignored).
+template <int DIR, bool LOCAL, bool COH, bool SHARED_ARGS = false, bool MAXOUT = true>
 __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
   __shared__ uint32_t s_list[LOCAL ? 256 * 4 : 1];
   __shared__ unsigned s_n;
@@ -300,9 +305,24 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
       E4 = ld_state4<COH>(A.srf + q0);
       X4 = ld_state4<COH>(A.xu + q0);
       Y4 = ld_state4<COH>(A.yv + q0);
-      if (A.hmax) {
+      if (MAXOUT && A.hmax) {
         H4 = ld_state4<COH>(A.hmax + q0);
         V4 = ld_state4<COH>(A.velmax + q0);
+      }
+      if (A.hmax_in) {
+        // the previous step's end state into the max-wave fields
+        // (cliffs_main.f:347-355), before this sweep replaces it
+        float4 HI = ld_state4<COH>(A.hmax_in + q0), VI = ld_state4<COH>(A.velmax_in + q0);
+        HI.x = fmaxf(HI.x, eta_of(E4.x, D4.x));
+        HI.y = fmaxf(HI.y, eta_of(E4.y, D4.y));
+        HI.z = fmaxf(HI.z, eta_of(E4.z, D4.z));
+        HI.w = fmaxf(HI.w, eta_of(E4.w, D4.w));
+        VI.x = fmaxf(VI.x, X4.x * X4.x + Y4.x * Y4.x);
+        VI.y = fmaxf(VI.y, X4.y * X4.y + Y4.y * Y4.y);
+        VI.z = fmaxf(VI.z, X4.z * X4.z + Y4.z * Y4.z);
+        VI.w = fmaxf(VI.w, X4.w * X4.w + Y4.w * Y4.w);
+        *reinterpret_cast<float4*>(A.hmax_in + q0) = HI;
+        *reinterpret_cast<float4*>(A.velmax_in + q0) = VI;
       }
     }
     d[1] = D4.x; d[2] = D4.y; d[3] = D4.z; d[4] = D4.w;
@@ -348,14 +368,14 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     for (int r = 0; r < kCellsPerThread; ++r) {
       hm[r] = vm[r] = 0.f;
       const int k = min(i0 + r, n);
-      if (active && A.hmax) {
+      if (MAXOUT && active && A.hmax) {
         const size_t q = cidx<1>(L, k, A.pitch);
         hm[r] = ld_state<COH>(A.hmax + q);
         vm[r] = ld_state<COH>(A.velmax + q);
       }
     }
   }
-  sweep_cells<DIR, LOCAL, COH, true, SHARED_ARGS>(A, L, i0, active, q0, d, e, u, v, hm, vm, s_list, &s_n);
+  sweep_cells<DIR, LOCAL, COH, true, SHARED_ARGS, MAXOUT>(A, L, i0, active, q0, d, e, u, v, hm, vm, s_list, &s_n);
 }
 
 // The cells i0..i0+3 of line L from their loaded window: d depth, e surface
@@ -369,7 +389,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
 // lives in shared memory (the batched kernels), where every field read is a
 // load; the geometry is then read per cell instead of held in registers for
 // the whole line, which measured 14 % faster there (fewer spills).
-template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS>
+template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS, bool MAXOUT>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
@@ -457,7 +477,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
     yo[r] = DIR == 0 ? ov[r] : ou[r];
     const bool done = i0 + r <= n && !((need >> r) & 1u);
     if (done) bad |= !isfinite(os[r] + xo[r] + yo[r]);
-    if (A.hmax && done) {  // max-wave update (cliffs_main.f:347-355)
+    if (MAXOUT && A.hmax && done) {  // max-wave update (cliffs_main.f:347-355)
       hm[r] = fmaxf(hm[r], eta_of(os[r], d[r + 1]));
       vm[r] = fmaxf(vm[r], xo[r] * xo[r] + yo[r] * yo[r]);
     }
@@ -469,7 +489,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
     *reinterpret_cast<float4*>(A.srf_o + q0) = make_float4(os[0], os[1], os[2], os[3]);
     *reinterpret_cast<float4*>(A.xu_o + q0) = make_float4(xo[0], xo[1], xo[2], xo[3]);
     *reinterpret_cast<float4*>(A.yv_o + q0) = make_float4(yo[0], yo[1], yo[2], yo[3]);
-    if (A.hmax) {
+    if (MAXOUT && A.hmax) {
       *reinterpret_cast<float4*>(A.hmax + q0) = make_float4(hm[0], hm[1], hm[2], hm[3]);
       *reinterpret_cast<float4*>(A.velmax + q0) = make_float4(vm[0], vm[1], vm[2], vm[3]);
     }
@@ -482,7 +502,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
       A.srf_o[q] = os[r];
       A.xu_o[q] = xo[r];
       A.yv_o[q] = yo[r];
-      if (A.hmax) {
+      if (MAXOUT && A.hmax) {
         A.hmax[q] = hm[r];
         A.velmax[q] = vm[r];
       }
@@ -501,11 +521,14 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
 // its own blocks have started, and waits for the previous grid to complete
 // (its stores visible) before any load or store of the state.  Without the
 // launch attribute both instructions are no-ops.
-template <int DIR, bool LOCAL>
+// MAXOUT = false: the variant without the max-wave update of the outputs
+// (the y-sweep of a two-dimensional step, whose end state the next x-sweep
+// folds in through hmax_in).
+template <int DIR, bool LOCAL, bool MAXOUT = true>
 __global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  sweep_tile<DIR, LOCAL, false>(A, blockIdx.x, blockIdx.y);
+  sweep_tile<DIR, LOCAL, false, false, MAXOUT>(A, blockIdx.x, blockIdx.y);
 }
 
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
