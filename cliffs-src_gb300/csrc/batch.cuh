@@ -10,11 +10,15 @@
 // scenario by bisection over the per-scenario tile offsets.  Two schedules:
 //   batch_persistent  one cooperative launch for many steps; the blocks loop
 //                     over the x tiles, meet at a grid barrier, loop over the
-//                     y tiles (max-wave fused), meet again, and so on;
+//                     y tiles, meet again, and so on;
 //   batch_phase<DIR>  one launch per sweep direction and step covering every
 //                     scenario, for capture in a CUDA graph.
 // A scenario's tiles do the same arithmetic as its own sweep launches, so a
-// batched run is bit-identical to stepping the grids one by one.
+// batched run is bit-identical to stepping the grids one by one.  Two
+// argument sets: "fused" (the y-sweep updates the max-wave fields with its
+// outputs), for a scenario's first step from a fresh state and for steps of
+// a rising source, and "fold" (the x-sweep folds the previous step's end
+// state in, the y-sweep has no max-wave code), for every other step.
 #pragma once
 #include "sweep.cuh"
 
@@ -50,7 +54,7 @@ __device__ __forceinline__ int batch_scenario(const int* off, int n, int t) {
 
 // The tiles first, first + stride, ... of one sweep direction over all
 // scenarios.  The scenario's arguments are staged in shared memory.
-template <int DIR, bool COH>
+template <int DIR, bool COH, bool MAXOUT>
 __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int stride) {
   __shared__ SweepArgs sA;
   const int* off = B.off + DIR * (B.n + 1);
@@ -62,7 +66,7 @@ __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int s
     __syncthreads();  // the previous tile is done with sA and its shared list
     if (threadIdx.x == 0) sA = B.args[2 * k + DIR];
     __syncthreads();
-    sweep_tile<DIR, true, COH, true>(sA, local % g, local / g);
+    sweep_tile<DIR, true, COH, true, MAXOUT>(sA, local % g, local / g);
   }
 }
 
@@ -113,19 +117,22 @@ __device__ __forceinline__ bool grid_sync(unsigned* bar, unsigned nblocks, unsig
   return s_ok != 0;
 }
 
+// MAXOUT = false: the y-sweeps carry no max-wave update (the argument set
+// whose x-sweeps fold the previous step's end state in, hmax_in).
+template <bool MAXOUT>
 __global__ void __launch_bounds__(kBatchThreads, 6) batch_persistent(const BatchArgs B) {
   unsigned epoch = 0;
   for (int s = 0; s < B.steps; ++s) {
-    batch_tiles<0, true>(B, blockIdx.x, gridDim.x);
+    batch_tiles<0, true, false>(B, blockIdx.x, gridDim.x);
     if (!grid_sync(B.bar, gridDim.x, epoch, B.err, B.wait_ns, B.extra)) return;
-    batch_tiles<1, true>(B, blockIdx.x, gridDim.x);
+    batch_tiles<1, true, MAXOUT>(B, blockIdx.x, gridDim.x);
     if (!grid_sync(B.bar, gridDim.x, epoch, B.err, B.wait_ns, B.extra)) return;
   }
 }
 
-template <int DIR>
+template <int DIR, bool MAXOUT>
 __global__ void __launch_bounds__(kBatchThreads, 6) batch_phase(const BatchArgs B) {
-  batch_tiles<DIR, false>(B, blockIdx.x, gridDim.x);
+  batch_tiles<DIR, false, MAXOUT>(B, blockIdx.x, gridDim.x);
 }
 
 }  // namespace cliffs

@@ -2192,7 +2192,8 @@ struct cliffs_batch {
   std::vector<cliffs_ctx*> ctx;
   int dev = 0, sms = 0, max_ctas = 0;
   cudaStream_t stream = nullptr;
-  SweepArgs* d_args = nullptr;
+  SweepArgs* d_args = nullptr;       // fused set
+  SweepArgs* d_args_fold = nullptr;  // fold set
   int* d_off = nullptr;
   int* d_gx = nullptr;
   unsigned* d_sync = nullptr;  // [0] barrier counter, [1] timeout flag
@@ -2203,9 +2204,9 @@ struct cliffs_batch {
   int64_t launches = 0;
 };
 
-static BatchArgs batch_args(const cliffs_batch* b, int steps) {
+static BatchArgs batch_args(const cliffs_batch* b, int steps, bool fold) {
   BatchArgs B;
-  B.args = b->d_args;
+  B.args = fold ? b->d_args_fold : b->d_args;
   B.off = b->d_off;
   B.gx = b->d_gx;
   B.n = (int)b->ctx.size();
@@ -2220,6 +2221,7 @@ static BatchArgs batch_args(const cliffs_batch* b, int steps) {
 static void batch_free(cliffs_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->d_args) cudaFree(b->d_args);
+  if (b->d_args_fold) cudaFree(b->d_args_fold);
   if (b->d_off) cudaFree(b->d_off);
   if (b->d_gx) cudaFree(b->d_gx);
   if (b->d_sync) cudaFree(b->d_sync);
@@ -2247,19 +2249,27 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
     return r;
   };
   if (cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->max_ctas, batch_persistent, kBatchThreads, 0) !=
-      cudaSuccess)
+  int ctas_fold = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->max_ctas, batch_persistent<true>, kBatchThreads, 0) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas_fold, batch_persistent<false>, kBatchThreads, 0) !=
+          cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
+  b->max_ctas = std::min(b->max_ctas, ctas_fold);  // resident with either argument set
   if (!coop) b->max_ctas = 0;  // graph schedule only
   // per scenario: the x-sweep reads copy cur and writes 1-cur, the y-sweep
   // (with the max-wave update) reads 1-cur and writes cur
-  std::vector<SweepArgs> args(2 * (size_t)n);
+  std::vector<SweepArgs> args(2 * (size_t)n), fold(2 * (size_t)n);
   std::vector<int> off(2 * ((size_t)n + 1), 0), gx(2 * (size_t)n, 0);
   for (int k = 0; k < n; ++k) {
     cliffs_ctx* c = ctxs[k];
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
     args[2 * k] = sweep_args(c, 1, false, c->cur);
     args[2 * k + 1] = sweep_args(c, 2, true, 1 - c->cur);
+    fold[2 * k] = args[2 * k];
+    fold[2 * k].hmax_in = c->hmax;
+    fold[2 * k].velmax_in = c->velmax;
+    fold[2 * k + 1] = sweep_args(c, 2, false, 1 - c->cur);
     const int xgx = (c->nx + kBatchThreads * kCellsPerThread - 1) / (kBatchThreads * kCellsPerThread);
     const int ygx = (c->ny + (kBatchThreads / 32) * kCellsPerThread - 1) / ((kBatchThreads / 32) * kCellsPerThread);
     gx[k] = xgx;
@@ -2269,10 +2279,11 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
   }
   b->total[0] = off[n];
   b->total[1] = off[(n + 1) + n];
-  if (dalloc(&b->d_args, args.size()) || dalloc(&b->d_off, off.size()) || dalloc(&b->d_gx, gx.size()) ||
-      dalloc(&b->d_sync, 2))
+  if (dalloc(&b->d_args, args.size()) || dalloc(&b->d_args_fold, fold.size()) || dalloc(&b->d_off, off.size()) ||
+      dalloc(&b->d_gx, gx.size()) || dalloc(&b->d_sync, 2))
     return fail(CLIFFS_ERR_NOMEM);
   if (cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_args_fold, fold.data(), fold.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_gx, gx.data(), gx.size() * sizeof(int), cudaMemcpyHostToDevice) ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking))
@@ -2316,11 +2327,14 @@ int cliffs_batch_launch_count(const cliffs_batch* b, int64_t* n) {
   return CLIFFS_OK;
 }
 
-static int batch_launch_phases(cliffs_batch* b, int steps) {
-  const BatchArgs B = batch_args(b, 1);
+static int batch_launch_phases(cliffs_batch* b, int steps, bool fold) {
+  const BatchArgs B = batch_args(b, 1, fold);
   for (int s = 0; s < steps; ++s) {
-    batch_phase<0><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
-    batch_phase<1><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    batch_phase<0, false><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
+    if (fold)
+      batch_phase<1, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    else
+      batch_phase<1, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
     b->launches += 2;
   }
   return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
@@ -2335,7 +2349,7 @@ static int batch_build_graph(cliffs_batch* b, int steps) {
   const int64_t before = b->launches;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  const int r = batch_launch_phases(b, steps);
+  const int r = batch_launch_phases(b, steps, true);
   const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   b->launches = before;  // captured, not launched
   if (r || e != cudaSuccess) {
@@ -2370,7 +2384,7 @@ static int batch_rising_steps(cliffs_batch* b, int* nsteps) {
       c->rise_w = w;
       if (w >= 1.0) c->rise_on = false;
     }
-    r = batch_launch_phases(b, 1);
+    r = batch_launch_phases(b, 1, false);
     for (cliffs_ctx* c : b->ctx) c->sweeps += 2u;
     --*nsteps;
   }
@@ -2380,29 +2394,44 @@ static int batch_rising_steps(cliffs_batch* b, int* nsteps) {
 
 int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
   if (!b || nsteps < 0) return CLIFFS_ERR_ARG;
-  // the batched kernels update the max-wave fields with each step's end
-  // state: a step a context took alone is folded in first
-  for (cliffs_ctx* c : b->ctx)
-    if (c->max_pending) {
-      RET(max_sync(c));
-      CK(cudaStreamSynchronize(c->stream));
-    }
-  if (nsteps > 0)
-    for (cliffs_ctx* c : b->ctx) c->max_fresh = false;
+  if (nsteps == 0) return CLIFFS_OK;
+  // Steps with the fused argument set (a fresh state's first step, the steps
+  // of a rising source) fold nothing in: pending end states go in first.
+  bool fused_first = false;
+  for (cliffs_ctx* c : b->ctx) fused_first = fused_first || c->max_fresh || c->rise_on;
+  if (fused_first)
+    for (cliffs_ctx* c : b->ctx)
+      if (c->max_pending) {
+        RET(max_sync(c));
+        CK(cudaStreamSynchronize(c->stream));
+      }
+  for (cliffs_ctx* c : b->ctx) c->max_fresh = false;
+  const int before = nsteps;
   int r = batch_rising_steps(b, &nsteps);
   if (r) return r;
-  if (nsteps == 0) return CLIFFS_OK;
+  if (fused_first && nsteps == before) {  // a fresh state's first step
+    r = batch_launch_phases(b, 1, false);
+    for (cliffs_ctx* c : b->ctx) c->sweeps += 2u;
+    --nsteps;
+    if (r) return r;
+  }
+  // the end state is folded in by the next x-sweep, or by max_sync
+  for (cliffs_ctx* c : b->ctx) c->max_pending = nsteps > 0;
+  if (nsteps == 0) {
+    CK(cudaStreamSynchronize(b->stream));
+    return CLIFFS_OK;
+  }
   if (b->plan.mode == CLIFFS_BATCH_PERSISTENT) {
     const int grid = b->plan.ctas_per_sm * b->sms;
     // at most 2^31 / grid barrier arrivals per launch keeps the counter exact
     const int chunk = std::max(1, std::min(100000, (int)(0x7fffffffu / (2u * (unsigned)grid)) - 1));
     for (int done = 0; done < nsteps && !r; done += chunk) {
       const int steps = std::min(chunk, nsteps - done);
-      BatchArgs B = batch_args(b, steps);
+      BatchArgs B = batch_args(b, steps, true);
       void* kargs[] = {&B};
       if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
-          cudaLaunchCooperativeKernel((const void*)batch_persistent, dim3(grid), dim3(kBatchThreads), kargs, 0,
-                                      b->stream) != cudaSuccess) {
+          cudaLaunchCooperativeKernel((const void*)batch_persistent<false>, dim3(grid), dim3(kBatchThreads), kargs,
+                                      0, b->stream) != cudaSuccess) {
         r = CLIFFS_ERR_CUDA;
         break;
       }
@@ -2422,7 +2451,7 @@ int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
       if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
       b->launches += 2 * (int64_t)k;
     }
-    if (!r && done < nsteps) r = batch_launch_phases(b, nsteps - done);
+    if (!r && done < nsteps) r = batch_launch_phases(b, nsteps - done, true);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   }
   if (!r)
@@ -2433,13 +2462,15 @@ int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
 int cliffs_batch_check_barrier_timeout(cliffs_batch* b, int32_t wait_ms) {
   if (!b || wait_ms < 1 || wait_ms > 2000) return CLIFFS_ERR_ARG;
   if (b->max_ctas < 1) return CLIFFS_ERR_DEVICE;
-  BatchArgs B = batch_args(b, 1);
+  // the fused set: its x-sweeps, the only tiles before the first barrier,
+  // leave the max-wave fields alone
+  BatchArgs B = batch_args(b, 1, false);
   B.wait_ns = (unsigned long long)wait_ms * 1000000ull;
   B.extra = 1;  // an arrival no block makes: the first barrier's wait runs out
   void* kargs[] = {&B};
   const int grid = b->sms;  // one block per SM
   if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
-      cudaLaunchCooperativeKernel((const void*)batch_persistent, dim3(grid), dim3(kBatchThreads), kargs, 0,
+      cudaLaunchCooperativeKernel((const void*)batch_persistent<true>, dim3(grid), dim3(kBatchThreads), kargs, 0,
                                   b->stream) != cudaSuccess)
     return CLIFFS_ERR_CUDA;
   ++b->launches;
@@ -2477,17 +2508,19 @@ int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_s
     }
     return cudaStreamSynchronize(b->stream) == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
   };
-  struct Rise {
+  struct Rise {  // a rising source's progress and the max-wave bookkeeping
     double el, w;
-    bool on;
+    bool on, pending, fresh;
   };
   std::vector<Rise> rise;
-  for (cliffs_ctx* c : b->ctx) rise.push_back(Rise{c->rise_el, c->rise_w, c->rise_on});
+  for (cliffs_ctx* c : b->ctx) rise.push_back(Rise{c->rise_el, c->rise_w, c->rise_on, c->max_pending, c->max_fresh});
   auto restore_rise = [&]() {
     for (size_t k = 0; k < b->ctx.size(); ++k) {
       b->ctx[k]->rise_el = rise[k].el;
       b->ctx[k]->rise_w = rise[k].w;
       b->ctx[k]->rise_on = rise[k].on;
+      b->ctx[k]->max_pending = rise[k].pending;
+      b->ctx[k]->max_fresh = rise[k].fresh;
     }
   };
   int r = copy_state(true);

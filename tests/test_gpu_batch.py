@@ -132,3 +132,28 @@ def test_batch_with_rising_sources_is_bit_identical():
     for g, t in zip(grids, twins):
         _same(g, t)
     b.close()
+
+
+def test_batch_after_single_steps_and_reads():
+    """Contexts that stepped alone join a batch with their last end state
+    pending; the batch's x-sweeps fold it in.  Reads of the max-wave fields
+    between batched steps, and single steps after them, keep the fields equal
+    to those of twins that never joined a batch."""
+    cases = _cases()[:3]
+    grids = [pkg.GpuGrid.from_case(c) for c in cases]
+    twins = [pkg.GpuGrid.from_case(c) for c in cases]
+    for g in grids + twins:
+        g.step(7)
+    b = pkg.Batch(grids)
+    for plan in ((cg.PERSISTENT, dict(ctas_per_sm=1)), (cg.GRAPH, dict(graph_steps=8))):
+        b.set_plan(plan[0], **plan[1])
+        b.step(20)
+        for t in twins:
+            t.step(20)
+        for g, t in zip(grids, twins):
+            _same(g, t)
+    for g in grids + twins:
+        g.step(3)
+    for g, t in zip(grids, twins):
+        _same(g, t)
+    b.close()
