@@ -175,7 +175,12 @@ int cliffs_gpu_feed_start(cliffs_ctx *ctx, double cuke);
  * y-sweep over columns 2..nx-1 (or column 1), max-wave update.  *t is the
  * model time (tinput(irec) at start).  Returns CLIFFS_FEED_ENDED with
  * *steps_done < nsteps when the forcing ended and freeze is set.  Does not
- * synchronise the stream. */
+ * synchronise the stream.
+ * The max-wave fields hold every completed step's end state, as the
+ * reference's update after each step leaves them, whenever they are read
+ * (get_maxwave, get_max_raw, runup).  In a two-dimensional grid the tiled
+ * kernels fold a step's end state in during the next step's x-sweep, and
+ * the readers fold the latest one in first. */
 int cliffs_gpu_step(cliffs_ctx *ctx, int32_t nsteps, double *t,
                     int32_t *steps_done);
 /* One sweep only: the OpenMP loop over call cliffs(iu, j, n) of
@@ -187,7 +192,8 @@ int cliffs_gpu_sweep(cliffs_ctx *ctx, int32_t iu);
  * cliffs_gpu_sweep only.  NULL clears them (still-water open boundary). */
 int cliffs_gpu_set_edges(cliffs_ctx *ctx, const double *edge1,
                          const double *edge2);
-/* Max-wave update alone (cliffs_main.f:347-355). */
+/* Max-wave update alone (cliffs_main.f:347-355), with the current state:
+ * for callers that step by single sweeps. */
 int cliffs_gpu_maxwave_update(cliffs_ctx *ctx);
 
 /* Output conversions (real*4 like the reference writers):
