@@ -1,11 +1,12 @@
 """Benchmark: Cliffs time stepping on the 2048x2048 Cartesian shelf basin.
 
-One step = one time step of the whole grid (x-sweep over all rows, y-sweep
-over all columns with the fused max-wave update), i.e. one pass of the hot
-path of cliffs_main.f:303-355.  Metric: Mcell-updates/s = nx*ny*steps/s.
+One step = one time step of the whole grid (x-sweep over all rows, which
+also folds the previous step's end state into the max-wave fields, and
+y-sweep over all columns), i.e. one pass of the hot path of
+cliffs_main.f:303-355.  Metric: Mcell-updates/s = nx*ny*steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--kernels-only] [--workload shelf2048|sphere4320]
+                  [--kernels-only] [--workload shelf2048|sphere4320] [--sweep tiled|staged]
 
 --kernels-only runs the device-resident passes alone (no end-to-end pass, no
 CPU sample): the command the ncu summaries under profiles/ capture.
@@ -255,8 +256,10 @@ def run_ours(args):
 
     # ---- device-resident throughput (value) ----------------------------------
     stream = torch.cuda.Stream()
+    kind = pkg.cliffs_gpu.STAGED if args.sweep == "staged" else pkg.cliffs_gpu.TILED
     g = pkg.GpuGrid.from_case(case)
     g.set_stream(stream.cuda_stream)
+    g.set_sweep_kernel(kind)
     g.step(args.warmup)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -280,6 +283,7 @@ def run_ours(args):
     # with CUDA events around every sweep on the solver's stream ---------------
     g = pkg.GpuGrid.from_case(case)
     g.set_stream(stream.cuda_stream)
+    g.set_sweep_kernel(kind)
     g.step(args.warmup)
     g.profile(True)
     g.step(args.steps)
@@ -351,6 +355,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernels-only", action="store_true")
     ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320"])
+    ap.add_argument("--sweep", default="tiled", choices=["tiled", "staged"],
+                    help="sweep kernels of the device-resident passes (cliffs_gpu_set_sweep_kernel)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

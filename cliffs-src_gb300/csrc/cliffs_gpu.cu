@@ -2258,7 +2258,8 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
   b->max_ctas = std::min(b->max_ctas, ctas_fold);  // resident with either argument set
   if (!coop) b->max_ctas = 0;  // graph schedule only
   // per scenario: the x-sweep reads copy cur and writes 1-cur, the y-sweep
-  // (with the max-wave update) reads 1-cur and writes cur
+  // reads 1-cur and writes cur; the max-wave update in the y-sweep (fused
+  // set) or the previous end state folded in by the x-sweep (fold set)
   std::vector<SweepArgs> args(2 * (size_t)n), fold(2 * (size_t)n);
   std::vector<int> off(2 * ((size_t)n + 1), 0), gx(2 * (size_t)n, 0);
   for (int k = 0; k < n; ++k) {
