@@ -310,14 +310,21 @@ def run_ours(args):
     # ---- roofline of the dominant kernel ---------------------------------------
     peak, peak_kind = _peaks()
     kx, ky = prof["x_ms"], prof["y_ms"]
-    if ky >= kx:
-        kname, kms, bpc = "y-sweep: fast_kernel<1, true, false>", ky, B_Y
+    if args.sweep == "staged":  # the max-wave update stays in the y-sweep
+        names = ("x-sweep: staged_x", "y-sweep + max-wave: staged_y")
+        bx, by = B_Y, B_X
     else:
-        kname, kms, bpc = "x-sweep + max-wave of the previous step's end state: fast_kernel<0, true, false>", kx, B_X
+        names = ("x-sweep + max-wave of the previous step's end state: fast_kernel<0, true, false>",
+                 "y-sweep: fast_kernel<1, true, false>")
+        bx, by = B_X, B_Y
+    if ky >= kx:
+        kname, kms, bpc = names[1], ky, by
+    else:
+        kname, kms, bpc = names[0], kx, bx
     achieved = bpc * cells / (kms / 1e3) / 1e9 if kms > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and args.sweep == "tiled":
         with open(tp) as f:
             tr = json.load(f)
         key = "y" if ky >= kx else "x"
