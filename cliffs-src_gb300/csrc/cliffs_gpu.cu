@@ -2002,6 +2002,7 @@ int cliffs_gpu_status(cliffs_ctx* c, uint32_t* flags) {
 
 int cliffs_gpu_set_sweep_kernel(cliffs_ctx* c, int32_t kind) {
   if (!c || (kind != CLIFFS_SWEEP_TILED && kind != CLIFFS_SWEEP_STAGED)) return CLIFFS_ERR_ARG;
+  if (c->have_state) RET(max_sync(c));  // the staged kernels fold nothing in
   c->sweep_kind = kind;
   return CLIFFS_OK;
 }

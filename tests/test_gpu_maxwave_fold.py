@@ -9,7 +9,7 @@ every kind of call that touches them:
   the first step from the initial state (nothing folded in), reads in the
   middle of a run, graph replays after a read, single sweeps, a state
   uploaded in mid-run, an instantaneous and a rising source, the runup
-  measure and an explicit maxwave_update."""
+  measure, an explicit maxwave_update, and a switch of kernels in mid-run."""
 import importlib
 
 import numpy as np
@@ -63,6 +63,12 @@ def test_fold_equals_update_in_the_y_sweep():
         lambda g: g.runup(),
         lambda g: g.add_source(c["xcrd"], c["ycrd"], **src, rise_time=4 * c["dt"]),
         lambda g: g.step(21),
+        None,
+        lambda g: g.step(9),
+        lambda g: g.set_sweep_kernel(cg.STAGED),  # a pending end state, then the other kernels
+        lambda g: g.step(12),
+        lambda g: g.set_sweep_kernel(cg.TILED),
+        lambda g: g.step(12),
         None,
     ]
     for f in calls:
