@@ -299,6 +299,17 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
   size_t q0 = 0;
   if (DIR == 0) {
     q0 = cidx<0>(min(L, A.nlines), i0, A.pitch);
+    // the halo cells of the warp's ends first, so that their loads do not
+    // wait behind the shuffles of the window
+    const bool hl = active && lane == 0 && i0 > 1, hr = active && lane == 31 && i0 + 4 <= n;
+    float hd = 0.f, he = 0.f, hu = 0.f, hv = 0.f;
+    if (hl || hr) {
+      const size_t qh = hl ? q0 - 1 : q0 + 4;
+      hd = __ldg(A.dep + qh);
+      he = ld_state<COH>(A.srf + qh);
+      hu = ld_state<COH>(A.xu + qh);
+      hv = ld_state<COH>(A.yv + qh);
+    }
     float4 D4 = make_float4(0, 0, 0, 0), E4 = D4, X4 = D4, Y4 = D4, H4 = D4, V4 = D4;
     if (active) {
       D4 = __ldg(reinterpret_cast<const float4*>(A.dep + q0));
@@ -339,17 +350,17 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
     e[5] = __shfl_down_sync(0xffffffffu, E4.x, 1);
     u[5] = __shfl_down_sync(0xffffffffu, X4.x, 1);
     v[5] = __shfl_down_sync(0xffffffffu, Y4.x, 1);
-    if (active && lane == 0 && i0 > 1) {
-      d[0] = __ldg(A.dep + q0 - 1);
-      e[0] = ld_state<COH>(A.srf + q0 - 1);
-      u[0] = ld_state<COH>(A.xu + q0 - 1);
-      v[0] = ld_state<COH>(A.yv + q0 - 1);
+    if (hl) {
+      d[0] = hd;
+      e[0] = he;
+      u[0] = hu;
+      v[0] = hv;
     }
-    if (active && lane == 31 && i0 + 4 <= n) {
-      d[5] = __ldg(A.dep + q0 + 4);
-      e[5] = ld_state<COH>(A.srf + q0 + 4);
-      u[5] = ld_state<COH>(A.xu + q0 + 4);
-      v[5] = ld_state<COH>(A.yv + q0 + 4);
+    if (hr) {
+      d[5] = hd;
+      e[5] = he;
+      u[5] = hu;
+      v[5] = hv;
     }
   } else {
 #pragma unroll
