@@ -357,10 +357,18 @@ class GpuGrid:
         _chk(self.L.cliffs_gpu_upload_state(self.h, _p(_f64(cel, s)), _p(_f64(u, s)), _p(_f64(v, s))),
              "upload_state")
 
-    def download_state(self):
-        cel = np.empty((self.ny, self.nx))
-        u = np.empty((self.ny, self.nx))
-        v = np.empty((self.ny, self.nx))
+    def _out(self, out, k, dtype):
+        if out is None:
+            return np.empty((self.ny, self.nx), dtype)
+        a = out[k]
+        if a.shape != (self.ny, self.nx) or a.dtype != dtype or not a.flags.c_contiguous:
+            raise ValueError(f"output {k}: expected C-contiguous {dtype} of shape {(self.ny, self.nx)}")
+        return a
+
+    def download_state(self, out=None):
+        """(cel, u, v) in FP64; out: three arrays to fill instead of new ones
+        (a caller's own arrays, as the Fortran driver keeps them)."""
+        cel, u, v = (self._out(out, k, np.float64) for k in range(3))
         _chk(self.L.cliffs_gpu_download_state(self.h, _p(cel), _p(u), _p(v)), "download_state")
         return cel, u, v
 
@@ -427,9 +435,10 @@ class GpuGrid:
         return r, f.value
 
     # -- outputs ----------------------------------------------------------------
-    def maxwave(self):
-        me = np.empty((self.ny, self.nx), np.float32)
-        mv = np.empty((self.ny, self.nx), np.float32)
+    def maxwave(self, out=None):
+        """(MaxE, MaxV) as output_maxwave.f writes them; out: two float32
+        arrays to fill instead of new ones."""
+        me, mv = (self._out(out, k, np.float32) for k in range(2))
         _chk(self.L.cliffs_gpu_get_maxwave(self.h, _p(me, _fp), _p(mv, _fp)), "get_maxwave")
         return me, mv
 

@@ -79,6 +79,17 @@ def test_fold_equals_update_in_the_y_sweep():
     for x, y in zip(a.download_state(), b.download_state()):
         assert np.array_equal(x, y)
     _same_max(a, b)
+    # the caller's own output arrays are filled in place
+    st = [np.full((a.ny, a.nx), 7.0) for _ in range(3)]
+    mw = [np.full((a.ny, a.nx), 7.0, np.float32) for _ in range(2)]
+    assert all(x is y for x, y in zip(a.download_state(out=st), st))
+    assert all(x is y for x, y in zip(a.maxwave(out=mw), mw))
+    for x, y in zip(st, b.download_state()):
+        assert np.array_equal(x, y)
+    for x, y in zip(mw, b.maxwave()):
+        assert np.array_equal(x, y)
+    with pytest.raises(ValueError):
+        a.maxwave(out=[np.zeros((a.ny, a.nx))] * 2)  # float64 where float32 is due
     assert a.status()[0] == 0 and b.status()[0] == 0
     a.close()
     b.close()
