@@ -52,6 +52,23 @@ def _env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(x, dist):
+    """The largest of every rank's x (seconds): the job's time is its slowest
+    replica's.  dist is torch.distributed with a process group, or None."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, cells, steps, seconds):
+    """Whole-job Mcell-updates/s: every replica's cells and steps over the
+    slowest replica's time."""
+    return world * cells * steps / seconds / 1e6
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -226,13 +243,10 @@ def run_e2e(pkg, case, args, barrier, dist, world):
     g2.wait(last)
     t_e2e = time.perf_counter() - t0
     g2.close()
-    if dist is not None:
-        t = torch.tensor([t_e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e, dist)
     h2d = cells * 8 * 4 + (nx + ny) * 8 * 3 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), metrics, gauge indices
     d2h = cells * 8 * 3 + cells * 4 * 2 + nrec * 64 * 3 * 8
-    return {"value": round(world * cells * args.steps / t_e2e / 1e6, 3), "unit": "Mcell-updates/s",
+    return {"value": round(job_value(world, cells, args.steps, t_e2e), 3), "unit": "Mcell-updates/s",
             "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps)}
 
 
@@ -297,13 +311,8 @@ def run_ours(args):
         raise RuntimeError(f"solver status {r} flags {flags}")
     g.close()
     t_local = ms / 1e3
-    if dist is not None:
-        t = torch.tensor([t_local], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    else:
-        t_max = t_local
-    value = world * cells * args.steps / t_max / 1e6
+    t_max = max_over_ranks(t_local, dist)
+    value = job_value(world, cells, args.steps, t_max)
 
     # ---- end to end through the C ABI with host buffers (e2e) -----------------
     e2e = None
