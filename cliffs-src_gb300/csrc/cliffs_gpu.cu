@@ -163,6 +163,20 @@ struct cliffs_ctx {
   // fresh: the state is not the end of a step (initial, uploaded, a source
   // added, after a single sweep) and is never folded in.
   bool max_pending = false, max_fresh = true;
+  // forced steps from a graph: per-step edge tables of graph_k steps (ring),
+  // the cursor's record and weight of each step, and the graph itself
+  float *ring_x = nullptr, *ring_y = nullptr;
+  int32_t* ring_irec = nullptr;
+  double* ring_cc = nullptr;
+  int ring_k = 0;
+  // pinned host slots for the cursor of the next chunks, and an event per slot
+  // that marks its copy done
+  static constexpr int kRingSlots = 4;
+  char* ring_host = nullptr;
+  cudaEvent_t ring_ev[kRingSlots] = {};
+  int ring_slot = 0;
+  cudaGraphExec_t fgraph = nullptr;
+  int fgraph_k = 0, fgraph_cur = -1, fgraph_blk = 0, fgraph_wy = 0, fgraph_kind = -1;
   // asynchronous outputs: a copy stream and a ring of slots; ticket k uses
   // slot k % kOutSlots.  Gauge indices stay on the device between calls.
   cudaStream_t cpy = nullptr;
@@ -647,14 +661,16 @@ cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArg
 enum { MAXM_NONE = 0, MAXM_OUT = 1, MAXM_IN = 2 };
 
 int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double* fB,
-                 int flen, int irec, double cc) {
+                 int flen, int irec, double cc, const float* pre = nullptr) {
   SweepArgs A = sweep_args(c, iu, maxm == MAXM_OUT, c->cur);
   if (maxm == MAXM_IN && iu == 1) {
     A.hmax_in = c->hmax;
     A.velmax_in = c->velmax;
   }
   const int o = 1 - c->cur;
-  if (fA || fB) {
+  if (pre) {  // this step's edge table, already in the ring
+    A.edges = pre;
+  } else if (fA || fB) {
     float* eb = iu == 1 ? c->edge_x : c->edge_y;
     const int nl = iu == 1 ? c->ny : c->nx;
     ++c->launches;
@@ -945,7 +961,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
                   c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
                   c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y,
-                  c->rise_q};
+                  c->rise_q, c->ring_x, c->ring_y, c->ring_irec, c->ring_cc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& n : c->nests) {
@@ -964,6 +980,10 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   if (c->g_ij) cudaFree(c->g_ij);
   if (c->cpy) cudaStreamDestroy(c->cpy);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
+  if (c->ring_host) cudaFreeHost(c->ring_host);
+  for (cudaEvent_t e : c->ring_ev)
+    if (e) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
 }
@@ -1345,6 +1365,10 @@ int cliffs_gpu_set_feed(cliffs_ctx* c, int32_t nt, const double* tinput, const d
                         int32_t freeze) {
   if (!c) return CLIFFS_ERR_ARG;
   CK(cudaStreamSynchronize(c->stream));
+  if (c->fgraph) {  // captured with the records being replaced
+    cudaGraphExecDestroy(c->fgraph);
+    c->fgraph = nullptr;
+  }
   double** bufs[] = {&c->fw, &c->fe, &c->fs, &c->fn};
   for (double** b : bufs)
     if (*b) {
@@ -1422,6 +1446,120 @@ int cliffs_gpu_feed_start(cliffs_ctx* c, double cuke) {
     if (wave >= cuke) break;
   }
   return it >= nt ? -1 : it;
+}
+
+// Forced steps of a two-dimensional grid from a CUDA graph of graph_k steps:
+// the host advances the forcing record cursor for the chunk exactly as
+// one_step does, copies each step's record and weight to the device, and the
+// graph computes all the chunk's edge tables in one kernel (edges_ring_kernel)
+// before its 2 * graph_k sweeps, each reading its own table.  A chunk in
+// which the forcing ends is left to one_step.
+static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done, int* done_out) {
+  const int k = c->graph_k;
+  *done_out = 0;
+  if (!c->feed_on || k < 2 || nsteps < k || c->prof || c->rise_on || c->max_fresh || !c->xrun || !c->yrun)
+    return CLIFFS_OK;
+  if (c->ring_k != k) {
+    for (void* p : {(void*)c->ring_x, (void*)c->ring_y, (void*)c->ring_irec, (void*)c->ring_cc})
+      if (p) cudaFree(p);
+    c->ring_x = c->ring_y = nullptr;
+    c->ring_irec = nullptr;
+    c->ring_cc = nullptr;
+    c->ring_k = 0;
+    if (c->ring_host) {
+      CK(cudaStreamSynchronize(c->stream));  // no copy from the old slots is pending
+      cudaFreeHost(c->ring_host);
+      c->ring_host = nullptr;
+    }
+    if (dalloc(&c->ring_x, (size_t)k * 6 * c->ny) || dalloc(&c->ring_y, (size_t)k * 6 * c->nx) ||
+        dalloc(&c->ring_irec, (size_t)k) || dalloc(&c->ring_cc, (size_t)k) ||
+        cudaHostAlloc((void**)&c->ring_host, (size_t)cliffs_ctx::kRingSlots * k * 16, cudaHostAllocDefault) !=
+            cudaSuccess)
+      return CLIFFS_ERR_NOMEM;
+    for (cudaEvent_t& e : c->ring_ev)
+      if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return CLIFFS_ERR_CUDA;
+    c->ring_k = k;
+    if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
+    c->fgraph = nullptr;
+  }
+  if (!c->fgraph || c->fgraph_k != k || c->fgraph_cur != c->cur || c->fgraph_blk != c->blk_x ||
+      c->fgraph_wy != c->warps_y || c->fgraph_kind != c->sweep_kind) {
+    if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
+    c->fgraph = nullptr;
+    const int64_t launches = c->launches;
+    const unsigned sweeps = c->sweeps;
+    const bool pending = c->max_pending, fresh = c->max_fresh;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const long long work = (long long)(c->nx + c->ny) * k;
+    edges_ring_kernel<<<(unsigned)((work + 127) / 128), 128, 0, c->stream>>>(
+        k, c->nx, c->ny, c->fw, c->fe, c->fs, c->fn, c->ring_irec, c->ring_cc, c->ring_x, c->ring_y);
+    int r = cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+    for (int s = 0; s < k && !r; ++s) {  // every step alike: the state is not fresh here
+      int mx, my;
+      step_modes(c, &mx, &my);
+      r = launch_sweep(c, 1, mx, c->fw, c->fe, c->ny, 2, 0.0, c->ring_x + (size_t)s * 6 * c->ny);
+      if (!r) r = launch_sweep(c, 2, my, c->fs, c->fn, c->nx, 2, 0.0, c->ring_y + (size_t)s * 6 * c->nx);
+      step_done(c);
+    }
+    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    c->launches = launches;  // captured, not launched
+    c->sweeps = sweeps;
+    c->max_pending = pending;
+    c->max_fresh = fresh;
+    if (r || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return r ? r : CLIFFS_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->fgraph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return CLIFFS_ERR_CUDA;
+    c->fgraph_k = k;
+    c->fgraph_cur = c->cur;
+    c->fgraph_blk = c->blk_x;
+    c->fgraph_wy = c->warps_y;
+    c->fgraph_kind = c->sweep_kind;
+  }
+  int done = 0;
+  while (done + k <= nsteps) {
+    // a free pinned slot: its previous copy has completed
+    const int slot = c->ring_slot;
+    CK(cudaEventSynchronize(c->ring_ev[slot]));
+    double* hcc = reinterpret_cast<double*>(c->ring_host + (size_t)slot * k * 16);
+    int32_t* hir = reinterpret_cast<int32_t*>(c->ring_host + (size_t)slot * k * 16 + (size_t)k * 8);
+    // the cursor of cliffs_main.f:305-315 over the chunk, as one_step runs it
+    double tt = *t;
+    int ir = c->irec;
+    bool regular = true;
+    for (int s = 0; s < k && regular; ++s) {
+      tt = tt + c->dt;
+      while (tt >= c->tinput[ir - 1]) {
+        if (ir == c->nt) {
+          regular = false;
+          break;
+        }
+        ir = ir + 1;
+      }
+      if (!regular) break;
+      hir[s] = ir;
+      hcc[s] = (c->tinput[ir - 1] - tt) / (c->tinput[ir - 1] - c->tinput[ir - 2]);
+    }
+    if (!regular) break;  // the forcing ends in this chunk
+    CK(cudaMemcpyAsync(c->ring_irec, hir, (size_t)k * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->ring_cc, hcc, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaEventRecord(c->ring_ev[slot], c->stream));
+    c->ring_slot = (slot + 1) % cliffs_ctx::kRingSlots;
+    CK(cudaGraphLaunch(c->fgraph, c->stream));
+    c->launches += 1 + 2 * (int64_t)k;
+    c->sweeps += 2u * (unsigned)k;
+    *t = tt;
+    c->irec = ir;
+    for (int s = 0; s < k; ++s) step_done(c);
+    if (steps_done) *steps_done += k;
+    done += k;
+  }
+  *done_out = done;
+  return CLIFFS_OK;
 }
 
 // Plain steps (no forcing, profiling or rising source) from a CUDA graph of
@@ -1539,6 +1677,10 @@ int cliffs_gpu_step(cliffs_ctx* c, int32_t nsteps, double* t, int32_t* steps_don
     done = 1;
     if (steps_done) *steps_done = 1;
   }
+  int fdone = 0;
+  const int fr = forced_graph_steps(c, nsteps - done, t, steps_done, &fdone);
+  if (fr) return fr;
+  done += fdone;
   int gdone = 0;
   const int gr = graph_steps(c, nsteps - done, t, steps_done, &gdone);
   if (gr) return gr;

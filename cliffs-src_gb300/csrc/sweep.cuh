@@ -557,10 +557,9 @@ __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {
 // are the records of the low and high edge, (len,3,nt); irec is 1-based with
 // tinput(irec-1) <= t < tinput(irec); cc the weight of record irec-1.  cn is
 // the normal velocity component (iu-1 in the reference), ct the tangential.
-__global__ void edges_kernel(int nlines, int len, const double* __restrict__ recA, const double* __restrict__ recB,
-                             int irec, double cc, int cn, int ct, float* out) {
-  const int L = blockIdx.x * blockDim.x + threadIdx.x;
-  if (L >= nlines) return;
+__device__ __forceinline__ void edges_line(int L, int len, const double* __restrict__ recA,
+                                           const double* __restrict__ recB, int irec, double cc, int cn, int ct,
+                                           float* out) {
   const size_t r0 = (size_t)(irec - 2) * 3 * (size_t)len;
   const size_t r1 = (size_t)(irec - 1) * 3 * (size_t)len;
   const int comp[3] = {cn, ct, 2};
@@ -577,6 +576,32 @@ __global__ void edges_kernel(int nlines, int len, const double* __restrict__ rec
       out[(size_t)L * 6 + side * 3 + k] = v;
     }
   }
+}
+
+__global__ void edges_kernel(int nlines, int len, const double* __restrict__ recA, const double* __restrict__ recB,
+                             int irec, double cc, int cn, int ct, float* out) {
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nlines) return;
+  edges_line(L, len, recA, recB, irec, cc, cn, ct, out);
+}
+
+// The edge tables of k forced steps at once, for replay from a graph: step s
+// of the x-sweep (ny lines, west/east records) into ring_x + s*6*ny, of the
+// y-sweep (nx lines, south/north) into ring_y + s*6*nx, with record irec[s]
+// and weight cc[s] as the time loop's cursor gives them.  A thread per line
+// and step; the values are those edges_kernel writes.
+__global__ void edges_ring_kernel(int k, int nx, int ny, const double* __restrict__ fw, const double* __restrict__ fe,
+                                  const double* __restrict__ fs, const double* __restrict__ fn,
+                                  const int* __restrict__ irec, const double* __restrict__ cc, float* ring_x,
+                                  float* ring_y) {
+  const int per = nx + ny;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)per * k) return;
+  const int s = (int)(t / per), L = (int)(t % per);
+  if (L < ny)
+    edges_line(L, ny, fw, fe, irec[s], cc[s], 0, 1, ring_x + (size_t)s * 6 * ny);
+  else
+    edges_line(L - ny, nx, fs, fn, irec[s], cc[s], 1, 0, ring_y + (size_t)s * 6 * nx);
 }
 
 }  // namespace cliffs

@@ -109,8 +109,9 @@ def run_level(case, source, t_end, feed=None, child=None, cuke=0.001, bndout=3, 
     nest = g.nest_add(nest_tables(case["xcrd"], case["ycrd"], child["xcrd"], child["ycrd"])) if child else None
     total = max(0, int(np.floor((t_end - t0) / case["dt"] + 1e-9)))
     step = bndout if nest is not None else gout
-    if feed is None and step >= 2:
-        g.set_graph_steps(min(step, 16))  # plain steps between outputs replay from graphs
+    if step >= 2:
+        # the steps between outputs replay from graphs, forced or not
+        g.set_graph_steps(min(step, 16))
     I, J = case["gauges"]
     ng = len(I)
     n_g = total // gout + 1
