@@ -274,8 +274,11 @@ int cliffs_gpu_profile_read(cliffs_ctx *ctx, double *x_ms, int64_t *x_count,
 int cliffs_gpu_launch_count(cliffs_ctx *ctx, int64_t *n);
 
 /* Steps captured in one CUDA graph by cliffs_gpu_step (default 16; 0 or 1:
- * no graph).  Plain steps (no boundary forcing, profiling or rising source)
- * are replayed from the graph, one launch per k steps. */
+ * no graph).  Steps without profiling or a rising source are replayed from
+ * a graph, one launch per k steps.  With boundary forcing (two-dimensional
+ * grids) the graph first fills the k steps' edge tables in one kernel, from
+ * the records and weights the library's cursor gives each step; a chunk in
+ * which the forcing ends runs step by step. */
 int cliffs_gpu_set_graph_steps(cliffs_ctx *ctx, int32_t k);
 
 /* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
