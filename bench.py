@@ -158,15 +158,17 @@ def workload(name="shelf2048"):
     raise ValueError(f"unknown workload {name}")
 
 
-def config_dict(case, impl_note):
+def config_dict(case):
+    """The workload; the same for both arms (the implementation is named
+    outside it, under "implementation")."""
     ny, nx = case["dep"].shape
     return {"workload": case["label"], "grid": [nx, ny], "dt_s": round(case["dt"], 6), "ground_m": case["ground"],
             "crough": case["crough"], "source": case["source_label"],
             "l2": f"working set ~{9 * nx * ny * 4 / 1e6:.0f} MB per step > 129 MB L2; no flush",
-            "parallelism": "replicas only (one independent grid per GPU)", "impl": impl_note}
+            "parallelism": "replicas only (one independent grid per GPU)"}
 
 
-def cpu_baseline(case, steps, threads, f32=True):
+def cpu_baseline(case, steps, threads, f32=True, warmup=1):
     """The CPU restatement (oracle) timed on a bounded sample of the workload;
     with f32, also the same source built in FP32 (like for like with the FP32
     GPU path), reported under "f32"."""
@@ -176,15 +178,15 @@ def cpu_baseline(case, steps, threads, f32=True):
     cells = case["dep"].size
 
     def timed(m):
-        m.step(1)  # warm-up
+        m.step(warmup)
         t0 = time.perf_counter()
         m.step(steps)
         return cells * steps / (time.perf_counter() - t0) / 1e6
 
     val = timed(oracle_model(case))
     line = {"value": round(val, 3), "unit": "Mcell-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{case['dep'].shape[1]}x{case['dep'].shape[0]} grid, {steps} time steps after 1 warm-up step, "
-                      f"OpenMP over lines ({threads} threads), FP64"}
+            "sample": f"{case['dep'].shape[1]}x{case['dep'].shape[0]} grid, {steps} time steps after {warmup} "
+                      f"warm-up step{'s' if warmup != 1 else ''}, OpenMP over lines ({threads} threads), FP64"}
     if f32:
         line["f32"] = {"value": round(timed(oracle_model32(case)), 3), "unit": "Mcell-updates/s",
                        "sample": "the same steps with the same source built in FP32 (orc_real = float)"}
@@ -200,13 +202,17 @@ def run_reference(args):
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle  # noqa: F401  (builds/loads the CPU restatement)
     case = workload(args.workload)
+    # a bounded sample: at most 300 timed steps after at most 50 warm-up steps
+    # (~28 ms per step on 16 cores)
     steps = max(1, min(args.steps, 300))
-    cb = cpu_baseline(case, steps, threads, f32=False)
+    warm = max(1, min(args.warmup, 50))
+    cb = cpu_baseline(case, steps, threads, f32=False, warmup=warm)
     line = {"metric": "Mcell-updates/s", "value": cb["value"], "unit": "Mcell-updates/s",
-            "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
             "ms_per_step": round(1e3 * case["dep"].size / (cb["value"] * 1e6), 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(case, "CPU restatement of cliffs.f + cliffs_main.f time loop"),
+            "config": config_dict(case),
+            "implementation": "CPU restatement of cliffs.f + cliffs_main.f time loop (oracle, OpenMP)",
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "Mcell-updates/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -215,39 +221,52 @@ def run_reference(args):
 
 
 def run_e2e(pkg, case, args, barrier, dist, world):
-    """Steps through the public API from host buffers: upload, step, gauge
-    records every 10 steps (asynchronous outputs into pinned host memory,
-    cliffs_gpu_get_gauges_async), final state and max-wave fields back to the
-    host."""
+    """Steps through the public API from host buffers: create the grid from
+    the FP64 bathymetry and metrics, upload the initial state, step, gauge
+    records every 10 steps (asynchronous outputs, cliffs_gpu_get_gauges_async),
+    final state and max-wave fields back to the host.  The driver's arrays
+    (inputs read from its files, outputs it writes) are pinned host memory
+    (cliffs_gpu_host_alloc), allocated and filled before the clock starts, as
+    a driver that keeps its module arrays there does."""
     import numpy as np
-    import torch
 
     cells = case["dep"].size
     ny, nx = case["dep"].shape
     I, J = case["gauges"]
     nrec = (args.steps + 9) // 10
-    rec = pkg.cliffs_gpu.pinned((nrec, 3, len(I)))  # allocated before the clock starts, as a driver would
-    # the driver's own state and max-wave arrays, in use since its set-up
-    state = [np.full((ny, nx), 0.0) for _ in range(3)]
-    maxes = [np.full((ny, nx), 0.0, np.float32) for _ in range(2)]
+    pin = pkg.cliffs_gpu.pinned
+    rec = pin((nrec, 3, len(I)))
+    state = [pin((ny, nx)) for _ in range(3)]
+    maxes = [pin((ny, nx), np.float32) for _ in range(2)]
+    inputs = {}
+    for k in ("dep", "H0", "u0", "v0"):
+        inputs[k] = pin((ny, nx))
+        inputs[k][...] = case[k]
     barrier()
     t0 = time.perf_counter()
-    g2 = pkg.GpuGrid.from_case(case)  # metrics, create, initial state
+    dx, rs, dy, zeta = pkg.cliffs_gpu.metrics(case["xcrd"], case["ycrd"], case["cartesian"])
+    g2 = pkg.GpuGrid(inputs["dep"], dx=dx, row_scale=rs, dy=dy, zeta=zeta, ground=case["ground"],
+                     crough=case["crough"], dt=case["dt"])  # create: bathymetry H2D
+    g2.set_initial(inputs["H0"], inputs["u0"], inputs["v0"])  # initial state H2D
     g2.set_graph_steps(10)  # one graph per gauge interval
     last = -1
     for k, s0 in enumerate(range(0, args.steps, 10)):
         g2.step(min(10, args.steps - s0))
         last = g2.gauges_async(I, J, (rec[k, 0], rec[k, 1], rec[k, 2]))
-    cel, u, v = g2.download_state(out=state)
-    me, mv = g2.maxwave(out=maxes)
+    g2.download_state(out=state)
+    g2.maxwave(out=maxes)
     g2.wait(last)
     t_e2e = time.perf_counter() - t0
+    r, flags = g2.status()
     g2.close()
+    if r != 0:
+        raise RuntimeError(f"solver status {r} flags {flags} (end-to-end pass)")
     t_e2e = max_over_ranks(t_e2e, dist)
     h2d = cells * 8 * 4 + (nx + ny) * 8 * 3 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), metrics, gauge indices
     d2h = cells * 8 * 3 + cells * 4 * 2 + nrec * 64 * 3 * 8
     return {"value": round(job_value(world, cells, args.steps, t_e2e), 3), "unit": "Mcell-updates/s",
-            "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps)}
+            "h2d_bytes_per_step": int(h2d // args.steps), "d2h_bytes_per_step": int(d2h // args.steps),
+            "ms": round(t_e2e * 1e3, 3), "host_buffers": "pinned (cliffs_gpu_host_alloc)"}
 
 
 def run_ours(args):
@@ -278,6 +297,9 @@ def run_ours(args):
     g.set_stream(stream.cuda_stream)
     g.set_sweep_kernel(kind)
     g.step(args.warmup)
+    # the CUDA graphs the timed call replays are instantiated here, so the
+    # timed region launches them only
+    g.prepare_steps(args.steps)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -356,7 +378,7 @@ def run_ours(args):
                 "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": round(ms / args.steps, 5), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": config_dict(case, "CUDA sm_103a, include/cliffs_gpu.h"),
+                "config": config_dict(case), "implementation": "CUDA sm_103a, include/cliffs_gpu.h",
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
                 "gpu_launches": int(launches),
                 "hbm_frac_step": round(B_STEP * cells * args.steps / (ms / 1e3) / 1e9 / peak, 4)}

@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libcliffs_gpu.so")
 
 CLIFFS_OK = 0
 CLIFFS_FEED_ENDED = 1
+CLIFFS_WARN_CFL = 2
+CLIFFS_ST_NAN, CLIFFS_ST_STALL, CLIFFS_ST_CFL = 1, 2, 4
 GRAV = 9.800000190734863
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -198,7 +200,10 @@ SIGNATURES = {
                                  ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_set_graph_steps": ([_V, _I], ctypes.c_int),
+    "cliffs_gpu_prepare_steps": ([_V, _I], ctypes.c_int),
+    "cliffs_gpu_courant": ([_V, _dp], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
+    "cliffs_gpu_set_column_run": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_set_sweep_kernel": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
@@ -230,6 +235,7 @@ SIGNATURES = {
                          ctypes.c_int),
     "cliffs_mlp_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "cliffs_gpu_sweep_noalloc": ([_I, _I, _I, _I] + [_V] * 7 + [_D] * 5 + [_V], ctypes.c_int),
+    "cliffs_gpu_sweep_noalloc_status": ([_V, _V, _V], ctypes.c_int),
 }
 
 _lib = None
@@ -280,7 +286,7 @@ def _f64(a, shape=None):
 
 
 def metrics(xcrd, ycrd, cartesian):
-    """MasterGrid.f:237-268 through the library: (dx, row_scale, dy, zeta)."""
+    """MasterGrid.f:85-116 through the library: (dx, row_scale, dy, zeta)."""
     xcrd = _f64(xcrd)
     ycrd = _f64(ycrd)
     nx, ny = len(xcrd), len(ycrd)
@@ -434,6 +440,12 @@ class GpuGrid:
         r = self.L.cliffs_gpu_status(self.h, ctypes.byref(f))
         return r, f.value
 
+    def courant(self):
+        """The largest Courant number above 1 any sweep has read (0: none)."""
+        x = ctypes.c_double(0.0)
+        _chk(self.L.cliffs_gpu_courant(self.h, ctypes.byref(x)), "courant")
+        return x.value
+
     # -- outputs ----------------------------------------------------------------
     def maxwave(self, out=None):
         """(MaxE, MaxV) as output_maxwave.f writes them; out: two float32
@@ -554,8 +566,17 @@ class GpuGrid:
     def set_graph_steps(self, k):
         _chk(self.L.cliffs_gpu_set_graph_steps(self.h, int(k)), "set_graph_steps")
 
+    def prepare_steps(self, nsteps):
+        """Capture and instantiate the CUDA graphs a later step(nsteps) from
+        the current state replays, without running them."""
+        _chk(self.L.cliffs_gpu_prepare_steps(self.h, int(nsteps)), "prepare_steps")
+
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")
+
+    def set_column_run(self, cells):
+        """Cells per thread along a column in the tiled y-sweep (4..32)."""
+        _chk(self.L.cliffs_gpu_set_column_run(self.h, int(cells)), "set_column_run")
 
     def set_sweep_kernel(self, kind):
         """STAGED (persistent, TMA-staged windows; the default) or TILED."""

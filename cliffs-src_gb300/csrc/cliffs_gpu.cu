@@ -5,6 +5,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <initializer_list>
 #include <cmath>
 #include <cstdlib>
@@ -106,7 +108,11 @@ struct cliffs_ctx {
   float *hmax = nullptr, *velmax = nullptr;
   int cur = 0;
   int64_t launches = 0;  // kernels this context has launched
-  std::vector<double> dep64;  // the caller's FP64 depth, for the state conversions
+  // the caller's FP64 depth on the device (nx*ny, unpadded), for the state
+  // conversions, and a staging area of 3*nx*ny doubles for FP64 transfers,
+  // allocated at the first transfer and kept
+  double* dep64 = nullptr;
+  double* xfer = nullptr;
   // a source rising over time (cliffs_gpu_add_source): its full uplift, its
   // duration, the time since it was added and the fraction applied so far
   float* rise_q = nullptr;
@@ -135,6 +141,9 @@ struct cliffs_ctx {
   int* d_flag = nullptr;
   bool have_state = false;
   int blk_x = 128, warps_y = 4;
+  // y-sweep: groups of 4 cells per thread along a column (1: the fast
+  // kernel, one group; 2, 4, 8: column_kernel)
+  int col_groups = 1;
   // worklist of cells for the general kernel and one counter per sweep parity
   uint32_t* list = nullptr;
   uint32_t* cnt = nullptr;
@@ -144,8 +153,15 @@ struct cliffs_ctx {
   // steps of the sweep loop captured in a CUDA graph (cliffs_gpu_step);
   // valid for the tiling and state copy it was captured with
   int graph_k = 16;
-  cudaGraphExec_t graph = nullptr;
-  int graph_built = 0, graph_cur = -1, graph_blk = 0, graph_wy = 0;
+  // [0]: the graph of graph_k steps; [1..]: graphs of the shorter tails of
+  // step calls (their lengths differ), replaced oldest first
+  static constexpr int kPlainGraphs = 4;
+  struct PlainGraph {
+    cudaGraphExec_t exec = nullptr;
+    int len = 0, cur = -1, blk = 0, wy = 0, kind = -1;
+    int64_t used = 0;
+  } pgraph[kPlainGraphs];
+  int64_t pgraph_clock = 0;
   // sweep kernels (cliffs_gpu_set_sweep_kernel): the staged persistent pair
   // needs the y-sweep's tensor maps (one per state copy) and its grid size
   int sweep_kind = CLIFFS_SWEEP_TILED;
@@ -153,7 +169,6 @@ struct cliffs_ctx {
   CUtensorMap m_dep, m_srf[2], m_xu[2], m_yv[2], m_hmax, m_velmax;
   int grid_sx = 0, grid_sy = 0;  // resident blocks of staged_x / staged_y
   unsigned long long stage_ns = 2000000000ull;  // limit of one stage wait
-  int graph_kind = -1;
   // fast-kernel sweeps launched as programmatic dependents of the previous
   // sweep (CLIFFS_PDL=0 in the environment at context creation turns it off)
   bool pdl = true;
@@ -185,6 +200,8 @@ struct cliffs_ctx {
   int32_t* g_ij = nullptr;
   int g_n = 0, g_cap = 0;
   std::vector<int32_t> g_host;
+  // the largest Courant number above 1 that cliffs_gpu_status has cleared
+  double courant_seen = 0;
   bool prof = false;
   std::vector<ProfPair> prof_pending;
   double prof_ms[2] = {0, 0};
@@ -232,6 +249,14 @@ __global__ void k_init_state(int nx, int ny, int pitch, const double* __restrict
   srf[q] = (float)(land ? H : H - dep64[s]);  // surface state: H on land, eta at sea
   xu[q] = xv ? (float)xv[s] : 0.f;
   yv[q] = yvv ? (float)yvv[s] : 0.f;
+}
+
+// FP32 device depth (pitched, zero padding) from the FP64 depth.
+__global__ void k_dep_from64(int nx, int ny, int pitch, const double* __restrict__ dep64, float* dep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= pitch || j >= ny) return;
+  dep[(size_t)j * pitch + i] = i < nx ? (float)dep64[(size_t)j * nx + i] : 0.f;
 }
 
 __global__ void k_reset_max(int nx, int ny, int pitch, const float* __restrict__ dep, float* hmax,
@@ -401,7 +426,7 @@ __global__ void k_arrival(int ii1, int ii2, int kk1, int kk2, int pitch,
   if (hit) atomicOr(flag, 1);
 }
 
-// Edge records of feed_children_grid.f:197-325; one thread per child edge node.
+// Edge records of feed_children_grid.f:47-177; one thread per child edge node.
 __device__ __forceinline__ void feed_clm(int i, int k, int pitch, const float* dep,
                                          const float* srf, const float* xu, const float* yv,
                                          double cc, double hmin, double g, double out[3]) {
@@ -573,21 +598,25 @@ __global__ void k_add_surface(int nx, int ny, int pitch, const float* __restrict
   }
 }
 
-// The bottom moves from dep_old to dep_new under a standing water column
-// (cliffs_main.f:205-208): eta rises where it is sea before and after, the
-// depth stays where it is land before and after, and a cell changing sides
-// converts through its total depth.
-__global__ void k_move_bottom(int nx, int ny, int pitch, const float* __restrict__ dep_old,
-                              const float* __restrict__ dep_new, float* srf) {
+// The bottom rises by q (pitched FP32) under a standing water column
+// (cliffs_main.f:205-208).  The FP64 depth moves and the FP32 depth becomes
+// its rounding.  eta rises where it is sea before and after, the depth stays
+// where it is land before and after, and a cell changing sides converts
+// through its total depth.
+__global__ void k_move_bottom64(int nx, int ny, int pitch, const float* __restrict__ q, double* dep64,
+                                float* dep, float* srf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= nx || j >= ny) return;
-  const size_t k = (size_t)j * pitch + i;
-  const float d0 = dep_old[k], d1 = dep_new[k], s = srf[k];
+  const size_t k = (size_t)j * pitch + i, s = (size_t)j * nx + i;
+  const double d = dep64[s] - (double)q[k];
+  dep64[s] = d;
+  const float d0 = dep[k], d1 = (float)d, v = srf[k];
+  dep[k] = d1;
   if (d0 >= 0.f && d1 >= 0.f)
-    srf[k] = s + (d0 - d1);
+    srf[k] = v + (d0 - d1);
   else if (!(d0 < 0.f && d1 < 0.f))
-    srf[k] = state_from_depth(depth_of(s, d0), d1);
+    srf[k] = state_from_depth(depth_of(v, d0), d1);
 }
 
 // The arguments of one sweep reading state copy s and writing 1 - s.
@@ -638,6 +667,9 @@ SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
   return A;
 }
 
+// The y-sweep's launch shape, as a captured graph holds it.
+inline int ykey(const cliffs_ctx* c) { return c->warps_y | (c->col_groups << 8); }
+
 // One fast-kernel sweep on the context's stream, a programmatic dependent of
 // the previous launch when c->pdl is set.
 template <int DIR, bool MAXOUT>
@@ -653,6 +685,33 @@ cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArg
   cfg.attrs = at;
   cfg.numAttrs = c->pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT>, A);
+}
+
+// One column-run y-sweep (column_kernel, G groups of 4 cells per thread).
+template <bool MAXOUT, int G>
+cudaError_t launch_column_g(cliffs_ctx* c, const SweepArgs& A) {
+  const unsigned block = 32u * (unsigned)c->warps_y;
+  const int rows = c->warps_y * kCellsPerThread * G;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = (size_t)block * kCellsPerThread * G * sizeof(uint32_t);
+  cfg.stream = c->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = c->pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, column_kernel<true, MAXOUT, G>, A);
+}
+
+template <bool MAXOUT>
+cudaError_t launch_column(cliffs_ctx* c, const SweepArgs& A) {
+  switch (c->col_groups) {
+    case 2: return launch_column_g<MAXOUT, 2>(c, A);
+    case 4: return launch_column_g<MAXOUT, 4>(c, A);
+    default: return launch_column_g<MAXOUT, 8>(c, A);
+  }
 }
 
 // Max-wave handling of one sweep: none, the update with its outputs (the last
@@ -706,6 +765,12 @@ int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double
       CK((launch_fast<0, true>(c, grid, (unsigned)c->blk_x, A)));
     else
       CK((launch_fast<0, false>(c, grid, (unsigned)c->blk_x, A)));
+  } else if (c->col_groups > 1) {
+    ++c->launches;
+    if (maxm == MAXM_OUT)
+      CK(launch_column<true>(c, A));
+    else
+      CK(launch_column<false>(c, A));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
@@ -796,6 +861,7 @@ const char* cliffs_gpu_strerror(int code) {
   switch (code) {
     case CLIFFS_OK: return "ok";
     case CLIFFS_FEED_ENDED: return "boundary forcing ended (freeze)";
+    case CLIFFS_WARN_CFL: return "a sweep read a state with a Courant number above 1";
     case CLIFFS_ERR_ARG: return "invalid argument";
     case CLIFFS_ERR_CUDA: return "CUDA runtime error";
     case CLIFFS_ERR_NAN: return "non-finite value in the state";
@@ -810,7 +876,7 @@ const char* cliffs_gpu_strerror(int code) {
 int cliffs_gpu_metrics(int32_t nx, int32_t ny, int32_t cartesian, const double* xcrd,
                        const double* ycrd, double* dx, double* row_scale, double* dy, double* zeta) {
   if (nx < 1 || ny < 1 || !xcrd || !ycrd) return CLIFFS_ERR_ARG;
-  const double beta = kPi * kEarthR / 180.;  // MasterGrid.f:237
+  const double beta = kPi * kEarthR / 180.;  // MasterGrid.f:85
   if (nx > 2) {
     if (dx)
       for (int i = 0; i < nx - 1; ++i)
@@ -867,16 +933,17 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
       dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
       dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
-      dalloc(&c->status, 1) || dalloc(&c->d_flag, 1) || dalloc(&c->list, (size_t)c->nx * c->ny) ||
+      dalloc(&c->status, 2) || dalloc(&c->d_flag, 1) || dalloc(&c->list, (size_t)c->nx * c->ny) ||
       dalloc(&c->edge_x, (size_t)c->ny * 6) || dalloc(&c->edge_y, (size_t)c->nx * 6) ||
-      dalloc(&c->cnt, 2))
+      dalloc(&c->cnt, 2) || dalloc(&c->dep64, (size_t)c->nx * c->ny))
     return fail(CLIFFS_ERR_NOMEM);
-  // bathymetry, padded rows
-  c->dep64.assign(d->dep, d->dep + (size_t)c->nx * c->ny);
-  std::vector<float> h((size_t)c->pitch * c->ny, 0.f);
-  for (int j = 0; j < c->ny; ++j)
-    for (int i = 0; i < c->nx; ++i) h[(size_t)j * c->pitch + i] = (float)d->dep[(size_t)j * c->nx + i];
-  if (cudaMemcpy(c->dep, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+  // bathymetry: the FP64 depth as passed, and its rounding in padded rows
+  if (cudaMemcpyAsync(c->dep64, d->dep, (size_t)c->nx * c->ny * sizeof(double), cudaMemcpyHostToDevice,
+                      c->stream) != cudaSuccess)
+    return fail(CLIFFS_ERR_CUDA);
+  ++c->launches;
+  k_dep_from64<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep64, c->dep);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
   // geometry tables
   auto build_geo = [&](int n, const double* s, std::vector<float4>& geo, float& i1, float& in1) {
@@ -918,7 +985,7 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       cudaMemcpy(c->geo_y, gy.data(), gy.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->scl_y, sy.data(), sy.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->lscale, ls.data(), ls.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(c->status, 0, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(c->status, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(c->cnt, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
   if (!d->row_scale) {
@@ -961,7 +1028,7 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
                   c->hmax, c->velmax, c->list, c->cnt,
                   c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
                   c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y,
-                  c->rise_q, c->ring_x, c->ring_y, c->ring_irec, c->ring_cc};
+                  c->rise_q, c->ring_x, c->ring_y, c->ring_irec, c->ring_cc, c->dep64, c->xfer};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& n : c->nests) {
@@ -979,7 +1046,8 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   }
   if (c->g_ij) cudaFree(c->g_ij);
   if (c->cpy) cudaStreamDestroy(c->cpy);
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto& pg : c->pgraph)
+    if (pg.exec) cudaGraphExecDestroy(pg.exec);
   if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
   if (c->ring_host) cudaFreeHost(c->ring_host);
   for (cudaEvent_t e : c->ring_ev)
@@ -995,16 +1063,22 @@ int cliffs_gpu_set_stream(cliffs_ctx* c, void* stream) {
   return CLIFFS_OK;
 }
 
+// The FP64 transfer staging of a context: three nx*ny arrays of doubles.
+static int xfer_area(cliffs_ctx* c, double** out) {
+  if (!c->xfer && dalloc(&c->xfer, 3 * (size_t)c->nx * c->ny)) return CLIFFS_ERR_NOMEM;
+  *out = c->xfer;
+  return CLIFFS_OK;
+}
+
 static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const double* xv,
                          const double* yv, bool reset_max) {
   if (!c || !src) return CLIFFS_ERR_ARG;
   const size_t n = (size_t)c->nx * c->ny;
-  double *dsrc = nullptr, *dx = nullptr, *dy = nullptr, *dd = nullptr;
+  double* x = nullptr;
+  RET(xfer_area(c, &x));
+  double *dsrc = x, *dx = xv ? x + n : nullptr, *dy = yv ? x + 2 * n : nullptr;
   int r = CLIFFS_OK;
-  if (dalloc(&dsrc, n) || dalloc(&dd, n) || (xv && dalloc(&dx, n)) || (yv && dalloc(&dy, n))) r = CLIFFS_ERR_NOMEM;
-  if (!r && cudaMemcpyAsync(dsrc, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && cudaMemcpyAsync(dd, c->dep64.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
-    r = CLIFFS_ERR_CUDA;
+  if (cudaMemcpyAsync(dsrc, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && xv && cudaMemcpyAsync(dx, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && !reset_max && c->have_state) r = max_sync(c);  // the replaced state's pending end state
@@ -1014,7 +1088,7 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
     c->cur = 0;
     ++c->launches;
     k_init_state<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(
-        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, dd, c->srf[0], c->xu[0], c->yv[0], c->ground,
+        c->nx, c->ny, c->pitch, dsrc, is_cel, dx, dy, c->dep, c->dep64, c->srf[0], c->xu[0], c->yv[0], c->ground,
         kGrav);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
@@ -1023,11 +1097,8 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
     k_reset_max<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax);
     if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
+  // the caller's arrays are read before the call returns
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
-  cudaFree(dsrc);
-  if (dd) cudaFree(dd);
-  if (dx) cudaFree(dx);
-  if (dy) cudaFree(dy);
   if (!r) c->have_state = true;
   return r;
 }
@@ -1048,59 +1119,34 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   const size_t n = (size_t)c->nx * c->ny;
-  double *a = nullptr, *b = nullptr, *e = nullptr, *dd = nullptr;
+  double* x = nullptr;
+  RET(xfer_area(c, &x));
+  double *a = x, *b = x + n, *e = x + 2 * n;
   int r = CLIFFS_OK;
-  if (dalloc(&a, n) || dalloc(&b, n) || dalloc(&e, n) || dalloc(&dd, n)) r = CLIFFS_ERR_NOMEM;
-  if (!r && cudaMemcpyAsync(dd, c->dep64.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
-    r = CLIFFS_ERR_CUDA;
-  if (!r) {
-    ++c->launches;
-    k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dd,
-                                                          c->srf[c->cur], c->xu[c->cur], c->yv[c->cur], a,
-                                                          b, e, kGrav);
-    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
-  }
+  ++c->launches;
+  k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->dep64,
+                                                        c->srf[c->cur], c->xu[c->cur], c->yv[c->cur], a, b, e,
+                                                        kGrav);
+  if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && cel && cudaMemcpyAsync(cel, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && xv && cudaMemcpyAsync(xv, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && yv && cudaMemcpyAsync(yv, e, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
-  if (a) cudaFree(a);
-  if (b) cudaFree(b);
-  if (e) cudaFree(e);
-  if (dd) cudaFree(dd);
   return r;
 }
 
 namespace {
 
 // The bottom rises by q (device, pitched FP32) under the standing water
-// column (cliffs_main.f:205-208).  The FP64 depth the context keeps moves on
-// the host; the device depth becomes its rounding.  Synchronises.
+// column (cliffs_main.f:205-208): the FP64 depth the context keeps moves, the
+// FP32 depth becomes its rounding.  Synchronises.
 int move_bottom(cliffs_ctx* c, const float* q) {
-  const size_t cells = (size_t)c->pitch * c->ny;
-  std::vector<float> hq(cells), hd(cells, 0.f);
-  CK(cudaMemcpyAsync(hq.data(), q, cells * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  ++c->launches;
+  k_move_bottom64<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, q, c->dep64, c->dep,
+                                                              c->srf[c->cur]);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->stream));
-  for (int j = 0; j < c->ny; ++j)
-    for (int i = 0; i < c->nx; ++i) {
-      double& d = c->dep64[(size_t)j * c->nx + i];
-      d -= (double)hq[(size_t)j * c->pitch + i];
-      hd[(size_t)j * c->pitch + i] = (float)d;
-    }
-  float* dnew = nullptr;
-  if (dalloc(&dnew, cells)) return CLIFFS_ERR_NOMEM;
-  int r = CLIFFS_OK;
-  if (cudaMemcpyAsync(dnew, hd.data(), cells * sizeof(float), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r) {
-    ++c->launches;
-    k_move_bottom<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, dnew, c->srf[c->cur]);
-    if (cudaGetLastError() != cudaSuccess ||
-        cudaMemcpyAsync(c->dep, dnew, cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream))
-      r = CLIFFS_ERR_CUDA;
-  }
-  if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
-  cudaFree(dnew);
-  return r;
+  return CLIFFS_OK;
 }
 
 }  // namespace
@@ -1402,7 +1448,7 @@ int cliffs_gpu_set_feed(cliffs_ctx* c, int32_t nt, const double* tinput, const d
 }
 
 int cliffs_gpu_feed_start(cliffs_ctx* c, double cuke) {
-  // get_boundary_feed.f:473-496, on the host copy of the records
+  // get_boundary_feed.f:144-167, on the host copy of the records
   if (!c || c->nt < 2) return CLIFFS_ERR_ARG;
   const int nt = c->nt;
   std::vector<double> w, e, s, n;
@@ -1483,7 +1529,7 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
     c->fgraph = nullptr;
   }
   if (!c->fgraph || c->fgraph_k != k || c->fgraph_cur != c->cur || c->fgraph_blk != c->blk_x ||
-      c->fgraph_wy != c->warps_y || c->fgraph_kind != c->sweep_kind) {
+      c->fgraph_wy != ykey(c) || c->fgraph_kind != c->sweep_kind) {
     if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
     c->fgraph = nullptr;
     const int64_t launches = c->launches;
@@ -1517,7 +1563,7 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
     c->fgraph_k = k;
     c->fgraph_cur = c->cur;
     c->fgraph_blk = c->blk_x;
-    c->fgraph_wy = c->warps_y;
+    c->fgraph_wy = ykey(c);
     c->fgraph_kind = c->sweep_kind;
   }
   int done = 0;
@@ -1562,56 +1608,129 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
   return CLIFFS_OK;
 }
 
-// Plain steps (no forcing, profiling or rising source) from a CUDA graph of
-// graph_k steps: one launch per graph_k steps instead of two per step.  A
-// whole step leaves the state copy where it found it, so the graph's
-// arguments hold for every replay.
-static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done, int* done_out) {
-  const int k = c->graph_k;
-  *done_out = 0;
-  if (k < 2 || nsteps < k || c->feed_on || c->prof || c->rise_on) return CLIFFS_OK;
-  if (!c->graph || c->graph_built != k || c->graph_cur != c->cur || c->graph_blk != c->blk_x ||
-      c->graph_wy != c->warps_y || c->graph_kind != c->sweep_kind) {
-    if (c->graph) cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
-    const int64_t launches = c->launches;
-    const unsigned sweeps = c->sweeps;
-    cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int r = CLIFFS_OK;
-    for (int s = 0; s < k && !r; ++s) {  // every step alike: the state is not fresh here
-      int mx, my;
-      step_modes(c, &mx, &my);
-      if (c->xrun) r = launch_sweep(c, 1, mx, nullptr, nullptr, c->ny, 2, 0.0);
-      if (!r && c->yrun) r = launch_sweep(c, 2, my, nullptr, nullptr, c->nx, 2, 0.0);
-      step_done(c);
+// Plain steps (no forcing, profiling or rising source) from CUDA graphs: one
+// launch per graph_k steps instead of two per step, and the remaining steps
+// of a call (at least 2) from a graph of their own length.  A whole step
+// leaves the state copy where it found it, so a graph's arguments hold for
+// every replay.  Every captured step folds the previous step's end state
+// into the max-wave fields (the state is not fresh).
+static bool plain_graph_valid(const cliffs_ctx* c, const cliffs_ctx::PlainGraph& pg, int len) {
+  return pg.exec && pg.len == len && pg.cur == c->cur && pg.blk == c->blk_x && pg.wy == ykey(c) &&
+         pg.kind == c->sweep_kind;
+}
+
+static int plain_graph(cliffs_ctx* c, int len, cliffs_ctx::PlainGraph** out) {
+  *out = nullptr;
+  const bool full = len == c->graph_k;
+  int slot = 0;
+  if (!full) {  // a tail: the slot that holds this length, else the oldest
+    slot = 1;
+    for (int s = 1; s < cliffs_ctx::kPlainGraphs; ++s) {
+      if (plain_graph_valid(c, c->pgraph[s], len)) {
+        slot = s;
+        break;
+      }
+      if (c->pgraph[s].used < c->pgraph[slot].used) slot = s;
     }
-    const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    c->launches = launches;  // captured, not launched
-    c->sweeps = sweeps;
-    if (r || e != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return r ? r : CLIFFS_ERR_CUDA;
-    }
-    const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (ie != cudaSuccess) return CLIFFS_ERR_CUDA;
-    c->graph_built = k;
-    c->graph_cur = c->cur;
-    c->graph_blk = c->blk_x;
-    c->graph_wy = c->warps_y;
-    c->graph_kind = c->sweep_kind;
   }
+  cliffs_ctx::PlainGraph& pg = c->pgraph[slot];
+  pg.used = ++c->pgraph_clock;
+  if (plain_graph_valid(c, pg, len)) {
+    *out = &pg;
+    return CLIFFS_OK;
+  }
+  if (pg.exec) cudaGraphExecDestroy(pg.exec);
+  pg = cliffs_ctx::PlainGraph{};
+  pg.used = c->pgraph_clock;
+  const int64_t launches = c->launches;
+  const unsigned sweeps = c->sweeps;
+  const bool fresh = c->max_fresh, pending = c->max_pending;
+  const int cur = c->cur;
+  c->max_fresh = false;  // every captured step folds in the previous one
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int r = CLIFFS_OK;
+  for (int s = 0; s < len && !r; ++s) {
+    int mx, my;
+    step_modes(c, &mx, &my);
+    if (c->xrun) r = launch_sweep(c, 1, mx, nullptr, nullptr, c->ny, 2, 0.0);
+    if (!r && c->yrun) r = launch_sweep(c, 2, my, nullptr, nullptr, c->nx, 2, 0.0);
+    step_done(c);
+  }
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  // captured, not launched: the bookkeeping is the caller's, per replay
+  c->launches = launches;
+  c->sweeps = sweeps;
+  c->max_fresh = fresh;
+  c->max_pending = pending;
+  c->cur = cur;
+  if (r || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return r ? r : CLIFFS_ERR_CUDA;
+  }
+  const cudaError_t ie = cudaGraphInstantiate(&pg.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    pg.exec = nullptr;
+    return CLIFFS_ERR_CUDA;
+  }
+  pg.len = len;
+  pg.cur = c->cur;
+  pg.blk = c->blk_x;
+  pg.wy = ykey(c);
+  pg.kind = c->sweep_kind;
+  *out = &pg;
+  return CLIFFS_OK;
+}
+
+static bool plain_graphs_apply(const cliffs_ctx* c) {
+  return c->graph_k >= 2 && !c->feed_on && !c->prof && !c->rise_on;
+}
+
+// Steps of the next graph for `remaining` steps: graph_k, or the rest; a
+// one-dimensional grid (one sweep per step) takes an even count, so that a
+// graph ends on the state copy it started from.  0: none (run directly).
+static int plain_graph_len(const cliffs_ctx* c, int remaining) {
+  const int per = (c->xrun ? 1 : 0) + (c->yrun ? 1 : 0);
+  int len = std::min(c->graph_k, remaining);
+  if ((per * len) & 1) len -= 1;
+  return len >= 2 ? len : 0;
+}
+
+static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done, int* done_out) {
+  *done_out = 0;
+  if (!plain_graphs_apply(c) || nsteps < 2) return CLIFFS_OK;
   const int per = (c->xrun ? 1 : 0) + (c->yrun ? 1 : 0);
   int done = 0;
-  for (; done + k <= nsteps; done += k) {
-    CK(cudaGraphLaunch(c->graph, c->stream));
-    c->launches += (int64_t)per * k;
-    c->sweeps += (unsigned)(per * k);
-    for (int s = 0; s < k; ++s) *t = *t + c->dt;
-    if (steps_done) *steps_done += k;
+  for (int len; (len = plain_graph_len(c, nsteps - done)) > 0;) {
+    cliffs_ctx::PlainGraph* pg = nullptr;
+    RET(plain_graph(c, len, &pg));
+    CK(cudaGraphLaunch(pg->exec, c->stream));
+    c->launches += (int64_t)per * len;
+    c->sweeps += (unsigned)(per * len);
+    for (int s = 0; s < len; ++s) step_done(c);
+    for (int s = 0; s < len; ++s) *t = *t + c->dt;
+    if (steps_done) *steps_done += len;
+    done += len;
   }
   *done_out = done;
+  return CLIFFS_OK;
+}
+
+int cliffs_gpu_prepare_steps(cliffs_ctx* c, int32_t nsteps) {
+  if (!c || nsteps < 0) return CLIFFS_ERR_ARG;
+  if (!c->have_state) return CLIFFS_ERR_STATE;
+  if (!plain_graphs_apply(c)) return CLIFFS_OK;
+  // the graphs cliffs_gpu_step(nsteps) would replay; a fresh state's first
+  // step runs alone
+  int n = nsteps - (c->max_fresh && nsteps > 0 ? 1 : 0);
+  int last = -1;
+  for (int len; (len = plain_graph_len(c, n)) > 0; n -= len) {
+    if (len == last) continue;
+    cliffs_ctx::PlainGraph* pg = nullptr;
+    RET(plain_graph(c, len, &pg));
+    last = len;
+  }
   return CLIFFS_OK;
 }
 
@@ -1748,20 +1867,17 @@ int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
   if (!c || !me || !mv) return CLIFFS_ERR_ARG;
   RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
-  float *a = nullptr, *b = nullptr;
+  double* x = nullptr;
+  RET(xfer_area(c, &x));
+  float *a = (float*)x, *b = (float*)(x + n);
   int r = CLIFFS_OK;
-  if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
-  if (!r) {
-    ++c->launches;
-    k_maxwave_out<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax,
-                                                             c->velmax, (float)c->ground, a, b);
-    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
-  }
+  ++c->launches;
+  k_maxwave_out<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax,
+                                                           (float)c->ground, a, b);
+  if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && cudaMemcpyAsync(me, a, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && cudaMemcpyAsync(mv, b, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
-  if (a) cudaFree(a);
-  if (b) cudaFree(b);
   return r;
 }
 
@@ -1769,20 +1885,17 @@ int cliffs_gpu_get_max_raw(cliffs_ctx* c, double* hm, double* vm) {
   if (!c) return CLIFFS_ERR_ARG;
   RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
-  double *a = nullptr, *b = nullptr;
+  double* x = nullptr;
+  RET(xfer_area(c, &x));
+  double *a = x, *b = x + n;
   int r = CLIFFS_OK;
-  if (dalloc(&a, n) || dalloc(&b, n)) r = CLIFFS_ERR_NOMEM;
-  if (!r) {
-    ++c->launches;
-    k_max_raw<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax,
-                                                         a, b, kGrav);
-    if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
-  }
+  ++c->launches;
+  k_max_raw<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax, a, b,
+                                                       kGrav);
+  if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
   if (!r && hm && cudaMemcpyAsync(hm, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (!r && vm && cudaMemcpyAsync(vm, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
-  if (a) cudaFree(a);
-  if (b) cudaFree(b);
   return r;
 }
 
@@ -2133,13 +2246,28 @@ void cliffs_gpu_host_free(void* p) {
 
 int cliffs_gpu_status(cliffs_ctx* c, uint32_t* flags) {
   if (!c || !flags) return CLIFFS_ERR_ARG;
-  unsigned f = 0;
-  CK(cudaMemcpyAsync(&f, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+  unsigned w[2] = {0, 0};
+  CK(cudaMemcpyAsync(w, c->status, sizeof(w), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemsetAsync(c->status, 0, sizeof(w), c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  *flags = f;
-  if (f & CLIFFS_ST_NAN) return CLIFFS_ERR_NAN;
-  return (f & CLIFFS_ST_STALL) ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
+  *flags = w[0];
+  float courant = 0.f;
+  std::memcpy(&courant, &w[1], sizeof(float));
+  c->courant_seen = std::max(c->courant_seen, (double)courant);
+  if (w[0] & CLIFFS_ST_NAN) return CLIFFS_ERR_NAN;
+  if (w[0] & CLIFFS_ST_STALL) return CLIFFS_ERR_TIMEOUT;
+  return (w[0] & CLIFFS_ST_CFL) ? CLIFFS_WARN_CFL : CLIFFS_OK;
+}
+
+int cliffs_gpu_courant(cliffs_ctx* c, double* courant) {
+  if (!c || !courant) return CLIFFS_ERR_ARG;
+  unsigned w[2] = {0, 0};
+  CK(cudaMemcpyAsync(w, c->status, sizeof(w), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  float now = 0.f;
+  std::memcpy(&now, &w[1], sizeof(float));
+  *courant = std::max(c->courant_seen, (double)now);
+  return CLIFFS_OK;
 }
 
 int cliffs_gpu_set_sweep_kernel(cliffs_ctx* c, int32_t kind) {
@@ -2204,6 +2332,12 @@ int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t block_x, int32_t warps_y) {
   return CLIFFS_OK;
 }
 
+int cliffs_gpu_set_column_run(cliffs_ctx* c, int32_t cells) {
+  if (!c || (cells != 0 && cells != 4 && cells != 8 && cells != 16 && cells != 32)) return CLIFFS_ERR_ARG;
+  if (cells) c->col_groups = cells / kCellsPerThread;
+  return CLIFFS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Sweep without device allocation.
 //
@@ -2219,35 +2353,40 @@ int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t block_x, int32_t warps_y) {
 
 static constexpr int kNoAllocCells = 1 << 20;  // largest nx*ny accepted
 static __device__ __align__(256) uint32_t g_noalloc_list[kNoAllocCells];
-static __device__ __align__(256) uint32_t g_noalloc_count[2];
-static __device__ __align__(256) unsigned g_noalloc_status[1];
+// [0] worklist length of the current call (afterwards: the cells it listed),
+// [1] the other parity's counter (zeroed by the fast kernel), [2] status bits,
+// [3] the largest Courant number above 1 (float bits)
+static __device__ __align__(256) uint32_t g_noalloc_words[4];
 
 struct NoAllocScratch {
   uint32_t* list = nullptr;
-  uint32_t* count = nullptr;
-  unsigned* status = nullptr;
+  uint32_t* words = nullptr;
 };
 
 // Device addresses of the scratch arrays, resolved once per device with that
 // device current.  In host code the array names are host-side stand-ins, never
-// device addresses.
+// device addresses.  Host threads making their first calls at the same time
+// serialise on the lock; later calls read the published entry without it.
 static int noalloc_scratch(NoAllocScratch* out) {
   constexpr int kMaxDevices = 64;
   static NoAllocScratch cache[kMaxDevices];
+  static std::atomic<bool> ready[kMaxDevices];
+  static std::mutex lock;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CLIFFS_ERR_DEVICE;
-  NoAllocScratch& s = cache[dev];
-  if (!s.list) {
-    void *a = nullptr, *b = nullptr, *c = nullptr;
-    if (cudaGetSymbolAddress(&a, g_noalloc_list) != cudaSuccess ||
-        cudaGetSymbolAddress(&b, g_noalloc_count) != cudaSuccess ||
-        cudaGetSymbolAddress(&c, g_noalloc_status) != cudaSuccess)
-      return CLIFFS_ERR_CUDA;
-    s.count = (uint32_t*)b;
-    s.status = (unsigned*)c;
-    s.list = (uint32_t*)a;
+  if (!ready[dev].load(std::memory_order_acquire)) {
+    std::lock_guard<std::mutex> g(lock);
+    if (!ready[dev].load(std::memory_order_relaxed)) {
+      void *a = nullptr, *b = nullptr;
+      if (cudaGetSymbolAddress(&a, g_noalloc_list) != cudaSuccess ||
+          cudaGetSymbolAddress(&b, g_noalloc_words) != cudaSuccess)
+        return CLIFFS_ERR_CUDA;
+      cache[dev].list = (uint32_t*)a;
+      cache[dev].words = (uint32_t*)b;
+      ready[dev].store(true, std::memory_order_release);
+    }
   }
-  *out = s;
+  *out = cache[dev];
   return CLIFFS_OK;
 }
 
@@ -2297,11 +2436,12 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
   A.inv_dx1 = A.inv_dxn1 = (float)(1.0 / h);
   A.edges = nullptr;
   A.list = sc.list;
-  A.count = sc.count;
-  A.count_next = sc.count + 1;
-  A.status = sc.status;
-  // the shared counter keeps the previous call's value: start from zero
-  CK(cudaMemsetAsync(sc.count, 0, sizeof(uint32_t), st));
+  A.count = sc.words;
+  A.count_next = sc.words + 1;
+  A.status = (unsigned*)(sc.words + 2);
+  // the shared words keep the previous call's values: the counter, the
+  // status and the Courant word start from zero
+  CK(cudaMemsetAsync(sc.words, 0, 4 * sizeof(uint32_t), st));
   if (iu == 1) {
     A.n = nx;
     A.nlines = ny;
@@ -2323,6 +2463,19 @@ int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch, 
   }
   CK(cudaGetLastError());
   return CLIFFS_OK;
+}
+
+int cliffs_gpu_sweep_noalloc_status(void* stream, uint32_t* flags, uint32_t* listed) {
+  NoAllocScratch sc;
+  int r = noalloc_scratch(&sc);
+  if (r) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint32_t w[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(w, sc.words, sizeof(w), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (flags) *flags = w[2];
+  if (listed) *listed = w[0];
+  return (w[2] & ST_NAN) ? CLIFFS_ERR_NAN : CLIFFS_OK;
 }
 
 }  // extern "C"

@@ -10,7 +10,7 @@ The reference runs every level as its own process:
   output_feed.f);
 - the child run reads them back (get_boundary_feed.f:144-167);
 - it starts at the first record whose edge elevation reaches cuke
-  (get_boundary_feed.f:473-496);
+  (get_boundary_feed.f:144-167);
 - it interpolates its edge values between records in time
   (cliffs_main.f:305-323) and stops when the records end (freeze).
 run_chain does the same without the files: level k runs to the end time and

@@ -30,6 +30,7 @@ extern "C" {
 enum {
   CLIFFS_OK = 0,
   CLIFFS_FEED_ENDED = 1,      /* forcing ended with freeze set (cliffs_main.f:305-311) */
+  CLIFFS_WARN_CFL = 2,        /* a sweep read a state whose Courant number exceeds 1 */
   CLIFFS_ERR_ARG = -1,        /* bad argument or grid description */
   CLIFFS_ERR_CUDA = -2,       /* CUDA runtime error */
   CLIFFS_ERR_NAN = -3,        /* a non-finite eta/u/v appeared */
@@ -42,7 +43,9 @@ enum {
 /* status bits reported by cliffs_gpu_status() */
 enum {
   CLIFFS_ST_NAN = 1u,         /* a sweep produced a non-finite value */
-  CLIFFS_ST_STALL = 2u        /* a staged sweep's shared-memory stage wait ran out */
+  CLIFFS_ST_STALL = 2u,       /* a staged sweep's shared-memory stage wait ran out */
+  CLIFFS_ST_CFL = 4u          /* a sweep read a cell whose Courant number
+                                 (|u|+c) dt / ((dx(m-1)+dx(m))/2) exceeds 1 */
 };
 
 typedef struct cliffs_ctx cliffs_ctx;
@@ -83,9 +86,9 @@ typedef struct cliffs_runup {
   int64_t wet_now;       /* cells currently wet */
 } cliffs_runup;
 
-/* MasterGrid.f:237-268 restated: the spacing factors of cliffs_grid_desc from
+/* MasterGrid.f:85-116 restated: the spacing factors of cliffs_grid_desc from
  * grid coordinates.  Replaces the s1/s2/zeta computation of MasterGrid; the
- * optional zeta override of MasterGrid.f:270-273 (channel width) is the
+ * optional zeta override of MasterGrid.f:118-121 (channel width) is the
  * caller's.  Outputs may be NULL when the grid shape does not use them. */
 int cliffs_gpu_metrics(int32_t nx, int32_t ny, int32_t cartesian,
                        const double *xcrd, const double *ycrd, double *dx,
@@ -159,14 +162,14 @@ int cliffs_gpu_apply_lattice(cliffs_ctx *ctx, const double *xcrd, const double *
 /* Boundary forcing (get_boundary_feed.f): nt records at times tinput(nt);
  * west/east (ny,3,nt) and south/north (nx,3,nt) hold (u, v, eta) per edge
  * node, either pair may be NULL when that sweep does not run.  irec is the
- * 1-based start record (get_boundary_feed.f:473-496), freeze the stop flag of
+ * 1-based start record (get_boundary_feed.f:144-167), freeze the stop flag of
  * allabout.f:65.  The time-loop cursor of cliffs_main.f:305-315 is kept by the
  * library.  nt = 0 removes the forcing. */
 int cliffs_gpu_set_feed(cliffs_ctx *ctx, int32_t nt, const double *tinput,
                         const double *west, const double *east,
                         const double *south, const double *north,
                         int32_t irec, int32_t freeze);
-/* First record whose edge elevation reaches cuke (get_boundary_feed.f:473-496);
+/* First record whose edge elevation reaches cuke (get_boundary_feed.f:144-167);
  * -1 when the signal stays below it.  Uses the records of cliffs_gpu_set_feed. */
 int cliffs_gpu_feed_start(cliffs_ctx *ctx, double cuke);
 
@@ -257,8 +260,18 @@ int cliffs_gpu_host_alloc(int64_t bytes, void **p);
 void cliffs_gpu_host_free(void *p);
 
 /* Sticky status bits (CLIFFS_ST_*) since the last call; synchronises.
- * Returns CLIFFS_ERR_NAN or CLIFFS_ERR_TIMEOUT when the matching bit is set. */
+ * Returns CLIFFS_ERR_NAN or CLIFFS_ERR_TIMEOUT when the matching bit is set,
+ * else CLIFFS_WARN_CFL when CLIFFS_ST_CFL is.
+ * The Courant check has no counterpart in the reference, whose dt is fixed by
+ * the user (allabout.f:55) and never checked.  Every sweep evaluates
+ * (|u|+c) dt / ((dx(m-1)+dx(m))/2) along its lines on the state it reads
+ * (row spacing scaled by cos(lat) on a spherical grid), reduced per warp by a
+ * vote and, where a number exceeds 1, a warp max reduction; VTCS-2 is stable
+ * up to 1. */
 int cliffs_gpu_status(cliffs_ctx *ctx, uint32_t *flags);
+/* The largest Courant number above 1 that any sweep of this context has read
+ * (0 when none has); synchronises.  No counterpart in the reference. */
+int cliffs_gpu_courant(cliffs_ctx *ctx, double *courant);
 /* Block until queued work on the context's stream is done. */
 int cliffs_gpu_sync(cliffs_ctx *ctx);
 
@@ -275,17 +288,33 @@ int cliffs_gpu_launch_count(cliffs_ctx *ctx, int64_t *n);
 
 /* Steps captured in one CUDA graph by cliffs_gpu_step (default 16; 0 or 1:
  * no graph).  Steps without profiling or a rising source are replayed from
- * a graph, one launch per k steps.  With boundary forcing (two-dimensional
- * grids) the graph first fills the k steps' edge tables in one kernel, from
- * the records and weights the library's cursor gives each step; a chunk in
- * which the forcing ends runs step by step. */
+ * a graph, one launch per k steps; the last steps of a call, when fewer than
+ * k but at least 2, from a graph of their own length (a few such lengths are
+ * kept per context).  A fresh state's first step (after set_initial, an
+ * upload, a source, a single sweep) runs on its own.  With boundary forcing
+ * (two-dimensional grids) the graph first fills the k steps' edge tables in
+ * one kernel, from the records and weights the library's cursor gives each
+ * step; a chunk in which the forcing ends runs step by step. */
 int cliffs_gpu_set_graph_steps(cliffs_ctx *ctx, int32_t k);
+/* Capture and instantiate, without running them, the graphs that a
+ * cliffs_gpu_step(ctx, nsteps) call made from the current state would
+ * replay, so that the call itself only launches them (no counterpart in the
+ * reference).  Graphs stay valid until the tiling, the sweep kernels or
+ * graph_k change. */
+int cliffs_gpu_prepare_steps(cliffs_ctx *ctx, int32_t nsteps);
 
 /* Tuning: threads per block of the x-sweep kernel (multiple of 32, <= 256)
  * and warps per block of the y-sweep kernel (<= 8).  0 keeps the current
  * value.  Results do not depend on the tiling.  Applies to the tiled sweep
  * kernels. */
 int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
+/* Tuning of the tiled y-sweep: cells per thread along a column, 4, 8, 16 or
+ * 32 (0 keeps the current value; default 4).  With 4 each thread takes one
+ * 4-cell group and its 6-cell window; with more, a thread walks down its
+ * column group by group and carries the window's last two cells and last
+ * face flux into the next group instead of loading and computing them again.
+ * Results do not depend on it. */
+int cliffs_gpu_set_column_run(cliffs_ctx *ctx, int32_t cells);
 
 /* The sweep kernels, two choices with identical results:
  * - CLIFFS_SWEEP_TILED (the default): one block per tile, loads straight into
@@ -329,13 +358,25 @@ int cliffs_gpu_check_stage_timeout(cliffs_ctx *ctx, int32_t wait_ms);
  * until the process exits; all calls share it, so calls that overlap on the
  * GPU (different streams, or devices sharing a process without ordering) race
  * on it.  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Host threads that make their first calls at the same time are serialised
+ * by a lock around that look-up.  Each call clears the shared status word
+ * and the worklist counter before its kernels run. */
 int cliffs_gpu_sweep_noalloc(int32_t iu, int32_t nx, int32_t ny, int32_t pitch,
                              const float *dep, const float *srf,
                              const float *xvel, const float *yvel,
                              float *srf_out, float *xvel_out, float *yvel_out,
                              double dx, double dy, double ground, double crough,
                              double dt, void *stream);
+/* Status of the latest cliffs_gpu_sweep_noalloc call on this device, read
+ * after `stream` (the call's stream) has finished: *flags gets its
+ * CLIFFS_ST_* bits (CLIFFS_ST_NAN when the sweep produced a non-finite
+ * value), *listed the number of cells the sweep sent through the full
+ * wet/dry rules (shorelines, line ends, supercritical windows).  Either
+ * pointer may be NULL.  Synchronises the stream and allocates nothing.
+ * Returns CLIFFS_ERR_NAN when CLIFFS_ST_NAN is set.  No counterpart in the
+ * reference. */
+int cliffs_gpu_sweep_noalloc_status(void *stream, uint32_t *flags, uint32_t *listed);
 
 /* ---- ensembles ------------------------------------------------------------
  * No reference counterpart: the reference runs one grid per process.  A batch

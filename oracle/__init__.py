@@ -120,7 +120,7 @@ def pinpoint(xx, xp):
 
 
 def metrics(xcrd, ycrd, cartesian):
-    """MasterGrid.f:237-268 -> (s1 (ny, nx-1) or None, s2 or None, zeta or None)."""
+    """MasterGrid.f:85-116 -> (s1 (ny, nx-1) or None, s2 or None, zeta or None)."""
     xcrd = np.ascontiguousarray(xcrd, dtype=np.float64)
     ycrd = np.ascontiguousarray(ycrd, dtype=np.float64)
     nx, ny = len(xcrd), len(ycrd)

@@ -746,7 +746,7 @@ void orc_nest_tables(const double *xcrd, int nx, const double *ycrd, int ny,
   for (int i = 0; i < nn; ++i) orc_pinpoint(ycrd, ny, ynst[i], &t->WE_ny[i], &t->WE_cy[i]);
 }
 
-/* clm(kk,1:3) for one parent column or row, weighted by cc (feed_children_grid.f:203-222). */
+/* clm(kk,1:3) for one parent column or row, weighted by cc (feed_children_grid.f:53-73). */
 static void feed_clm(const orc_grid *g, int fixed_is_col, int fixed, int a, int b,
                      double cc, double hmin, double *clm, int ld) {
   const double grav = ORC_GRAV;

@@ -103,7 +103,7 @@ void orc_apply_ic(int nx, int ny, const double *xq, const double *yq,
                   const double *yp, double *pp);
 /* NestedGrid.f:129-148 (ip is 1-based). */
 void orc_pinpoint(const double *xx, int nx, double xp, int32_t *ip, double *cp);
-/* MasterGrid.f:237-268: s1 (nx-1,ny), s2 (ny-1), zeta (ny).  Pass NULL for
+/* MasterGrid.f:85-116: s1 (nx-1,ny), s2 (ny-1), zeta (ny).  Pass NULL for
  * outputs that the grid shape does not allocate. */
 void orc_metrics(int nx, int ny, int cartesian, const double *xcrd,
                  const double *ycrd, double *s1, double *s2, double *zeta);
@@ -125,7 +125,7 @@ void orc_nest_tables(const double *xcrd, int nx, const double *ycrd, int ny,
 int orc_feed_child(const orc_grid *g, const orc_nest *t, double hmin,
                    double cuke, int32_t *iarv, double *uvq_w, double *uvq_e,
                    double *uvq_s, double *uvq_n);
-/* get_boundary_feed.f:473-496: first record whose edge |eta| >= cuke.
+/* get_boundary_feed.f:144-167: first record whose edge |eta| >= cuke.
  * Returns the 1-based record index, or -1 when the signal stays below it. */
 int orc_feed_start(const orc_feed *f, int nx, int ny, int xrun, int yrun,
                    double cuke);

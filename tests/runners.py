@@ -108,3 +108,38 @@ def shadow(m, g, steps, window, scale):
         cel, u, v = g.download_state()
         out.append(compare_state(m, cel, u, v, scale))
     return out
+
+
+def runup_line(maxe):
+    """Per row of a max-wave elevation field (output_maxwave.f:14-27, -1e32
+    where never wet): the landward-most node ever wet, i.e. the largest x
+    index with hmax > celmin (the coast of every workload lies on the high-x
+    side); -1 for a row never wet."""
+    wet = maxe > -1e30
+    last = wet.shape[1] - 1 - np.argmax(wet[:, ::-1], axis=1)
+    return np.where(wet.any(axis=1), last, -1)
+
+
+def compare_runup(mo, mg, dep):
+    """The runup line of the GPU's max-wave field mg against the oracle's mo:
+    per row, the landward-most wetted node, GPU minus oracle, in cells and in
+    metres of ground elevation (-dep) at those nodes.  Also the runup itself,
+    the highest land elevation (-dep over dep < 0) ever wetted, of each."""
+    io, ig = runup_line(mo), runup_line(mg)
+    rows = np.nonzero((io >= 0) | (ig >= 0))[0]
+    r = dict(rows=int(len(rows)), rows_differ=0, max_cells=0, max_elev_m=0.0)
+    if len(rows):
+        both = rows[(io[rows] >= 0) & (ig[rows] >= 0)]
+        dc = ig[both] - io[both]
+        de = np.abs(dep[both, ig[both]] - dep[both, io[both]])
+        r["rows_differ"] = int((io[rows] != ig[rows]).sum())
+        r["max_cells"] = int(np.abs(dc).max()) if len(dc) else 0
+        r["max_elev_m"] = float(de.max()) if len(de) else 0.0
+        r["one_sided"] = int(len(rows) - len(both))
+        if r["rows_differ"]:
+            k = rows[np.argmax(np.abs(np.where(io[rows] >= 0, io[rows], 0) - np.where(ig[rows] >= 0, ig[rows], 0)))]
+            r["worst_row"] = dict(j=int(k) + 1, i_oracle=int(io[k]) + 1, i_gpu=int(ig[k]) + 1)
+    for key, m in (("runup_oracle_m", mo), ("runup_gpu_m", mg)):
+        land = (dep < 0) & (m > -1e30)
+        r[key] = float((-dep[land]).max()) if land.any() else 0.0
+    return r

@@ -1,10 +1,10 @@
 """GPU parity of the time loop's other pieces, through the C ABI:
 
-- boundary forcing: start record (get_boundary_feed.f:473-496), record cursor,
+- boundary forcing: start record (get_boundary_feed.f:144-167), record cursor,
   FP64 lerp and the freeze stop (cliffs_main.f:305-339);
 - nested-grid feed: arrival test and edge records (feed_children_grid.f);
 - spherical grids: cos(lat) row factor and the zeta metric term (MasterGrid.f);
-- 1-D channels along y with a width term (MasterGrid.f:270-273);
+- 1-D channels along y with a width term (MasterGrid.f:118-121);
 - 1-D grids with a passive second row;
 - non-finite state reported through the status word.
 Tolerances as in test_gpu_parity.py.
@@ -188,4 +188,31 @@ def test_nonfinite_state_is_reported():
     assert r == pkg.cliffs_gpu.CliffsError(-3, "x").code and flags & 1
     r, flags = g.status()  # the status word is cleared by reading it
     assert flags == 0
+    g.close()
+
+
+def test_courant_check():
+    """A time step past the Courant limit is reported (CLIFFS_ST_CFL, status
+    CLIFFS_WARN_CFL) with the largest Courant number the sweeps read; the
+    workload's own time step (Courant 0.8 on the deepest water) raises
+    nothing."""
+    case = W.shelf_2d(seed=4, nx=256, ny=192, dx=1000.0, steps=0, ngauges=0)
+    g = pkg.GpuGrid.from_case(case)
+    g.step(20)
+    assert g.status() == (0, 0)
+    assert g.courant() == 0.0
+    g.close()
+    case["dt"] *= 1.5
+    g = pkg.GpuGrid.from_case(case)
+    g.step(1)
+    r, flags = g.status()
+    assert r == pkg.cliffs_gpu.CLIFFS_WARN_CFL and flags == pkg.cliffs_gpu.CLIFFS_ST_CFL, (r, flags)
+    # the first x-sweep reads the state at rest: sqrt(g H) dt / dx at the
+    # deepest cell (H in FP32 as the device holds it)
+    H = np.asarray(case["H0"], np.float32).astype(np.float64)
+    expect = np.sqrt(GRAV * H.max()) * case["dt"] / 1000.0
+    cn = g.courant()
+    assert expect * (1 - 1e-4) <= cn <= expect * 1.05, (cn, expect)
+    assert g.status() == (0, 0)  # read and cleared
+    assert g.courant() == cn     # the largest number stays reported
     g.close()

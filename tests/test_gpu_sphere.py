@@ -3,7 +3,7 @@ GPU against the FP64 oracle.
 
 Every field (37 MB in FP32) is far larger than the shares of L2 a sweep
 keeps, so this is the case whose DRAM counters read at face value.  The
-metric terms are the spherical ones of MasterGrid.f:237-268: x spacing
+metric terms are the spherical ones of MasterGrid.f:85-116: x spacing
 scaled by cos(latitude) per row, zeta per row.  Tolerances as in
 test_gpu_parity.py: eta and max-wave within 1e-4 of the source amplitude on
 cells wet in both runs, velocities within 2e-4 m/s + 2e-4 relative, gauges
