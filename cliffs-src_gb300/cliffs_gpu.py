@@ -203,7 +203,6 @@ SIGNATURES = {
     "cliffs_gpu_prepare_steps": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_courant": ([_V, _dp], ctypes.c_int),
     "cliffs_gpu_set_tiling": ([_V, _I, _I], ctypes.c_int),
-    "cliffs_gpu_set_column_run": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_set_sweep_kernel": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_check_stage_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_gpu_strerror": ([ctypes.c_int], ctypes.c_char_p),
@@ -574,12 +573,8 @@ class GpuGrid:
     def set_tiling(self, block_x=0, warps_y=0):
         _chk(self.L.cliffs_gpu_set_tiling(self.h, int(block_x), int(warps_y)), "set_tiling")
 
-    def set_column_run(self, cells):
-        """Cells per thread along a column in the tiled y-sweep (4..32)."""
-        _chk(self.L.cliffs_gpu_set_column_run(self.h, int(cells)), "set_column_run")
-
     def set_sweep_kernel(self, kind):
-        """STAGED (persistent, TMA-staged windows; the default) or TILED."""
+        """TILED (one block per tile; the default) or STAGED (persistent, TMA-staged windows)."""
         _chk(self.L.cliffs_gpu_set_sweep_kernel(self.h, int(kind)), "set_sweep_kernel")
 
     def check_stage_timeout(self, wait_ms=50):

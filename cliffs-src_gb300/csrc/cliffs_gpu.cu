@@ -141,9 +141,6 @@ struct cliffs_ctx {
   int* d_flag = nullptr;
   bool have_state = false;
   int blk_x = 128, warps_y = 4;
-  // y-sweep: groups of 4 cells per thread along a column (1: the fast
-  // kernel, one group; 2, 4, 8: column_kernel)
-  int col_groups = 1;
   // worklist of cells for the general kernel and one counter per sweep parity
   uint32_t* list = nullptr;
   uint32_t* cnt = nullptr;
@@ -667,9 +664,6 @@ SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
   return A;
 }
 
-// The y-sweep's launch shape, as a captured graph holds it.
-inline int ykey(const cliffs_ctx* c) { return c->warps_y | (c->col_groups << 8); }
-
 // One fast-kernel sweep on the context's stream, a programmatic dependent of
 // the previous launch when c->pdl is set.
 template <int DIR, bool MAXOUT>
@@ -685,33 +679,6 @@ cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArg
   cfg.attrs = at;
   cfg.numAttrs = c->pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT>, A);
-}
-
-// One column-run y-sweep (column_kernel, G groups of 4 cells per thread).
-template <bool MAXOUT, int G>
-cudaError_t launch_column_g(cliffs_ctx* c, const SweepArgs& A) {
-  const unsigned block = 32u * (unsigned)c->warps_y;
-  const int rows = c->warps_y * kCellsPerThread * G;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = (size_t)block * kCellsPerThread * G * sizeof(uint32_t);
-  cfg.stream = c->stream;
-  cfg.attrs = at;
-  cfg.numAttrs = c->pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, column_kernel<true, MAXOUT, G>, A);
-}
-
-template <bool MAXOUT>
-cudaError_t launch_column(cliffs_ctx* c, const SweepArgs& A) {
-  switch (c->col_groups) {
-    case 2: return launch_column_g<MAXOUT, 2>(c, A);
-    case 4: return launch_column_g<MAXOUT, 4>(c, A);
-    default: return launch_column_g<MAXOUT, 8>(c, A);
-  }
 }
 
 // Max-wave handling of one sweep: none, the update with its outputs (the last
@@ -765,12 +732,6 @@ int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double
       CK((launch_fast<0, true>(c, grid, (unsigned)c->blk_x, A)));
     else
       CK((launch_fast<0, false>(c, grid, (unsigned)c->blk_x, A)));
-  } else if (c->col_groups > 1) {
-    ++c->launches;
-    if (maxm == MAXM_OUT)
-      CK(launch_column<true>(c, A));
-    else
-      CK(launch_column<false>(c, A));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
@@ -1529,7 +1490,7 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
     c->fgraph = nullptr;
   }
   if (!c->fgraph || c->fgraph_k != k || c->fgraph_cur != c->cur || c->fgraph_blk != c->blk_x ||
-      c->fgraph_wy != ykey(c) || c->fgraph_kind != c->sweep_kind) {
+      c->fgraph_wy != c->warps_y || c->fgraph_kind != c->sweep_kind) {
     if (c->fgraph) cudaGraphExecDestroy(c->fgraph);
     c->fgraph = nullptr;
     const int64_t launches = c->launches;
@@ -1563,7 +1524,7 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
     c->fgraph_k = k;
     c->fgraph_cur = c->cur;
     c->fgraph_blk = c->blk_x;
-    c->fgraph_wy = ykey(c);
+    c->fgraph_wy = c->warps_y;
     c->fgraph_kind = c->sweep_kind;
   }
   int done = 0;
@@ -1615,7 +1576,7 @@ static int forced_graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* ste
 // every replay.  Every captured step folds the previous step's end state
 // into the max-wave fields (the state is not fresh).
 static bool plain_graph_valid(const cliffs_ctx* c, const cliffs_ctx::PlainGraph& pg, int len) {
-  return pg.exec && pg.len == len && pg.cur == c->cur && pg.blk == c->blk_x && pg.wy == ykey(c) &&
+  return pg.exec && pg.len == len && pg.cur == c->cur && pg.blk == c->blk_x && pg.wy == c->warps_y &&
          pg.kind == c->sweep_kind;
 }
 
@@ -1677,7 +1638,7 @@ static int plain_graph(cliffs_ctx* c, int len, cliffs_ctx::PlainGraph** out) {
   pg.len = len;
   pg.cur = c->cur;
   pg.blk = c->blk_x;
-  pg.wy = ykey(c);
+  pg.wy = c->warps_y;
   pg.kind = c->sweep_kind;
   *out = &pg;
   return CLIFFS_OK;
@@ -2329,12 +2290,6 @@ int cliffs_gpu_set_tiling(cliffs_ctx* c, int32_t block_x, int32_t warps_y) {
   if (!c || block_x < 0 || warps_y < 0 || block_x % 32 || block_x > 256 || warps_y > 8) return CLIFFS_ERR_ARG;
   if (block_x) c->blk_x = block_x;
   if (warps_y) c->warps_y = warps_y;
-  return CLIFFS_OK;
-}
-
-int cliffs_gpu_set_column_run(cliffs_ctx* c, int32_t cells) {
-  if (!c || (cells != 0 && cells != 4 && cells != 8 && cells != 16 && cells != 32)) return CLIFFS_ERR_ARG;
-  if (cells) c->col_groups = cells / kCellsPerThread;
   return CLIFFS_OK;
 }
 

@@ -576,178 +576,6 @@ __global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
   sweep_tile<DIR, LOCAL, false, false, MAXOUT>(A, blockIdx.x, blockIdx.y);
 }
 
-// y-sweep by column runs.  A warp's lanes are 32 neighbouring columns (every
-// row load is one 128-byte line); each thread walks G groups of 4 cells down
-// its column.  A group is the fast kernel's 4 cells with their 6-cell window,
-// aligned alike (first cell 4m+1), so the plain update, the sup test and the
-// rare branch see exactly the same values as in sweep_tile; only the window's
-// last two cells and the last face flux move on to the next group instead of
-// being loaded and computed again.  Per cell that is 1 + 2/(4G) window loads
-// and derived values (1.5 in the fast kernel) and 1 + 1/(4G) face fluxes
-// (1.25).  The block's listed cells go to a shared-memory list of
-// blockDim * 4 * G entries (dynamic shared memory) and are finished after
-// one block barrier, as in sweep_cells.
-template <bool LOCAL, bool COH, bool MAXOUT, int G>
-__device__ __forceinline__ void column_tile(const SweepArgs& A, int bx, int by) {
-  extern __shared__ uint32_t s_list[];
-  __shared__ unsigned s_n;
-  if (LOCAL) {
-    if (threadIdx.x == 0) s_n = 0u;
-    __syncthreads();
-  } else if (bx == 0 && by == 0 && threadIdx.x == 0) {
-    *A.count_next = 0u;
-  }
-  const int lane = threadIdx.x & 31;
-  const int n = A.n;
-  const int L = by * 32 + lane + 1;
-  const int warps = (int)(blockDim.x >> 5);
-  const int ibase = (bx * warps + (int)(threadIdx.x >> 5)) * G * kCellsPerThread + 1;
-  const bool lact = L <= A.nlines;
-  const bool swept = lact && L >= A.lo && L <= A.hi;
-  const int Lc = min(L, A.nlines);
-  const Phys<float>& p = A.ph;
-  // window of the current group: positions i0-1 .. i0+4; e is eta once
-  // derived, s the surface state as loaded
-  float d[6], e[6], u[6], v[6], H[6], c[6], sw[6];
-  bool wet[6], sc[6];
-  float FP[5], FQ[5];
-  float cour = 0.f;
-  bool bad = false;
-  auto load = [&](int w, int pos) {
-    const int k = min(max(pos, 1), n);
-    const size_t q = cidx<1>(Lc, k, A.pitch);
-    d[w] = e[w] = u[w] = v[w] = 0.f;
-    if (lact) {
-      d[w] = __ldg(A.dep + q);
-      e[w] = ld_state<COH>(A.srf + q);
-      v[w] = ld_state<COH>(A.xu + q);  // tangential in the y-sweep
-      u[w] = ld_state<COH>(A.yv + q);  // normal
-    }
-  };
-  auto derive = [&](int w) {  // as sweep_cells: surface state -> (eta, H), celerity
-    sw[w] = e[w];
-    H[w] = e[w] + fmaxf(d[w], 0.f);
-    e[w] = e[w] - fminf(d[w], 0.f);
-    wet[w] = H[w] > p.ground;
-    c[w] = fsqrt_pos(p.g * fmaxf(H[w], p.ground));
-    sc[w] = fabsf(u[w]) > c[w];
-  };
-#pragma unroll
-  for (int g = 0; g < G; ++g) {
-    const int i0 = ibase + g * kCellsPerThread;
-    if (i0 > n) break;  // the same rows for the whole warp
-    if (g == 0) {
-#pragma unroll
-      for (int w = 0; w < 6; ++w) load(w, i0 - 1 + w);
-#pragma unroll
-      for (int w = 0; w < 6; ++w) derive(w);
-#pragma unroll
-      for (int f = 0; f < 5; ++f) face_flux(u[f], c[f], e[f], u[f + 1], c[f + 1], e[f + 1], p, FP[f], FQ[f]);
-    } else {
-#pragma unroll
-      for (int w = 0; w < 2; ++w) {  // positions i0-1, i0: the previous window's last two
-        d[w] = d[w + 4];
-        e[w] = e[w + 4];
-        u[w] = u[w + 4];
-        v[w] = v[w + 4];
-        H[w] = H[w + 4];
-        c[w] = c[w + 4];
-        sw[w] = sw[w + 4];
-        wet[w] = wet[w + 4];
-        sc[w] = sc[w + 4];
-      }
-      FP[0] = FP[4];
-      FQ[0] = FQ[4];
-#pragma unroll
-      for (int w = 2; w < 6; ++w) load(w, i0 - 1 + w);
-#pragma unroll
-      for (int w = 2; w < 6; ++w) derive(w);
-#pragma unroll
-      for (int f = 1; f < 5; ++f) face_flux(u[f], c[f], e[f], u[f + 1], c[f + 1], e[f + 1], p, FP[f], FQ[f]);
-    }
-    float hm[kCellsPerThread], vm[kCellsPerThread];
-#pragma unroll
-    for (int r = 0; r < kCellsPerThread; ++r) {
-      hm[r] = vm[r] = 0.f;
-      if (MAXOUT && lact && A.hmax) {
-        const size_t q = cidx<1>(L, min(i0 + r, n), A.pitch);
-        hm[r] = ld_state<COH>(A.hmax + q);
-        vm[r] = ld_state<COH>(A.velmax + q);
-      }
-    }
-    float os[kCellsPerThread], ou[kCellsPerThread], ov[kCellsPerThread];
-#pragma unroll
-    for (int r = 0; r < kCellsPerThread; ++r) {
-      os[r] = sw[r + 1];
-      ou[r] = u[r + 1];
-      ov[r] = v[r + 1];
-    }
-    unsigned need = 0u;
-    if (swept) {
-      const bool sup = sc[0] || sc[1] || sc[2] || sc[3] || sc[4] || sc[5];
-      const unsigned rest =
-          plain_cells<false>(A, i0, sup, d, e, u, v, H, c, wet, FP, FQ, 1.f, 1.f, os, ou, ov, cour);
-      if (rest) {
-        bool wr[6];  // rest_cells applies the line's range to its copy
-#pragma unroll
-        for (int w = 0; w < 6; ++w) wr[w] = wet[w];
-        need = rest_cells(A, L, i0, rest, d, e, u, v, H, c, wr, 1.f, os, ou, ov);
-      }
-    }
-    if (LOCAL) {
-#pragma unroll
-      for (int r = 0; r < kCellsPerThread; ++r)
-        if (lact && ((need >> r) & 1u))
-          s_list[atomicAdd(&s_n, 1u)] = (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1);
-    } else {
-#pragma unroll
-      for (int r = 0; r < kCellsPerThread; ++r)
-        enqueue(A, lact && ((need >> r) & 1u), (uint32_t)(L - 1) * (uint32_t)n + (uint32_t)(i0 + r - 1));
-    }
-    if (lact) {
-#pragma unroll
-      for (int r = 0; r < kCellsPerThread; ++r) {
-        const int k = i0 + r;
-        if (k > n) break;
-        const float xo = ov[r], yo = ou[r];
-        const bool done = !((need >> r) & 1u);
-        if (done) bad |= !isfinite(os[r] + xo + yo);
-        const size_t q = cidx<1>(L, k, A.pitch);
-        A.srf_o[q] = os[r];
-        A.xu_o[q] = xo;
-        A.yv_o[q] = yo;
-        if (MAXOUT && A.hmax) {  // max-wave update (cliffs_main.f:347-355)
-          A.hmax[q] = done ? fmaxf(hm[r], eta_of(os[r], d[r + 1])) : hm[r];
-          A.velmax[q] = done ? fmaxf(vm[r], xo * xo + yo * yo) : vm[r];
-        }
-      }
-    }
-  }
-  if (bad) atomicOr(A.status, ST_NAN);
-  if (__any_sync(0xffffffffu, cour > 0.5f)) {  // Courant check, as in sweep_cells
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(2.f * cour));
-    if (lane == 0) {
-      atomicOr(A.status, ST_CFL);
-      atomicMax(A.status + 1, m);
-    }
-  }
-  if (LOCAL) {
-    __syncthreads();  // the block's fast values are stored; its listed cells overwrite theirs
-    const unsigned cnt = s_n;
-    for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) general_store<1, COH>(A, s_list[t]);
-  }
-}
-
-// The y-sweep by column runs of 4 * G cells per thread (column_tile).  Block:
-// 32 columns x (blockDim / 32) warps; grid: (rows / (4 * G * warps), columns / 32).
-// Dynamic shared memory: blockDim * 4 * G list entries (LOCAL).
-template <bool LOCAL, bool MAXOUT, int G>
-__global__ void __launch_bounds__(256, 4) column_kernel(const SweepArgs A) {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  column_tile<LOCAL, false, MAXOUT, G>(A, blockIdx.x, blockIdx.y);
-}
-
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
 template <int DIR>
 __global__ void __launch_bounds__(128) general_kernel(const SweepArgs A) {

@@ -308,13 +308,6 @@ int cliffs_gpu_prepare_steps(cliffs_ctx *ctx, int32_t nsteps);
  * value.  Results do not depend on the tiling.  Applies to the tiled sweep
  * kernels. */
 int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
-/* Tuning of the tiled y-sweep: cells per thread along a column, 4, 8, 16 or
- * 32 (0 keeps the current value; default 4).  With 4 each thread takes one
- * 4-cell group and its 6-cell window; with more, a thread walks down its
- * column group by group and carries the window's last two cells and last
- * face flux into the next group instead of loading and computing them again.
- * Results do not depend on it. */
-int cliffs_gpu_set_column_run(cliffs_ctx *ctx, int32_t cells);
 
 /* The sweep kernels, two choices with identical results:
  * - CLIFFS_SWEEP_TILED (the default): one block per tile, loads straight into

@@ -5,10 +5,13 @@ runup on the innermost level and walls on the others.
 
 The chain is the benchmark's nested configuration at a tenth of the size
 (nested.SMALL: a 432 x 216 master at 1/12 degree, children of 60^2 and 90^2,
-a +3/-1 m dipole source 400 km offshore), 3 hours of model time.  Every
-level is compared on its own: the start time and record count, the gauge
-series, and the max-wave fields.  Tolerances are those of test_gpu_parity.py:
-elevation 1e-4 of the source amplitude, velocities 2e-4 m/s.
+a +3/-1 m dipole source 400 km offshore), for the configuration's full 6
+hours of model time.  Every level is compared on its own: the start time and
+record count, the gauge series, the max-wave fields and the runup line (per
+row, the landward-most node ever wet; on the innermost level the wave runs
+up onto land).  Tolerances are those of test_gpu_parity.py: elevation 1e-4
+of the source amplitude, velocities 2e-4 m/s; the runup line must be the
+oracle's in every row.
 """
 import importlib
 
@@ -16,13 +19,14 @@ import numpy as np
 import pytest
 
 import oracle
+from tests.runners import compare_runup
 
 pytestmark = pytest.mark.gpu
 pkg = importlib.import_module("cliffs-src_gb300")
 nested = importlib.import_module("cliffs-src_gb300.nested")
 cg = pkg.cliffs_gpu
 
-HOURS = 3.0
+HOURS = 6.0
 CUKE = 0.001
 BNDOUT, GOUT = 3, 10
 A = 3.0
@@ -106,6 +110,8 @@ def test_nested_chain_against_oracle():
         both = so & sg
         assert np.abs(g["maxe"] - mo)[both].max() <= 1e-4 * A, k
         assert np.abs(g["maxv"] - vo)[both].max() <= 2e-4, k
+        ru = compare_runup(mo, g["maxe"], levels[k]["dep"])
+        assert ru["rows_differ"] == 0 and ru["runup_gpu_m"] == ru["runup_oracle_m"], (k, ru)
     # the wave ran up on the innermost grid: land cells (dep < 0) got wet
     land_wet = (levels[2]["dep"] < 0) & (got[2]["maxe"] > -1e30)
     assert land_wet.sum() > 0

@@ -7,13 +7,15 @@ within 1e-4 of the amplitude.  The GPU keeps the state as FP32 surface
 elevation; the oracle keeps FP64 celerity exactly as the reference does.
 """
 import importlib
+import json
 
 import numpy as np
 import pytest
 
 import oracle
 from tests.lines import random_grid, random_spacing
-from tests.runners import GRAV, compare_maxwave, compare_state, gpu_grid, maxwave_ties, oracle_model
+from tests.runners import (GRAV, compare_maxwave, compare_runup, compare_state, gpu_grid, maxwave_ties,
+                           oracle_model, shadow)
 
 pytestmark = pytest.mark.gpu
 pkg = importlib.import_module("cliffs-src_gb300")
@@ -95,14 +97,67 @@ def test_channel_1d_runup():
     mg, vg = g.maxwave()
     rm = compare_maxwave(mo, vo, mg, vg, A, maxwave_ties(m))
     assert rm["mismatch"] <= 2 and rm["maxe"] <= 1e-4, rm
-    # runup: highest land elevation reached
+    # runup: the highest land elevation reached, and the runup line (the
+    # landward-most node ever wet) of the oracle exactly
     ro = g.runup()
     land = (m.dep < 0) & (m.hmax > m.celmin)
     ref_runup = float((-m.dep[land]).max()) if land.any() else 0.0
-    assert abs(ro["max_runup"] - ref_runup) <= 0.05 * 0.5 + 1e-9, (ro, ref_runup)
+    assert ro["max_runup"] == ref_runup, (ro, ref_runup)
+    ru = compare_runup(mo, mg, case["dep"])
+    assert ru["rows_differ"] == 0 and ru["runup_gpu_m"] == ref_runup, ru
     assert ro["wetted_land"] > 0
     assert g.status() == (0, 0)
     g.close()
+
+
+@pytest.mark.parametrize("seed", [13, 17])
+def test_channel_1d_runup_front_departure(seed):
+    """Seeds whose run-up passes a near-tie of the wet/dry switch (a flooded
+    cell ending a step within ~1e-4 m of ground, cliffs.f:56-122).  The free
+    FP32 run then departs from the FP64 oracle at the runup front.  The test
+    names the step and cell where the free-run eta difference first exceeds
+    1e-4 of the amplitude and checks that the cell is in the swash zone (a
+    thin water column over the beach), reports the free-run divergence at the
+    end beside the windowed comparison (250-step windows restarted from the
+    GPU's state, each within 1e-4 of the amplitude), and checks that the
+    runup line, the max runup and the wet/dry state still match the oracle's
+    exactly."""
+    case = W.channel_1d(seed=seed)
+    A = case["amplitude"]
+    m = oracle_model(case)
+    g = gpu_grid(case)
+    first = None
+    for s in range(1, 5001):
+        m.step(1)
+        g.step(1)
+        if first is None:
+            cel, u, v = g.download_state()
+            wet = (m.cel > m.celmin) & (cel > m.celmin)
+            eo = m.cel ** 2 / GRAV - m.dep
+            eg = cel * np.abs(cel) / GRAV - m.dep
+            err = np.where(wet, np.abs(eo - eg), 0.0)[0]
+            if err.max() > 1e-4 * A:
+                k = int(np.argmax(err))
+                first = dict(step=s, cell=k + 1, dep=float(m.dep[0, k]), H=float(m.cel[0, k] ** 2 / GRAV),
+                             err=float(err[k] / A))
+    cel, u, v = g.download_state()
+    free = compare_state(m, cel, u, v, A)
+    mo, vo = m.maxwave()
+    mg, vg = g.maxwave()
+    ru = compare_runup(mo, mg, case["dep"])
+    g.close()
+    # the same case compared over windows restarted from the GPU's state
+    m2, g2 = oracle_model(case), gpu_grid(case)
+    windows = shadow(m2, g2, 5000, 250, A)
+    g2.close()
+    print(json.dumps(dict(seed=seed, first_departure=first, free_run_end=free,
+                          windowed_worst=max(w["eta"] for w in windows), runup=ru)))
+    assert first is not None  # this seed does part from the oracle
+    assert first["H"] < 0.1 and first["dep"] < 0.2, first  # in the swash zone of the 1:20 beach
+    assert max(w["eta"] for w in windows) <= 1e-4, windows
+    assert max(w["mismatch"] for w in windows) == 0, windows
+    assert free["mismatch"] == 0, free
+    assert ru["rows_differ"] == 0 and ru["runup_gpu_m"] == ru["runup_oracle_m"], ru
 
 
 @pytest.mark.parametrize("nx,ny,steps", [(256, 256, 600), (320, 200, 300)])
