@@ -15,6 +15,12 @@ CPU sample): the command the ncu summaries under profiles/ capture.
 longitude, 80S-80N) instead of the 2048^2 Cartesian shelf, the default and
 the benchmark line.
 
+--workload ensemble256 runs the batched ensemble: 256 source scenarios on
+grids of 256^2 to 1024^2 cells stepped together (cliffs_batch_*, plan from
+the autotuner), 32 gauges per scenario sampled every 10 steps; the metric is
+scenarios/s for 2000-step scenarios, beside the same scenarios solved one at
+a time (each grid's own step graphs).
+
 --impl reference times the CPU restatement of the reference solver (the
 Fortran reference cannot be compiled on these hosts) with all host threads on
 the same workload.  With N > 1 (torchrun) every rank runs an independent
@@ -388,6 +394,156 @@ def run_ours(args):
     return 0
 
 
+def run_ensemble(args):
+    """The batched ensemble line (one GPU; replicas only across GPUs)."""
+    import importlib
+
+    import torch
+
+    rank, world, local = _env_rank()
+    E = importlib.import_module("cliffs-src_gb300.ensemble")
+    n, steps = 256, max(10, args.steps)
+    scs = E.scenarios(n, 0)
+    cells = sum(sc["side"] ** 2 for sc in scs)
+    config = {"workload": f"ensemble of {n} source scenarios, sides drawn from {list(E.SIDES)} at {E.DX:g} m "
+                          f"(shelf/slope bathymetry), seeded Gaussian uplifts 0.5-5 m, FP32 state, "
+                          f"32 gauges per scenario every 10 steps",
+              "scenarios": n, "cells_total": int(cells), "run_steps_per_scenario": E.RUN_STEPS,
+              "l2": f"working set ~{9 * cells * 4 / 1e6:.0f} MB per step > 129 MB L2; no flush",
+              "parallelism": "replicas only (one independent ensemble per GPU)"}
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        threads = os.cpu_count() or 1
+        cb = ensemble_cpu_baseline(E, scs, threads)
+        line = {"metric": "scenarios/s", "value": cb["value"], "unit": cb["unit"], "n_gpus": args.gpus,
+                "steps": cb["steps"], "warmup": 1, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "implementation": "CPU restatement of cliffs.f + cliffs_main.f time loop (oracle, OpenMP), "
+                                  "one scenario after another",
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    torch.cuda.set_device(local)
+    pkg = importlib.import_module("cliffs-src_gb300")
+    pkg.build.build()
+    with ClockSampler(local) as clk:
+        r = E.run(n, steps, seed=0, warmup=max(3, args.warmup))
+    if not r["status_ok"]:
+        raise RuntimeError("a scenario reported a non-zero status")
+    e2e = ensemble_e2e(pkg, E, n, steps)
+    peak, peak_kind = _peaks()
+    ms = r["batched_ms_per_step"]
+    achieved = B_STEP * cells / (ms / 1e3) / 1e9
+    cb = ensemble_cpu_baseline(E, scs, os.cpu_count() or 1) if rank == 0 else None
+    line = {"metric": "scenarios/s", "value": r["batched_scenarios_per_s"],
+            "unit": f"scenarios/s ({E.RUN_STEPS}-step scenarios)", "n_gpus": world, "steps": steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dict(config, plan=r["plan"]),
+            "implementation": "CUDA sm_103a, include/cliffs_gpu.h cliffs_batch_* (graph or persistent plan)",
+            "timing": "host clock around synchronised batch calls (each call ends with a stream synchronise)",
+            "sequential": {"ms_per_step": r["sequential_ms_per_step"],
+                           "scenarios_per_s": r["sequential_scenarios_per_s"],
+                           "what": "the same scenarios one at a time, each grid's steps from its own CUDA "
+                                   "graphs, asynchronous gauge records"},
+            "speedup_vs_sequential": r["speedup"], "autotune_ms_per_step": r["autotune_ms_per_step"],
+            "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": "batched x- and y-sweep phases and gauges, per step",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "bytes_per_cell": B_STEP,
+                         "peak_source": peak_kind},
+            "cpu_baseline": cb, "clocks": clk.summary(), "gpu_launches": int(r["batch_launches"])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def ensemble_cpu_baseline(E, scs, threads, steps=10):
+    """The oracle's time loop on one grid of each side (the ensemble's
+    bathymetry and a source of the ensemble), `steps` steps each after one
+    warm-up step; the ensemble's time per step is the sum over its
+    scenarios of cells / measured rate of that side."""
+    import oracle  # noqa: F401
+    from tests.runners import oracle_model
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    base = E.bathymetries(0)
+    rate = {}
+    for side in E.SIDES:
+        sc = next(s for s in scs if s["side"] == side)
+        c = dict(base[side])
+        # the source as the GPU applies it (bottom fixed, surface raised)
+        c["H0"] = base[side]["dep"] + E.pkg.cliffs_gpu.source_field(
+            c["xcrd"], c["ycrd"], x0=sc["x0"], y0=sc["y0"], ax=sc["ax"], ay=sc["ay"], angle=sc["angle"],
+            amp=sc["amp"], dipole=sc["dipole"])
+        m = oracle_model(c)
+        m.step(1)
+        t0 = time.perf_counter()
+        m.step(steps)
+        rate[side] = side * side * steps / (time.perf_counter() - t0)
+    t_step = sum(s["side"] ** 2 / rate[s["side"]] for s in scs)
+    return {"value": round(len(scs) / (t_step * E.RUN_STEPS), 4),
+            "unit": f"scenarios/s ({E.RUN_STEPS}-step scenarios)",
+            "cores": threads, "kind": "port", "steps": steps, "ms_per_step": round(1e3 * t_step, 3),
+            "sample": f"one grid per side {list(E.SIDES)}, {steps} time steps after 1 warm-up step, OpenMP over "
+                      f"lines ({threads} threads), FP64; the ensemble's step time is the sum over its "
+                      f"{len(scs)} scenarios of cells / the measured rate of their side",
+            "rates_mcell_per_s": {str(k): round(v / 1e6, 1) for k, v in rate.items()}}
+
+
+def ensemble_e2e(pkg, E, n, steps):
+    """The ensemble end to end through the public API: grids created from the
+    host's FP64 bathymetry and initial state (pinned arrays), sources applied
+    on the device, the batch and its gauges set up, `steps` steps with the
+    gauge records every 10 steps, and every scenario's max-wave fields back
+    to pinned host arrays.  Unit: 2000-step scenarios per second, with the
+    set-up counted once per `steps` steps."""
+    import numpy as np
+
+    base = E.bathymetries(0)
+    scs = E.scenarios(n, 0)
+    pin = pkg.cliffs_gpu.pinned
+    host = {}
+    for side, c in base.items():
+        host[side] = {k: pin(c["dep"].shape) for k in ("dep", "H0")}
+        host[side]["dep"][...] = c["dep"]
+        host[side]["H0"][...] = c["dep"]
+    maxes = [(pin((sc["side"],) * 2, np.float32), pin((sc["side"],) * 2, np.float32)) for sc in scs]
+    gauges = [base[sc["side"]]["gauges"] for sc in scs]
+    m = sum(len(I) for I, _ in gauges)
+    rec = [pin((m,)) for _ in range(3)]
+    cells = sum(sc["side"] ** 2 for sc in scs)
+    t0 = time.perf_counter()
+    grids = []
+    for sc in scs:
+        c = base[sc["side"]]
+        dx, rs, dy, zeta = pkg.cliffs_gpu.metrics(c["xcrd"], c["ycrd"], True)
+        g = pkg.GpuGrid(host[sc["side"]]["dep"], dx=dx, row_scale=rs, dy=dy, zeta=zeta, ground=c["ground"],
+                        crough=c["crough"], dt=c["dt"])
+        g.set_initial(host[sc["side"]]["H0"])
+        g.add_source(c["xcrd"], c["ycrd"], x0=sc["x0"], y0=sc["y0"], ax=sc["ax"], ay=sc["ay"],
+                     angle=sc["angle"], amp=sc["amp"], dipole=sc["dipole"])
+        grids.append(g)
+    b = pkg.Batch(grids)
+    b.set_gauges(gauges)
+    b.set_plan(pkg.cliffs_gpu.GRAPH, graph_steps=10, x_rows=2, y_groups=2)
+    for s0 in range(0, steps, 10):
+        b.step(min(10, steps - s0))
+        b.gauges(out=rec)
+    for g, out in zip(grids, maxes):
+        g.maxwave(out=out)
+    t = time.perf_counter() - t0
+    b.close()
+    for g in grids:
+        g.close()
+    h2d = sum(sc["side"] ** 2 * 8 * 2 for sc in scs)
+    d2h = sum(sc["side"] ** 2 * 4 * 2 for sc in scs) + (steps // 10) * m * 24
+    return {"value": round(n * steps / (E.RUN_STEPS * t), 3), "unit": f"scenarios/s ({E.RUN_STEPS}-step scenarios)",
+            "h2d_bytes_per_step": int(h2d // steps), "d2h_bytes_per_step": int(d2h // steps),
+            "ms": round(1e3 * t, 1), "gcell_per_s": round(cells * steps / t / 1e9, 2),
+            "plan": "graph of 10 steps, tile shape 2 x 2 (no autotuning inside the timed region)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,7 +551,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320"])
+    ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320", "ensemble256"])
     ap.add_argument("--sweep", default="tiled", choices=["tiled", "staged"],
                     help="sweep kernels of the device-resident passes (cliffs_gpu_set_sweep_kernel)")
     args = ap.parse_args()
@@ -404,6 +560,8 @@ def main():
     if args.warmup + args.steps > HORIZON:
         args.warmup = min(args.warmup, 100)
         args.steps = HORIZON - args.warmup
+    if args.workload == "ensemble256":
+        return run_ensemble(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -66,7 +66,7 @@ def source_field(x, y, *, x0, y0, ax, ay, angle=0.0, amp=1.0, dipole=0.0):
 
 class BatchPlan(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("graph_steps", ctypes.c_int32)]
+                ("graph_steps", ctypes.c_int32), ("x_rows", ctypes.c_int32), ("y_groups", ctypes.c_int32)]
 
 
 PERSISTENT, GRAPH = 0, 1
@@ -220,6 +220,8 @@ SIGNATURES = {
     "cliffs_batch_autotune": ([_V, _I, _dp], ctypes.c_int),
     "cliffs_batch_check_barrier_timeout": ([_V, _I], ctypes.c_int),
     "cliffs_batch_launch_count": ([_V, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "cliffs_batch_set_gauges": ([_V, _ip, _ip, _ip], ctypes.c_int),
+    "cliffs_batch_get_gauges": ([_V, _dp, _dp, _dp], ctypes.c_int),
     "cliffs_mlp_create": ([ctypes.c_void_p, ctypes.POINTER(_V)], ctypes.c_int),
     "cliffs_mlp_destroy": ([_V], None),
     "cliffs_mlp_layers": ([_V, ctypes.POINTER(_I)], ctypes.c_int),
@@ -613,19 +615,36 @@ class Batch:
         for g in self.grids:
             g.t.value += n * g.dt
 
-    def set_plan(self, mode, ctas_per_sm=1, graph_steps=32):
-        p = BatchPlan(int(mode), int(ctas_per_sm), int(graph_steps))
+    def set_plan(self, mode, ctas_per_sm=1, graph_steps=32, x_rows=1, y_groups=1):
+        p = BatchPlan(int(mode), int(ctas_per_sm), int(graph_steps), int(x_rows), int(y_groups))
         _chk(self.L.cliffs_batch_set_plan(self.h, ctypes.byref(p)), "batch_set_plan")
 
     def plan(self):
         p = BatchPlan()
         _chk(self.L.cliffs_batch_get_plan(self.h, ctypes.byref(p)), "batch_get_plan")
-        return dict(mode=p.mode, ctas_per_sm=p.ctas_per_sm, graph_steps=p.graph_steps)
+        return dict(mode=p.mode, ctas_per_sm=p.ctas_per_sm, graph_steps=p.graph_steps, x_rows=p.x_rows,
+                    y_groups=p.y_groups)
 
     def autotune(self, probe_steps=8):
         ms = ctypes.c_double()
         _chk(self.L.cliffs_batch_autotune(self.h, int(probe_steps), ctypes.byref(ms)), "batch_autotune")
         return ms.value
+
+    def set_gauges(self, gauges):
+        """gauges: one (I, J) pair of 1-based index arrays per grid."""
+        counts = np.array([len(I) for I, _ in gauges], np.int32)
+        I = np.ascontiguousarray(np.concatenate([np.asarray(I, np.int32) for I, _ in gauges]), np.int32)
+        J = np.ascontiguousarray(np.concatenate([np.asarray(J, np.int32) for _, J in gauges]), np.int32)
+        _chk(self.L.cliffs_batch_set_gauges(self.h, _p(counts, _ip), _p(I, _ip), _p(J, _ip)), "batch_set_gauges")
+        self.gauge_counts = counts
+
+    def gauges(self, out=None):
+        """(eta, u, v) of every grid's gauges, concatenated in grid order;
+        out: three float64 arrays to fill (pinned for a fast copy)."""
+        m = int(self.gauge_counts.sum())
+        eta, u, v = out if out is not None else (np.empty(m), np.empty(m), np.empty(m))
+        _chk(self.L.cliffs_batch_get_gauges(self.h, _p(eta), _p(u), _p(v)), "batch_get_gauges")
+        return eta, u, v
 
     def check_barrier_timeout(self, wait_ms=100):
         """Status of a launch whose grid barrier waits for an absent block."""

@@ -35,6 +35,9 @@ struct BatchArgs {
   unsigned long long wait_ns;  // limit of one barrier wait
   unsigned extra;         // arrivals a barrier waits for beyond the grid's
                           // blocks: 0, except in the timeout self-test
+  int span[2];            // tile shape: single-grid tiles per list entry, along
+                          // the rows (x-sweep: rows of 512 cells; y-sweep:
+                          // groups of 16 rows of 32 columns)
 };
 
 constexpr int kBatchThreads = 128;
@@ -52,13 +55,17 @@ __device__ __forceinline__ int batch_scenario(const int* off, int n, int t) {
   return lo;
 }
 
-// The tiles first, first + stride, ... of one sweep direction over all
-// scenarios.  The scenario's arguments are staged in shared memory.
+// The list entries first, first + stride, ... of one sweep direction over
+// all scenarios.  An entry is B.span[DIR] single-grid tiles along the rows: x,
+// span consecutive rows of one 512-cell column chunk; y, span consecutive
+// 16-row groups of one 32-column group.  The scenario's arguments are staged
+// in shared memory once per entry.
 template <int DIR, bool COH, bool MAXOUT>
 __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int stride) {
   __shared__ SweepArgs sA;
   const int* off = B.off + DIR * (B.n + 1);
   const int total = __ldg(off + B.n);
+  const int span = B.span[DIR];
   for (int t = first; t < total; t += stride) {
     const int k = batch_scenario(off, B.n, t);
     const int local = t - __ldg(off + k);
@@ -66,7 +73,14 @@ __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int s
     __syncthreads();  // the previous tile is done with sA and its shared list
     if (threadIdx.x == 0) sA = B.args[2 * k + DIR];
     __syncthreads();
-    sweep_tile<DIR, true, COH, true, MAXOUT>(sA, local % g, local / g);
+    if (DIR == 0) {  // g: column chunks; rows (local / g) * span ...
+      const int bx = local % g, by0 = (local / g) * span;
+      for (int r = 0; r < span && by0 + r < sA.nlines; ++r) sweep_tile<0, true, COH, true, MAXOUT>(sA, bx, by0 + r);
+    } else {  // g: entries along the column, each span row groups of 16
+      const int bx0 = (local % g) * span, by = local / g;
+      const int groups = (sA.n + (kBatchThreads / 32) * kCellsPerThread - 1) / ((kBatchThreads / 32) * kCellsPerThread);
+      for (int r = 0; r < span && bx0 + r < groups; ++r) sweep_tile<1, true, COH, true, MAXOUT>(sA, bx0 + r, by);
+    }
   }
 }
 

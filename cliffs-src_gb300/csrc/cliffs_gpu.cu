@@ -2449,9 +2449,19 @@ struct cliffs_batch {
   int* d_gx = nullptr;
   unsigned* d_sync = nullptr;  // [0] barrier counter, [1] timeout flag
   int total[2] = {0, 0};
-  cliffs_batch_plan plan{CLIFFS_BATCH_PERSISTENT, 1, 32};
-  cudaGraphExec_t graph = nullptr;
-  int graph_built = 0;  // steps in the instantiated graph
+  // per scenario, in single-grid tiles: x (column chunks, rows), y (row
+  // groups, column groups); the list of a plan's tile shape is built from them
+  std::vector<int> tx, ty, lx, ly;
+  cliffs_batch_plan plan{CLIFFS_BATCH_PERSISTENT, 1, 32, 1, 1};
+  // gauges of every scenario (cliffs_batch_set_gauges): scenario, I, J per
+  // entry, and the device record of (eta, u, v)
+  int32_t* d_gauge = nullptr;
+  double* d_grec = nullptr;
+  int gauges = 0;
+  // [0]: graph of plan.graph_steps steps; [1]: the last steps of a call,
+  // when fewer (at least 2)
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_built[2] = {0, 0};  // steps in each instantiated graph
   int64_t launches = 0;
 };
 
@@ -2466,16 +2476,41 @@ static BatchArgs batch_args(const cliffs_batch* b, int steps, bool fold) {
   B.err = b->d_sync + 1;
   B.wait_ns = kBarrierNs;
   B.extra = 0;
+  B.span[0] = std::max(1, b->plan.x_rows);
+  B.span[1] = std::max(1, b->plan.y_groups);
   return B;
 }
 
+// The tile lists of the plan's tile shape: per direction, the offset of each
+// scenario's first list entry and its entries along the first tile dimension.
+static int batch_lists(cliffs_batch* b) {
+  const int n = (int)b->ctx.size();
+  const int sx = std::max(1, b->plan.x_rows), sy = std::max(1, b->plan.y_groups);
+  std::vector<int> off(2 * ((size_t)n + 1), 0), gx(2 * (size_t)n, 0);
+  for (int k = 0; k < n; ++k) {
+    gx[k] = b->tx[k];                        // column chunks
+    gx[n + k] = (b->ty[k] + sy - 1) / sy;    // entries of sy row groups
+    off[k + 1] = off[k] + gx[k] * ((b->lx[k] + sx - 1) / sx);
+    off[(n + 1) + k + 1] = off[(n + 1) + k] + gx[n + k] * b->ly[k];
+  }
+  b->total[0] = off[n];
+  b->total[1] = off[(n + 1) + n];
+  if (cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) ||
+      cudaMemcpy(b->d_gx, gx.data(), gx.size() * sizeof(int), cudaMemcpyHostToDevice))
+    return CLIFFS_ERR_CUDA;
+  return CLIFFS_OK;
+}
+
 static void batch_free(cliffs_batch* b) {
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaGraphExec_t g : b->graph)
+    if (g) cudaGraphExecDestroy(g);
   if (b->d_args) cudaFree(b->d_args);
   if (b->d_args_fold) cudaFree(b->d_args_fold);
   if (b->d_off) cudaFree(b->d_off);
   if (b->d_gx) cudaFree(b->d_gx);
   if (b->d_sync) cudaFree(b->d_sync);
+  if (b->d_gauge) cudaFree(b->d_gauge);
+  if (b->d_grec) cudaFree(b->d_grec);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -2522,23 +2557,17 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
     fold[2 * k].hmax_in = c->hmax;
     fold[2 * k].velmax_in = c->velmax;
     fold[2 * k + 1] = sweep_args(c, 2, false, 1 - c->cur);
-    const int xgx = (c->nx + kBatchThreads * kCellsPerThread - 1) / (kBatchThreads * kCellsPerThread);
-    const int ygx = (c->ny + (kBatchThreads / 32) * kCellsPerThread - 1) / ((kBatchThreads / 32) * kCellsPerThread);
-    gx[k] = xgx;
-    gx[n + k] = ygx;
-    off[k + 1] = off[k] + xgx * c->ny;
-    off[(n + 1) + k + 1] = off[(n + 1) + k] + ygx * ((c->nx + 31) / 32);
+    b->tx.push_back((c->nx + kBatchThreads * kCellsPerThread - 1) / (kBatchThreads * kCellsPerThread));
+    b->lx.push_back(c->ny);
+    b->ty.push_back((c->ny + (kBatchThreads / 32) * kCellsPerThread - 1) / ((kBatchThreads / 32) * kCellsPerThread));
+    b->ly.push_back((c->nx + 31) / 32);
   }
-  b->total[0] = off[n];
-  b->total[1] = off[(n + 1) + n];
   if (dalloc(&b->d_args, args.size()) || dalloc(&b->d_args_fold, fold.size()) || dalloc(&b->d_off, off.size()) ||
       dalloc(&b->d_gx, gx.size()) || dalloc(&b->d_sync, 2))
     return fail(CLIFFS_ERR_NOMEM);
   if (cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
       cudaMemcpy(b->d_args_fold, fold.data(), fold.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
-      cudaMemcpy(b->d_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice) ||
-      cudaMemcpy(b->d_gx, gx.data(), gx.size() * sizeof(int), cudaMemcpyHostToDevice) ||
-      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking))
+      batch_lists(b) || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking))
     return fail(CLIFFS_ERR_CUDA);
   b->plan.mode = b->max_ctas > 0 ? CLIFFS_BATCH_PERSISTENT : CLIFFS_BATCH_GRAPH;
   b->plan.ctas_per_sm = std::max(1, b->max_ctas);
@@ -2563,7 +2592,22 @@ int cliffs_batch_set_plan(cliffs_batch* b, const cliffs_batch_plan* p) {
   } else {
     return CLIFFS_ERR_ARG;
   }
+  if (p->x_rows < 0 || p->x_rows > 64 || p->y_groups < 0 || p->y_groups > 64) return CLIFFS_ERR_ARG;
+  const bool shape = std::max(1, p->x_rows) != std::max(1, b->plan.x_rows) ||
+                     std::max(1, p->y_groups) != std::max(1, b->plan.y_groups);
   b->plan = *p;
+  b->plan.x_rows = std::max(1, p->x_rows);
+  b->plan.y_groups = std::max(1, p->y_groups);
+  if (shape) {
+    // the captured graphs hold the old list sizes
+    for (int s = 0; s < 2; ++s) {
+      if (b->graph[s]) cudaGraphExecDestroy(b->graph[s]);
+      b->graph[s] = nullptr;
+      b->graph_built[s] = 0;
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    RET(batch_lists(b));
+  }
   return CLIFFS_OK;
 }
 
@@ -2592,11 +2636,11 @@ static int batch_launch_phases(cliffs_batch* b, int steps, bool fold) {
   return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
 }
 
-static int batch_build_graph(cliffs_batch* b, int steps) {
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-    b->graph_built = 0;
+static int batch_build_graph(cliffs_batch* b, int slot, int steps) {
+  if (b->graph[slot]) {
+    cudaGraphExecDestroy(b->graph[slot]);
+    b->graph[slot] = nullptr;
+    b->graph_built[slot] = 0;
   }
   const int64_t before = b->launches;
   cudaGraph_t g = nullptr;
@@ -2608,10 +2652,13 @@ static int batch_build_graph(cliffs_batch* b, int steps) {
     if (g) cudaGraphDestroy(g);
     return CLIFFS_ERR_CUDA;
   }
-  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+  const cudaError_t ie = cudaGraphInstantiate(&b->graph[slot], g, 0);
   cudaGraphDestroy(g);
-  if (ie != cudaSuccess) return CLIFFS_ERR_CUDA;
-  b->graph_built = steps;
+  if (ie != cudaSuccess) {
+    b->graph[slot] = nullptr;
+    return CLIFFS_ERR_CUDA;
+  }
+  b->graph_built[slot] = steps;
   return CLIFFS_OK;
 }
 
@@ -2696,12 +2743,17 @@ int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
         r = CLIFFS_ERR_TIMEOUT;
     }
   } else {
+    // graph_steps steps per replay; the last steps of the call, when fewer
+    // but at least 2, from a graph of their own length
     const int k = b->plan.graph_steps;
-    if (nsteps >= k && b->graph_built != k) r = batch_build_graph(b, k);
     int done = 0;
-    for (; !r && done + k <= nsteps; done += k) {
-      if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
-      b->launches += 2 * (int64_t)k;
+    while (!r && nsteps - done >= 2 && k >= 2) {
+      const int len = std::min(k, nsteps - done);
+      const int slot = len == k ? 0 : 1;
+      if (b->graph_built[slot] != len) r = batch_build_graph(b, slot, len);
+      if (!r && cudaGraphLaunch(b->graph[slot], b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
+      b->launches += 2 * (int64_t)len;
+      done += len;
     }
     if (!r && done < nsteps) r = batch_launch_phases(b, nsteps - done, true);
     if (cudaStreamSynchronize(b->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
@@ -2709,6 +2761,66 @@ int cliffs_batch_step(cliffs_batch* b, int32_t nsteps) {
   if (!r)
     for (cliffs_ctx* c : b->ctx) c->sweeps += 2u * (unsigned)nsteps;
   return r;
+}
+
+// output_gages.f:18-29 for the gauges of every scenario: entry t samples
+// scenario sc[t] at (I[t], J[t]) in the state its next x-sweep reads.
+__global__ void k_batch_gauges(int m, const int32_t* __restrict__ sc, const int32_t* __restrict__ I,
+                               const int32_t* __restrict__ J, const SweepArgs* __restrict__ args, double* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const SweepArgs& A = args[2 * sc[t]];
+  const size_t q = (size_t)(J[t] - 1) * A.pitch + (size_t)(I[t] - 1);
+  const float d = A.dep[q], s = A.srf[q];
+  out[t] = depth_of(s, d) > A.ph.ground ? (double)eta_of(s, d) : (double)kNan4;
+  out[m + t] = A.xu[q];
+  out[2 * m + t] = A.yv[q];
+}
+
+int cliffs_batch_set_gauges(cliffs_batch* b, const int32_t* counts, const int32_t* I, const int32_t* J) {
+  if (!b || !counts || !I || !J) return CLIFFS_ERR_ARG;
+  const int n = (int)b->ctx.size();
+  std::vector<int32_t> h;
+  int m = 0;
+  for (int k = 0; k < n; ++k) {
+    if (counts[k] < 0) return CLIFFS_ERR_ARG;
+    m += counts[k];
+  }
+  if (m < 1) return CLIFFS_ERR_ARG;
+  h.resize(3 * (size_t)m);
+  for (int k = 0, t = 0; k < n; ++k)
+    for (int e = 0; e < counts[k]; ++e, ++t) {
+      const cliffs_ctx* c = b->ctx[k];
+      if (I[t] < 1 || I[t] > c->nx || J[t] < 1 || J[t] > c->ny) return CLIFFS_ERR_ARG;
+      h[t] = k;
+      h[m + t] = I[t];
+      h[2 * m + t] = J[t];
+    }
+  CK(cudaStreamSynchronize(b->stream));
+  if (b->d_gauge) cudaFree(b->d_gauge);
+  if (b->d_grec) cudaFree(b->d_grec);
+  b->d_gauge = nullptr;
+  b->d_grec = nullptr;
+  b->gauges = 0;
+  if (dalloc(&b->d_gauge, h.size()) || dalloc(&b->d_grec, 3 * (size_t)m)) return CLIFFS_ERR_NOMEM;
+  CK(cudaMemcpy(b->d_gauge, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  b->gauges = m;
+  return CLIFFS_OK;
+}
+
+int cliffs_batch_get_gauges(cliffs_batch* b, double* eta, double* u, double* v) {
+  if (!b || !eta || !u || !v) return CLIFFS_ERR_ARG;
+  if (b->gauges < 1) return CLIFFS_ERR_STATE;
+  const int m = b->gauges;
+  k_batch_gauges<<<(m + 127) / 128, 128, 0, b->stream>>>(m, b->d_gauge, b->d_gauge + m, b->d_gauge + 2 * m,
+                                                         b->d_args, b->d_grec);
+  CK(cudaGetLastError());
+  ++b->launches;
+  CK(cudaMemcpyAsync(eta, b->d_grec, m * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaMemcpyAsync(u, b->d_grec + m, m * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaMemcpyAsync(v, b->d_grec + 2 * m, m * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return CLIFFS_OK;
 }
 
 int cliffs_batch_check_barrier_timeout(cliffs_batch* b, int32_t wait_ms) {
@@ -2780,29 +2892,43 @@ int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_s
     cleanup();
     return r;
   }
+  // candidates: the schedule (persistent with 1..max resident blocks per SM,
+  // graphs of 8 or 32 steps) and the tile shape (rows per x entry, 16-row
+  // groups per y entry)
   std::vector<cliffs_batch_plan> cand;
-  for (int k = 1; k <= b->max_ctas; ++k) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_PERSISTENT, k, 32});
-  for (int g : {8, 32}) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_GRAPH, 1, g});
+  for (int k = 1; k <= b->max_ctas; ++k)
+    for (int sh : {1, 2}) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_PERSISTENT, k, 32, sh, sh});
+  for (int g : {8, 32})
+    for (int sx : {1, 2, 4})
+      for (int sy : {1, 2, 4}) cand.push_back(cliffs_batch_plan{CLIFFS_BATCH_GRAPH, 1, g, sx, sy});
   const cliffs_batch_plan keep = b->plan;
   cliffs_batch_plan best = keep;
   double best_ms = 1e300;
   const int64_t launches0 = b->launches;
+  int64_t probed = 0;  // steps the probes ran
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) || cudaEventCreate(&e1)) r = CLIFFS_ERR_CUDA;
   for (const cliffs_batch_plan& p : cand) {
     if (r) break;
-    b->plan = p;
-    r = cliffs_batch_step(b, 1);  // warm-up; builds the graph of a graph plan
+    r = cliffs_batch_set_plan(b, &p);
+    // a graph plan is timed on replays of its graph: the warm-up builds and
+    // replays it once, the timed steps are whole graphs
+    const bool graph = p.mode == CLIFFS_BATCH_GRAPH;
+    const int warm = graph ? p.graph_steps : 1;
+    const int steps = graph ? (std::max(probe_steps, p.graph_steps) + p.graph_steps - 1) / p.graph_steps * p.graph_steps
+                            : probe_steps;
+    if (!r) r = cliffs_batch_step(b, warm);
     if (!r && cudaEventRecord(e0, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
-    if (!r) r = cliffs_batch_step(b, probe_steps);
+    if (!r) r = cliffs_batch_step(b, steps);
     if (!r && cudaEventRecord(e1, b->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
     float ms = 0;
     if (!r && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
       r = CLIFFS_ERR_CUDA;
-    if (!r && ms / probe_steps < best_ms) {
-      best_ms = ms / probe_steps;
+    if (!r && ms / steps < best_ms) {
+      best_ms = ms / steps;
       best = p;
     }
+    probed += warm + steps;
     if (!r) r = copy_state(false);
     restore_rise();
   }
@@ -2810,11 +2936,11 @@ int cliffs_batch_autotune(cliffs_batch* b, int32_t probe_steps, double* ms_per_s
   if (e1) cudaEventDestroy(e1);
   // the probes advanced the contexts' sweep counters; the restored state is
   // the one before the probes
-  const int64_t probes = (int64_t)cand.size() * (probe_steps + 1);
-  for (cliffs_ctx* c : b->ctx) c->sweeps -= (unsigned)(2 * probes);
+  for (cliffs_ctx* c : b->ctx) c->sweeps -= (unsigned)(2 * probed);
   b->launches = launches0;
   cleanup();
-  b->plan = r ? keep : best;
+  const int rp = cliffs_batch_set_plan(b, r ? &keep : &best);
+  if (!r) r = rp;
   if (!r && ms_per_step) *ms_per_step = best_ms;
   return r;
 }

@@ -9,9 +9,10 @@ whose side is drawn from {256, 384, 512, 768, 1024} nodes at 100 m spacing
 its own seeded source (amplitude 0.5-5 m, half-widths 10-40 % of the domain,
 any angle, dipole ratio 0-0.5) applied on the device, 32 gauges per scenario.
 Both runs time `steps` steps of every scenario (host clock around the calls,
-synchronised) and report
-scenarios per second for a 2000-step run (the per-step time times 2000); the
-batched run first lets the autotuner pick its plan.  Prints one JSON line.
+synchronised), sampling every scenario's 32 gauges every 10 steps, and
+report scenarios per second for a 2000-step run (the per-step time times
+2000); the batched run first lets the autotuner pick its plan (schedule and
+tile shape).  Prints one JSON line.
 """
 import argparse
 import importlib
@@ -57,50 +58,75 @@ def make_grid(base, sc):
     return g
 
 
-def run(n=256, steps=200, seed=0):
+def run(n=256, steps=200, seed=0, warmup=2, gout=10, probe_steps=32, sequential=True):
+    """Time `steps` steps of every scenario batched (after the autotuner and
+    `warmup` steps), and one at a time; the 32 gauges of every scenario are
+    sampled every `gout` steps in both runs (cliffs_batch_get_gauges, one
+    launch for all scenarios; asynchronous gauge records per grid,
+    cliffs_gpu_get_gauges_async).  Host clock around calls that
+    synchronise."""
     import torch
 
     base = bathymetries(seed)
     scs = scenarios(n, seed)
     cells = sum(sc["side"] ** 2 for sc in scs)
+    gauges = [base[sc["side"]]["gauges"] for sc in scs]
+    m = sum(len(I) for I, _ in gauges)
+    rec = [pkg.cliffs_gpu.pinned((m,)) for _ in range(3)]
     # ---- batched
     grids = [make_grid(base[sc["side"]], sc) for sc in scs]
     b = pkg.Batch(grids)
-    tune_ms = b.autotune(4)
+    b.set_gauges(gauges)
+    tune_ms = b.autotune(probe_steps)
     plan = b.plan()
-    b.step(2)  # warm-up
+    b.step(warmup)
     torch.cuda.synchronize()
+    l0 = b.launches()
     t0 = time.perf_counter()
-    b.step(steps)
+    for s0 in range(0, steps, gout):
+        b.step(min(gout, steps - s0))
+        b.gauges(out=rec)
     t_batch = time.perf_counter() - t0
-    launches = b.launches()
+    launches = b.launches() - l0
     maxe = [g.maxwave()[0] for g in grids[:4]]
+    status = [g.status()[0] for g in grids]
     b.close()
     for g in grids:
         g.close()
     del grids
-    # ---- one at a time: each scenario's own grid, its own launches
+    out = dict(scenarios=n, steps_timed=steps, gauges_every=gout, gauges_total=m, cells_total=int(cells),
+               mean_cells=cells / n, plan=plan, autotune_ms_per_step=round(tune_ms, 4),
+               batched_ms_per_step=round(1e3 * t_batch / steps, 4),
+               batched_scenarios_per_s=round(n / (t_batch / steps * RUN_STEPS), 3),
+               batched_gcell_per_s=round(cells * steps / t_batch / 1e9, 2),
+               batch_launches=launches, sample_maxe=[float(np.max(x)) for x in maxe],
+               status_ok=all(r == 0 for r in status))
+    if not sequential:
+        return out
+    # ---- one at a time: each scenario's own grid, its own step graphs
     t_seq = 0.0
     for sc in scs:
         g = make_grid(base[sc["side"]], sc)
-        g.step(2)
+        I, J = base[sc["side"]]["gauges"]
+        g.set_graph_steps(gout)
+        g.step(warmup)
+        g.prepare_steps(gout)
         g.sync()
+        grec = pkg.cliffs_gpu.pinned((3, len(I)))
         t1 = time.perf_counter()
-        g.step(steps)
+        last = -1
+        for s0 in range(0, steps, gout):
+            g.step(min(gout, steps - s0))
+            last = g.gauges_async(I, J, (grec[0], grec[1], grec[2]))
+        g.wait(last)
         g.sync()
         t_seq += time.perf_counter() - t1
         g.close()
-    ms_b = 1e3 * t_batch / steps
-    ms_s = 1e3 * t_seq / steps
-    return dict(scenarios=n, steps_timed=steps, cells_total=int(cells), mean_cells=cells / n,
-                plan=plan, autotune_ms_per_step=round(tune_ms, 4),
-                batched_ms_per_step=round(ms_b, 4), sequential_ms_per_step=round(ms_s, 4),
-                batched_scenarios_per_s=round(n / (ms_b * RUN_STEPS / 1e3), 3),
-                sequential_scenarios_per_s=round(n / (ms_s * RUN_STEPS / 1e3), 3),
-                speedup=round(ms_s / ms_b, 3),
-                batched_gcell_per_s=round(cells / (ms_b / 1e3) / 1e9, 2),
-                sequential_gcell_per_s=round(cells / (ms_s / 1e3) / 1e9, 2),
-                batch_launches=launches, sample_maxe=[float(np.max(m)) for m in maxe])
+    out.update(sequential_ms_per_step=round(1e3 * t_seq / steps, 4),
+               sequential_scenarios_per_s=round(n / (t_seq / steps * RUN_STEPS), 3),
+               sequential_gcell_per_s=round(cells * steps / t_seq / 1e9, 2),
+               speedup=round(t_seq / t_batch, 3))
+    return out
 
 
 def main():

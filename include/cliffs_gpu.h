@@ -390,7 +390,13 @@ enum { CLIFFS_BATCH_PERSISTENT = 0, CLIFFS_BATCH_GRAPH = 1 };
 typedef struct cliffs_batch_plan {
   int32_t mode;         /* CLIFFS_BATCH_PERSISTENT or CLIFFS_BATCH_GRAPH */
   int32_t ctas_per_sm;  /* persistent: resident blocks per SM of the launch */
-  int32_t graph_steps;  /* graph: steps captured in one CUDA graph */
+  int32_t graph_steps;  /* graph: steps captured in one CUDA graph; the last
+                           steps of a call, when fewer (at least 2), replay
+                           from a graph of their own length */
+  int32_t x_rows;       /* tile shape, x phases: rows of one 512-cell column
+                           chunk per tile (1..64; 0 = 1) */
+  int32_t y_groups;     /* tile shape, y phases: 16-row groups of one
+                           32-column group per tile (1..64; 0 = 1) */
 } cliffs_batch_plan;
 
 int cliffs_batch_create(cliffs_ctx *const *ctxs, int32_t n, cliffs_batch **out);
@@ -401,10 +407,13 @@ int cliffs_batch_get_plan(const cliffs_batch *b, cliffs_batch_plan *plan);
  * CLIFFS_ERR_TIMEOUT if a grid barrier wait ran out (the state is then
  * partial). */
 int cliffs_batch_step(cliffs_batch *b, int32_t nsteps);
-/* Time the candidate plans (persistent with 1..max resident blocks per SM,
- * graphs of 8 and 32 steps) over probe_steps steps each from a snapshot of
- * the state, restore the snapshot and keep the fastest plan; *ms_per_step
- * gets its time per step. */
+/* Time the candidate plans from a snapshot of the state, restore the
+ * snapshot and keep the fastest plan; *ms_per_step gets its time per step.
+ * Candidates: persistent with 1..max resident blocks per SM (tile shapes
+ * 1x1 and 2x2), and graphs of 8 and 32 steps with x_rows and y_groups each
+ * in {1, 2, 4}.  A persistent plan is timed over probe_steps steps after one
+ * warm-up step; a graph plan over whole replays of its graph (at least
+ * probe_steps steps) after one replay that builds it. */
 int cliffs_batch_autotune(cliffs_batch *b, int32_t probe_steps, double *ms_per_step);
 /* Failure-detection check of the grid barrier: one persistent launch whose
  * first barrier waits for an arrival that no block makes, with the wait
@@ -412,6 +421,14 @@ int cliffs_batch_autotune(cliffs_batch *b, int32_t probe_steps, double *ms_per_s
  * the host, with the device usable afterwards.  The launch applies the
  * x-sweep of one step to the contexts before the barrier. */
 int cliffs_batch_check_barrier_timeout(cliffs_batch *b, int32_t wait_ms);
+/* Gauges of every scenario, sampled in one launch (output_gages.f:18-29 for
+ * all contexts of the batch).  set_gauges takes counts[n] (gauges per
+ * scenario, in the batch's context order) and the 1-based nodes I, J of all
+ * scenarios concatenated; get_gauges fills eta (-1e32 where dry), u, v in
+ * the same order, from the state after the last batch step, and
+ * synchronises. */
+int cliffs_batch_set_gauges(cliffs_batch *b, const int32_t *counts, const int32_t *I, const int32_t *J);
+int cliffs_batch_get_gauges(cliffs_batch *b, double *eta, double *u, double *v);
 /* Kernels the batch has launched (a persistent launch counts once). */
 int cliffs_batch_launch_count(const cliffs_batch *b, int64_t *n);
 

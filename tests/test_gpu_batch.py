@@ -61,12 +61,27 @@ def test_batch_is_bit_identical_to_single_grids():
         t.step(21)
     for g, t in zip(grids, twins):
         _same(g, t)
+    # tile shapes: 3 rows per x tile, 2 row groups per y tile, graphs of 8
+    # steps and a tail graph of 5; then persistent with 4 x 4
+    b.set_plan(cg.GRAPH, graph_steps=8, x_rows=3, y_groups=2)
+    b.step(21)
+    for t in twins:
+        t.step(21)
+    for g, t in zip(grids, twins):
+        _same(g, t)
+    b.set_plan(cg.PERSISTENT, ctas_per_sm=1, x_rows=4, y_groups=4)
+    b.step(9)
+    for t in twins:
+        t.step(9)
+    for g, t in zip(grids, twins):
+        _same(g, t)
     # the autotuner probes every plan from a snapshot and restores it
     before = [g.download_state() for g in grids]
     ms = b.autotune(4)
     assert ms > 0
     plan = b.plan()
     assert plan["mode"] in (cg.PERSISTENT, cg.GRAPH)
+    assert plan["x_rows"] in (1, 2, 4) and plan["y_groups"] in (1, 2, 4)
     for g, st in zip(grids, before):
         for x, y in zip(g.download_state(), st):
             assert np.array_equal(x, y)
@@ -156,4 +171,36 @@ def test_batch_after_single_steps_and_reads():
         g.step(3)
     for g, t in zip(grids, twins):
         _same(g, t)
+    b.close()
+
+
+def test_batch_gauges_match_single_grids():
+    """cliffs_batch_get_gauges samples every scenario's gauges in one launch;
+    the records equal each twin's own cliffs_gpu_get_gauges bit for bit,
+    at the start and after batched steps."""
+    cases = _cases()
+    rng = np.random.default_rng(5)
+    gauges = []
+    for c in cases:
+        ny, nx = c["dep"].shape
+        m = int(rng.integers(1, 9))
+        gauges.append((rng.integers(1, nx + 1, m).astype(np.int32), rng.integers(1, ny + 1, m).astype(np.int32)))
+    grids = [pkg.GpuGrid.from_case(c) for c in cases]
+    twins = [pkg.GpuGrid.from_case(c) for c in cases]
+    b = pkg.Batch(grids)
+    b.set_gauges(gauges)
+    b.set_plan(cg.GRAPH, graph_steps=8, x_rows=2, y_groups=2)
+    for n in (0, 13, 8):
+        if n:
+            b.step(n)
+            for t in twins:
+                t.step(n)
+        eta, u, v = b.gauges()
+        k = 0
+        for t, (I, J) in zip(twins, gauges):
+            te, tu, tv = t.gauges(I, J)
+            m = len(I)
+            assert np.array_equal(eta[k:k + m], te) and np.array_equal(u[k:k + m], tu)
+            assert np.array_equal(v[k:k + m], tv)
+            k += m
     b.close()
