@@ -21,6 +21,13 @@ the autotuner), 32 gauges per scenario sampled every 10 steps; the metric is
 scenarios/s for 2000-step scenarios, beside the same scenarios solved one at
 a time (each grid's own step graphs).
 
+--workload surrogate runs the learned-surrogate study: 4096 training runs of
+2000 steps on a 512^2 grid from the batched solver, an ensemble of 4 networks
+(MLP and conv decoder) trained by the library's kernels for --steps epochs,
+and the gated path on 256 held-out scenarios against one-at-a-time solves;
+the metric is scenarios/s of the gated path (surrogate plus solver
+fallbacks).
+
 --impl reference times the CPU restatement of the reference solver (the
 Fortran reference cannot be compiled on these hosts) with all host threads on
 the same workload.  With N > 1 (torchrun) every rank runs an independent
@@ -544,6 +551,96 @@ def ensemble_e2e(pkg, E, n, steps):
             "plan": "graph of 10 steps, tile shape 2 x 2 (no autotuning inside the timed region)"}
 
 
+def run_surrogate(args):
+    """The learned-surrogate line: gated scenarios/s against one-at-a-time
+    solves, with the surrogate's errors against the solver."""
+    import importlib
+
+    rank, world, local = _env_rank()
+    S = importlib.import_module("cliffs-src_gb300.surrogate")
+    epochs = max(1, args.steps)
+    config = {"workload": f"learned surrogate of {S.SIDE}x{S.SIDE} shelf runs at {S.DX:g} m, 2000 steps each: 8 "
+                          f"source parameters -> {S.NGAUGES} gauge maxima and a {S.MAP}x{S.MAP} max-inundation "
+                          f"map; 4096 training runs from the batched solver, 256 held-out scenarios; ensemble of "
+                          f"4 (MLP 9 -> 512 x 3, conv decoder {list(S.MAP_CH)}), {epochs} epochs",
+              "parallelism": "replicas only"}
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        threads = os.cpu_count() or 1
+        cb = surrogate_cpu_baseline(S, threads)
+        line = {"metric": "scenarios/s", "value": cb["value"], "unit": "scenarios/s", "n_gpus": args.gpus,
+                "steps": cb["steps"], "warmup": 1, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "implementation": "CPU restatement of the solver (oracle, OpenMP), one scenario after another",
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "scenarios/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    S.pkg.build.build()
+    with ClockSampler(local) as clk:
+        D = S.make_data(4096, 256, 2000, 0)
+        r = S.fit_and_judge(D, epochs=epochs, target=0.045, members=4)
+    peak = None
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    achieved = r["predict_flop"] / (r["predict_ms"] / 1e3) / 1e12  # the gated path's forward products
+    cb = surrogate_cpu_baseline(S, os.cpu_count() or 1) if rank == 0 else None
+    n_y = S.NGAUGES + S.MAP * S.MAP
+    line = {"metric": "scenarios/s", "value": r["gated_scenarios_per_s"], "unit": "scenarios/s", "n_gpus": world,
+            "steps": epochs, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 products, fp32 accumulation", "data": "synthetic", "config": config,
+            "implementation": "CUDA sm_103a: cliffs_batch_* (data), cliffs_mlp_* (training, inference)",
+            "timing": "host clock; the gated path is the ensemble's predictions plus one batched solve of the "
+                      "rejected scenarios (grid set-up, sources, steps, max-wave download)",
+            "one_at_a_time_scenarios_per_s": r["one_at_a_time_scenarios_per_s"],
+            "speedup_vs_one_at_a_time": r["gated_speedup_vs_one_at_a_time"],
+            "gauge_rel_err_gated_mean": r["gated_rel_err_mean"],
+            "gauge_rel_err_accepted_mean": r["gauge_rel_err_accepted_mean"],
+            "map_abs_err_mean_m": r["map_abs_err_mean_m"], "map_iou_mean": r["map_iou_mean"],
+            "map_max_depth_rel_err_mean": r["map_max_depth_rel_err_mean"],
+            "fallback": r["fallback"], "data_seconds": r["data_seconds"], "train_seconds": r["train_seconds"],
+            "e2e": {"value": r["gated_scenarios_per_s"], "unit": "scenarios/s",
+                    "h2d_bytes_per_step": 256 * S.N_FEATURES * 4, "d2h_bytes_per_step": 4 * 256 * n_y * 4,
+                    "what": "host parameters in, host gauge maxima and maps out (the predictions copy both ways)"},
+            "roofline": {"bound": "tensor", "kernel": "the ensemble's forward products (gemm_tn, mma.sync BF16)",
+                         "achieved": round(achieved, 3), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(achieved / peak, 5) if peak else None, "traffic": None},
+            "cpu_baseline": cb, "clocks": clk.summary(), "result": r}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def surrogate_cpu_baseline(S, threads, steps=100):
+    """The oracle's time loop on the surrogate's grid with one of its sources,
+    `steps` steps after one warm-up step; scenarios/s for 2000-step runs."""
+    import oracle  # noqa: F401
+    from tests.runners import oracle_model
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    base = S.base_grid(0)
+    p = S.sample_params(1, 3)[0]
+    L = base["xcrd"][-1]
+    src = S.source_of(p, L)
+    src.pop("rise_time")
+    c = dict(base)
+    c["H0"] = base["dep"] + S.cg.source_field(c["xcrd"], c["ycrd"], **src)
+    m = oracle_model(c)
+    m.step(1)
+    t0 = time.perf_counter()
+    m.step(steps)
+    t = (time.perf_counter() - t0) / steps
+    return {"value": round(1.0 / (t * 2000), 4), "unit": "scenarios/s", "cores": threads, "kind": "port",
+            "steps": steps, "ms_per_step": round(1e3 * t, 3),
+            "sample": f"one {S.SIDE}x{S.SIDE} scenario, {steps} time steps after 1 warm-up step, OpenMP over lines "
+                      f"({threads} threads), FP64; scenarios/s of 2000-step runs"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -551,7 +648,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320", "ensemble256"])
+    ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320", "ensemble256", "surrogate"])
     ap.add_argument("--sweep", default="tiled", choices=["tiled", "staged"],
                     help="sweep kernels of the device-resident passes (cliffs_gpu_set_sweep_kernel)")
     args = ap.parse_args()
@@ -562,6 +659,8 @@ def main():
         args.steps = HORIZON - args.warmup
     if args.workload == "ensemble256":
         return run_ensemble(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

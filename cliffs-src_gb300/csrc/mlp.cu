@@ -24,6 +24,7 @@
 
 #include "../../include/cliffs_gpu.h"
 #include "../../include/cliffs_surrogate.h"
+#include "decoder.cuh"
 
 namespace cliffs_nn {
 
@@ -35,8 +36,9 @@ inline int pad16(int n) { return (n + 15) & ~15; }
 struct Epi {
   const float* bias;  // [N] or null
   int relu;
-  float* f32;         // [M][ldf] or null
+  float* f32;         // [M][ldf] or null; split z of a split-K product at f32 + z * zstride
   int ldf;
+  long long zstride;
   bf16* b16;          // [M][ldb] or null
   int ldb;
   bf16* b16t;         // [N][ldt] (transposed) or null
@@ -54,13 +56,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 // C[M,N] = A[M,K] B[N,K]^T.  A and B are BF16 with K contiguous (leading
 // dimensions lda, ldb, multiples of 8, 16-byte aligned rows); K is a multiple
 // of 16 and both operands hold zeros in [K, round_up(K, 32)) or that range is
-// past the end of the tile load (guarded).  M and N are arbitrary.
+// past the end of the tile load (guarded).  M and N are arbitrary; M tiles
+// run along grid x.  Split K (gridDim.z > 1): block z reduces K range
+// [z kc, (z+1) kc) (kc a multiple of BK) and writes its partial product to
+// e.f32 + z * e.zstride.
 __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* __restrict__ A, int lda,
-                                               const bf16* __restrict__ B, int ldb, Epi e) {
+                                               const bf16* __restrict__ B, int ldb, Epi e, int kc) {
   __shared__ __align__(16) bf16 sA[BM][BK + PAD];
   __shared__ __align__(16) bf16 sB[BN][BK + PAD];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
   const int g = lane >> 2, t = lane & 3;
   float acc[2][4][4];
@@ -70,14 +75,15 @@ __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* 
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
+  for (int k0 = kb; k0 < ke; k0 += BK) {
     // 64 rows x 32 columns per operand: 256 chunks of 8 elements (16 B)
     for (int c = tid; c < 256; c += 128) {
       const int r = c >> 2, col = (c & 3) * 8;
       const int gk = k0 + col;
       uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-      if (m0 + r < M && gk < K) va = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + gk);
-      if (n0 + r < N && gk < K) vb = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + gk);
+      if (m0 + r < M && gk < ke) va = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + gk);
+      if (n0 + r < N && gk < ke) vb = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + gk);
       *reinterpret_cast<uint4*>(&sA[r][col]) = va;
       *reinterpret_cast<uint4*>(&sB[r][col]) = vb;
     }
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* 
         float v = acc[i][j][q];
         if (e.bias) v += e.bias[col];
         if (e.relu) v = fmaxf(v, 0.f);
-        if (e.f32) e.f32[(size_t)row * e.ldf + col] = v;
+        if (e.f32) e.f32[(size_t)blockIdx.z * e.zstride + (size_t)row * e.ldf + col] = v;
         const bf16 h = __float2bfloat16(v);
         if (e.b16) e.b16[(size_t)row * e.ldb + col] = h;
         if (e.b16t) e.b16t[(size_t)col * e.ldt + row] = h;
@@ -255,13 +261,41 @@ struct cliffs_mlp {
   int* idx = nullptr;
   int adam_t = 0;
   int64_t launches = 0;
+  // dense layers, and the map decoder (d.map_side > 0): latent cells, latent
+  // side, outputs of the last dense layer (n_out + latent), values per
+  // sample of y and of the targets (n_out + map cells), channels per level
+  int nd = 0;
+  int lat = 0, s0 = 0, n_total = 0, n_y = 0, side2 = 0;
+  int dc[4] = {0, 0, 0, 1};
+  bf16* X[3] = {nullptr, nullptr, nullptr};  // decoder level inputs, NHWC
+  float* map = nullptr;                      // [cap][side2]
+  bf16* col = nullptr;                       // im2col [P][kp] and its transpose
+  bf16* colt = nullptr;
+  float* dzf = nullptr;  // a level's output gradient, FP32 [P][Cout]
+  bf16* dzb = nullptr;   // ... in BF16 [P][pad16(Cout)]
+  bf16* dzt = nullptr;   // ... transposed [pad16(Cout)][P]
+  float* dxf = nullptr;  // a level's input gradient (levels 1, 2)
+  float* wpart = nullptr;  // split-K partials of a weight gradient
+  float* cpart = nullptr;  // column-sum partials of a bias gradient
+  float* part2 = nullptr;  // map loss partial sums
 };
 
 namespace {
 
 constexpr int kLossBlocks = 64;
 
+void free_decoder(cliffs_mlp* m) {
+  void* p[] = {m->X[0], m->X[1], m->X[2], m->map, m->col, m->colt, m->dzf, m->dzb, m->dzt, m->dxf, m->wpart,
+               m->cpart, m->part2};
+  for (void* q : p)
+    if (q) cudaFree(q);
+  m->X[0] = m->X[1] = m->X[2] = nullptr;
+  m->col = m->colt = m->dzb = m->dzt = nullptr;
+  m->map = m->dzf = m->dxf = m->wpart = m->cpart = m->part2 = nullptr;
+}
+
 void free_all(cliffs_mlp* m) {
+  free_decoder(m);
   for (Layer& l : m->L) {
     void* p[] = {l.w, l.b, l.gw, l.gb, l.mw, l.vw, l.mb, l.vb, l.W, l.Wt};
     for (void* q : p)
@@ -281,7 +315,23 @@ void free_all(cliffs_mlp* m) {
   m->idx = nullptr;
 }
 
-int max_n(const cliffs_mlp* m) { return std::max(m->d.width, m->d.n_out); }
+int max_n(const cliffs_mlp* m) { return std::max(m->d.width, m->n_total); }
+
+// Decoder level l (0..2): input side, input and output channels, im2col width.
+struct Level {
+  int S, cin, cout, K, kp;
+};
+Level level(const cliffs_mlp* m, int l) {
+  Level v;
+  v.S = m->s0 << l;
+  v.cin = m->dc[l];
+  v.cout = m->dc[l + 1];
+  v.K = 9 * v.cin;
+  v.kp = pad16(v.K);
+  return v;
+}
+constexpr int kWSplits = 128;  // split-K blocks of a decoder weight gradient
+constexpr int kCSplits = 256;  // row chunks of a decoder bias gradient
 
 // Activation buffers for batches up to cap.
 int ensure_cap(cliffs_mlp* m, int cap) {
@@ -293,30 +343,124 @@ int ensure_cap(cliffs_mlp* m, int cap) {
   void* p[] = {m->out, m->dyf, m->dh, m->dyb, m->dyt, m->part};
   for (void* q : p)
     if (q) cudaFree(q);
-  m->H.assign(m->L.size(), nullptr);
-  m->Ht.assign(m->L.size(), nullptr);
+  m->H.assign(m->nd, nullptr);  // inputs of the dense layers
+  m->Ht.assign(m->nd, nullptr);
   const int mn = max_n(m), mnp = pad16(mn);
-  for (size_t l = 0; l < m->L.size(); ++l) {
+  for (int l = 0; l < m->nd; ++l) {
     if (dalloc(&m->H[l], (size_t)cap * m->L[l].kp) || dalloc(&m->Ht[l], (size_t)m->L[l].kp * cap))
       return CLIFFS_ERR_NOMEM;
   }
-  if (dalloc(&m->out, (size_t)cap * m->d.n_out) || dalloc(&m->dyf, (size_t)cap * mn) ||
+  if (dalloc(&m->out, (size_t)cap * m->n_total) || dalloc(&m->dyf, (size_t)cap * mn) ||
       dalloc(&m->dh, (size_t)cap * mn) || dalloc(&m->dyb, (size_t)cap * mnp) || dalloc(&m->dyt, (size_t)mnp * cap) ||
       dalloc(&m->part, kLossBlocks))
     return CLIFFS_ERR_NOMEM;
+  if (m->d.map_side > 0) {
+    free_decoder(m);
+    size_t col = 0, dz = 0, dzp = 0, dx = 0, wp = 0;
+    for (int l = 0; l < 3; ++l) {
+      const Level v = level(m, l);
+      const size_t P = (size_t)cap * 4 * v.S * v.S;
+      col = std::max(col, P * v.kp);
+      dz = std::max(dz, P * v.cout);
+      dzp = std::max(dzp, P * pad16(v.cout));
+      if (l > 0) dx = std::max(dx, (size_t)cap * v.S * v.S * v.cin);
+      wp = std::max(wp, (size_t)kWSplits * v.cout * v.kp);
+      if (dalloc(&m->X[l], (size_t)cap * v.S * v.S * v.cin)) return CLIFFS_ERR_NOMEM;
+    }
+    if (dalloc(&m->map, (size_t)cap * m->side2) || dalloc(&m->col, col) || dalloc(&m->colt, col) ||
+        dalloc(&m->dzf, std::max(dz, dx)) || dalloc(&m->dzb, dzp) || dalloc(&m->dzt, dzp) ||
+        dalloc(&m->dxf, std::max(dz, dx)) || dalloc(&m->wpart, wp) || dalloc(&m->cpart, (size_t)kCSplits * 64) ||
+        dalloc(&m->part2, kLossBlocks))
+      return CLIFFS_ERR_NOMEM;
+  }
   m->cap = cap;
   return CLIFFS_OK;
 }
 
-void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e) {
-  const dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  gemm_tn<<<grid, 128, 0, m->stream>>>(M, N, K, A, lda, B, ldb, e);
+void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e,
+          int splits = 1) {
+  // split K: kc a multiple of BK, every split non-empty
+  const int kc = splits > 1 ? ((K + splits - 1) / splits + BK - 1) / BK * BK : K;
+  if (splits > 1) splits = (K + kc - 1) / kc;
+  const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
+  gemm_tn<<<grid, 128, 0, m->stream>>>(M, N, K, A, lda, B, ldb, e, splits > 1 ? kc : K);
   ++m->launches;
+}
+
+// Blocks of 256 threads covering n elements.
+inline unsigned blocks256(long long n) { return (unsigned)((n + 255) / 256); }
+
+// The map decoder's forward pass for rows [0, B): latent columns of out -> map.
+void decoder_forward(cliffs_mlp* m, int B) {
+  k_dec_input<<<blocks256((long long)B * m->lat), 256, 0, m->stream>>>(B, m->lat, m->out, m->n_total, m->d.n_out,
+                                                                       m->X[0]);
+  ++m->launches;
+  for (int l = 0; l < 3; ++l) {
+    const Level v = level(m, l);
+    const Layer& y = m->L[m->nd + l];
+    const int P = B * 4 * v.S * v.S;
+    k_im2col_up<<<blocks256((long long)P * v.kp), 256, 0, m->stream>>>(B, v.S, v.cin, m->X[l], v.kp, m->col,
+                                                                       nullptr, 0);
+    ++m->launches;
+    Epi e{};
+    e.bias = y.b;
+    if (l < 2) {
+      e.relu = 1;
+      e.b16 = m->X[l + 1];
+      e.ldb = v.cout;
+    } else {
+      e.f32 = m->map;
+      e.ldf = 1;
+    }
+    gemm(m, P, v.cout, v.kp, m->col, v.kp, y.W, y.kp, e);
+  }
+}
+
+// The map decoder's backward pass: the map gradient is in dzf ([B][side2]);
+// the gradients of the decoder's weights and biases, and the latent's into
+// dyf columns [n_out, n_total).
+void decoder_backward(cliffs_mlp* m, int B) {
+  for (int l = 2; l >= 0; --l) {
+    const Level v = level(m, l);
+    Layer& y = m->L[m->nd + l];
+    const int P = B * 4 * v.S * v.S;
+    const int cp = pad16(v.cout);
+    // the output gradient in BF16, rows and transpose (ReLU masks applied by
+    // the level above's input gradient)
+    k_pack_grad<<<blocks256((long long)P * cp), 256, 0, m->stream>>>(P, v.cout, cp, m->dzf, m->dzb, m->dzt);
+    // bias gradient: column sums in two stages
+    const int chunk = (P + kCSplits - 1) / kCSplits;
+    k_colsum_part<<<dim3((v.cout + 127) / 128, kCSplits), 128, 0, m->stream>>>(P, v.cout, chunk, m->dzf, m->cpart);
+    k_reduce_splits<<<(v.cout + 127) / 128, 128, 0, m->stream>>>(v.cout, kCSplits, m->cpart, y.gb);
+    // weight gradient dZ^T im2col, split over the pixels
+    k_im2col_up<<<blocks256((long long)P * v.kp), 256, 0, m->stream>>>(B, v.S, v.cin, m->X[l], v.kp, m->col,
+                                                                       m->colt, P);
+    Epi ew{};
+    ew.f32 = m->wpart;
+    ew.ldf = v.kp;
+    ew.zstride = (long long)v.cout * v.kp;
+    gemm(m, v.cout, v.kp, P, m->dzt, P, m->colt, P, ew, kWSplits);
+    const int kc = ((P + kWSplits - 1) / kWSplits + BK - 1) / BK * BK;
+    const int splits = (P + kc - 1) / kc;
+    k_reduce_wgrad<<<blocks256((long long)v.cout * v.K), 256, 0, m->stream>>>(v.cout, v.K, v.kp, splits, m->wpart,
+                                                                              y.gw);
+    // input gradient, masked by the level input's ReLU; level 0's goes to
+    // the latent columns of the dense output gradient
+    const long long nin = (long long)B * v.S * v.S * v.cin;
+    if (l > 0)
+      k_dec_dx<<<blocks256(nin), 256, 0, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, cp, y.W, y.kp, m->X[l],
+                                                      m->dxf, v.S * v.S * v.cin, 0);
+    else
+      k_dec_dx<<<blocks256(nin), 256, 0, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, cp, y.W, y.kp, m->X[0],
+                                                      m->dyf, m->n_total, m->d.n_out);
+    m->launches += 6;
+    if (l > 0) std::swap(m->dzf, m->dxf);  // the input gradient is the next level's output gradient
+  }
 }
 
 // Forward pass of rows [0, B) staged in H[0] (and Ht[0]); out gets the result.
 void forward(cliffs_mlp* m, int B) {
-  const int nl = (int)m->L.size();
+  const int nl = m->nd;
   for (int l = 0; l < nl; ++l) {
     const Layer& y = m->L[l];
     Epi e{};
@@ -329,10 +473,11 @@ void forward(cliffs_mlp* m, int B) {
       e.ldt = m->cap;
     } else {
       e.f32 = m->out;
-      e.ldf = m->d.n_out;
+      e.ldf = m->n_total;
     }
     gemm(m, B, y.rows, y.kp, m->H[l], y.kp, y.W, y.kp, e);
   }
+  if (m->d.map_side > 0) decoder_forward(m, B);
 }
 
 void stage_inputs(cliffs_mlp* m, int B, const float* x_dev, const int* idx) {
@@ -344,12 +489,23 @@ void stage_inputs(cliffs_mlp* m, int B, const float* x_dev, const int* idx) {
 // Loss and gradients of the batch staged by stage_inputs with targets t_dev
 // (rows idx); returns the sum of squared errors through *part on the device.
 void backward(cliffs_mlp* m, int B, const float* t_dev, const int* idx) {
-  const int nl = (int)m->L.size();
+  const int nl = m->nd;
   const int no = m->d.n_out;
-  // targets of the batch into dh (scratch), then dY of the output layer
-  k_gather<<<dim3((no + 127) / 128, B), 128, 0, m->stream>>>(B, no, t_dev, idx, m->dh);
-  k_mse<<<kLossBlocks, 256, 0, m->stream>>>(B * no, m->out, m->dh, m->dyf, 2.f / ((float)B * no), m->part);
-  m->launches += 2;
+  if (m->d.map_side > 0) {
+    // dense outputs: dY of their columns; the map: its gradient, then the
+    // decoder's backward pass fills the latent columns of dY
+    k_mse_block<<<kLossBlocks, 256, 0, m->stream>>>(B, no, m->out, m->n_total, 0, t_dev, m->n_y, 0, idx, m->dyf,
+                                                    m->n_total, 0, 2.f / ((float)B * no), m->part);
+    k_mse_block<<<kLossBlocks, 256, 0, m->stream>>>(B, m->side2, m->map, m->side2, 0, t_dev, m->n_y, no, idx,
+                                                    m->dzf, m->side2, 0, 2.f / ((float)B * m->side2), m->part2);
+    m->launches += 2;
+    decoder_backward(m, B);
+  } else {
+    // targets of the batch into dh (scratch), then dY of the output layer
+    k_gather<<<dim3((no + 127) / 128, B), 128, 0, m->stream>>>(B, no, t_dev, idx, m->dh);
+    k_mse<<<kLossBlocks, 256, 0, m->stream>>>(B * no, m->out, m->dh, m->dyf, 2.f / ((float)B * no), m->part);
+    m->launches += 2;
+  }
   for (int l = nl - 1; l >= 0; --l) {
     const Layer& y = m->L[l];
     const int N = y.rows, Np = y.rp;
@@ -416,24 +572,29 @@ int stage_data(cliffs_mlp* m, int n, const float* x, const float* t) {
     m->xs = m->ts = nullptr;
     m->idx = nullptr;
     m->staged = 0;
-    if (dalloc(&m->xs, (size_t)n * m->d.n_in) || dalloc(&m->ts, (size_t)n * m->d.n_out) || dalloc(&m->idx, n))
+    if (dalloc(&m->xs, (size_t)n * m->d.n_in) || dalloc(&m->ts, (size_t)n * m->n_y) || dalloc(&m->idx, n))
       return CLIFFS_ERR_NOMEM;
     m->staged = n;
   }
   if (cudaMemcpyAsync(m->xs, x, (size_t)n * m->d.n_in * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
     return CLIFFS_ERR_CUDA;
-  if (t && cudaMemcpyAsync(m->ts, t, (size_t)n * m->d.n_out * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
+  if (t && cudaMemcpyAsync(m->ts, t, (size_t)n * m->n_y * 4, cudaMemcpyHostToDevice, m->stream) != cudaSuccess)
     return CLIFFS_ERR_CUDA;
   return CLIFFS_OK;
 }
 
 float loss_of(cliffs_mlp* m, int B) {
-  float part[kLossBlocks];
+  float part[kLossBlocks], part2[kLossBlocks];
   cudaMemcpyAsync(part, m->part, sizeof(part), cudaMemcpyDeviceToHost, m->stream);
+  if (m->d.map_side > 0) cudaMemcpyAsync(part2, m->part2, sizeof(part2), cudaMemcpyDeviceToHost, m->stream);
   cudaStreamSynchronize(m->stream);
-  double s = 0;
+  double s = 0, s2 = 0;
   for (float p : part) s += p;
-  return (float)(s / ((double)B * m->d.n_out));
+  if (m->d.map_side > 0)
+    for (float p : part2) s2 += p;
+  double loss = s / ((double)B * m->d.n_out);
+  if (m->d.map_side > 0) loss += s2 / ((double)B * m->side2);
+  return (float)loss;
 }
 
 }  // namespace
@@ -442,10 +603,24 @@ int cliffs_mlp_create(const cliffs_mlp_desc* d, cliffs_mlp** out) {
   if (!d || !out || d->n_in < 1 || d->n_in > 16 || d->width < 16 || d->width % 16 || d->width > 4096 ||
       d->depth < 1 || d->depth > 16 || d->n_out < 1 || d->n_out > 16384)
     return CLIFFS_ERR_ARG;
+  if (d->map_side < 0 || d->map_side % 8 || d->map_side > 512) return CLIFFS_ERR_ARG;
+  if (d->map_side > 0)
+    for (int c : d->map_ch)
+      if (c < 8 || c % 8 || c > 64) return CLIFFS_ERR_ARG;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return CLIFFS_ERR_DEVICE;
   auto* m = new cliffs_mlp;
   m->d = *d;
+  m->nd = d->depth + 1;
+  if (d->map_side > 0) {
+    m->s0 = d->map_side / 8;
+    m->lat = m->s0 * m->s0 * d->map_ch[0];
+    m->side2 = d->map_side * d->map_side;
+    for (int k = 0; k < 3; ++k) m->dc[k] = d->map_ch[k];
+    m->dc[3] = 1;
+  }
+  m->n_total = d->n_out + m->lat;
+  m->n_y = d->n_out + m->side2;
   auto fail = [&](int r) {
     free_all(m);
     if (m->stream) cudaStreamDestroy(m->stream);
@@ -454,10 +629,17 @@ int cliffs_mlp_create(const cliffs_mlp_desc* d, cliffs_mlp** out) {
   };
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
   std::mt19937_64 rng(d->seed);
-  for (int l = 0; l <= d->depth; ++l) {
+  const int nlayers = m->nd + (d->map_side > 0 ? 3 : 0);
+  for (int l = 0; l < nlayers; ++l) {
     Layer y;
-    y.cols = l == 0 ? d->n_in : d->width;
-    y.rows = l == d->depth ? d->n_out : d->width;
+    const bool conv = l >= m->nd;
+    if (conv) {  // decoder level l - nd: [Cout][9 Cin]
+      y.cols = 9 * m->dc[l - m->nd];
+      y.rows = m->dc[l - m->nd + 1];
+    } else {
+      y.cols = l == 0 ? d->n_in : d->width;
+      y.rows = l == d->depth ? m->n_total : d->width;
+    }
     y.kp = pad16(y.cols);
     y.rp = pad16(y.rows);
     const size_t nw = (size_t)y.rows * y.cols;
@@ -467,8 +649,10 @@ int cliffs_mlp_create(const cliffs_mlp_desc* d, cliffs_mlp** out) {
       m->L.push_back(y);
       return fail(CLIFFS_ERR_NOMEM);
     }
-    // He uniform for ReLU layers, Glorot-like for the linear output layer
-    const double a = l < d->depth ? std::sqrt(6.0 / y.cols) : std::sqrt(3.0 / y.cols);
+    // He uniform for layers followed by a ReLU (the latent passes one),
+    // Glorot-like for the linear outputs
+    const bool relu_after = conv ? l < nlayers - 1 : (l < d->depth || d->map_side > 0);
+    const double a = relu_after ? std::sqrt(6.0 / y.cols) : std::sqrt(3.0 / y.cols);
     std::uniform_real_distribution<double> U(-a, a);
     std::vector<float> w(nw);
     for (float& v : w) v = (float)U(rng);
@@ -538,15 +722,22 @@ int cliffs_mlp_set(cliffs_mlp* m, int32_t l, int32_t which, const float* host, i
 
 int cliffs_mlp_predict(cliffs_mlp* m, int32_t batch, const float* x, float* y) {
   if (!m || batch < 1 || !x || !y) return CLIFFS_ERR_ARG;
-  const int chunk = 4096;
+  // the decoder's buffers grow with the batch: predict maps in chunks of 256
+  const int chunk = m->d.map_side > 0 ? 256 : 4096;
   int r = ensure_cap(m, pad16(std::min<int>(batch, chunk)));
   if (!r) r = stage_data(m, batch, x, nullptr);
   for (int s = 0; !r && s < batch; s += chunk) {
     const int B = std::min(chunk, batch - s);
     stage_inputs(m, B, m->xs + (size_t)s * m->d.n_in, nullptr);
     forward(m, B);
-    if (cudaMemcpyAsync(y + (size_t)s * m->d.n_out, m->out, (size_t)B * m->d.n_out * 4, cudaMemcpyDeviceToHost,
-                        m->stream) != cudaSuccess)
+    // rows of n_y: the dense outputs, then the map
+    float* yr = y + (size_t)s * m->n_y;
+    if (cudaMemcpy2DAsync(yr, (size_t)m->n_y * 4, m->out, (size_t)m->n_total * 4, (size_t)m->d.n_out * 4, B,
+                          cudaMemcpyDeviceToHost, m->stream) != cudaSuccess)
+      r = CLIFFS_ERR_CUDA;
+    if (!r && m->d.map_side > 0 &&
+        cudaMemcpy2DAsync(yr + m->d.n_out, (size_t)m->n_y * 4, m->map, (size_t)m->side2 * 4, (size_t)m->side2 * 4,
+                          B, cudaMemcpyDeviceToHost, m->stream) != cudaSuccess)
       r = CLIFFS_ERR_CUDA;
   }
   if (cudaStreamSynchronize(m->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;

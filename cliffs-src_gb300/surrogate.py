@@ -2,8 +2,11 @@
 
 The surrogate maps eight source parameters to the quantities a hazard study
 reads from a run: the maximum elevation at 64 gauges and the maximum
-elevation over a 128 x 128 window of the coast (learnt at 32 x 32, 4 x 4
-means, and returned upsampled).  Its training data are runs of the batched
+inundation depth (the largest flow depth over ground, MaxE + dep on land,
+0 where the sea never reached) over a 128 x 128 window of the coast.  A
+4-layer MLP (width 512) gives the gauge maxima and a latent 16 x 16 x 32 grid,
+which a conv decoder (three 2x upsampling + 3x3 convolution levels) turns
+into the 128 x 128 map.  Its training data are runs of the batched
 solver (cliffs_batch_*) on one 512 x 512 shelf/slope grid at 100 m, every
 source applied on the device (cliffs_gpu_add_source, rising over its rise
 time); the network is trained on the GPU by the library's own kernels (BF16
@@ -43,7 +46,8 @@ SIDE = 512
 DX = 100.0
 NGAUGES = 64
 WIN = (slice(192, 320), slice(SIDE - 128, SIDE))  # rows, columns of the coastal window
-POOL = 4
+MAP = 128                 # the window's side: the decoder's map
+MAP_CH = (32, 16, 8)      # decoder channels: latent 16 x 16 x 32, levels of 16 and 8
 # parameter ranges, as fractions of the domain length where spatial
 LO = np.array([0.15, 0.20, 0.5, 0.05, 0.05, 0.0, 0.0, 0.0])
 HI = np.array([0.50, 0.80, 3.0, 0.20, 0.20, np.pi, 0.6, 60.0])
@@ -52,7 +56,8 @@ NAMES = ["x0", "y0", "amp", "ax", "ay", "angle", "dipole", "rise_time"]
 
 class MlpDesc(ctypes.Structure):
     _fields_ = [("n_in", ctypes.c_int32), ("width", ctypes.c_int32), ("depth", ctypes.c_int32),
-                ("n_out", ctypes.c_int32), ("seed", ctypes.c_uint64)]
+                ("n_out", ctypes.c_int32), ("seed", ctypes.c_uint64), ("map_side", ctypes.c_int32),
+                ("map_ch", ctypes.c_int32 * 3)]
 
 
 _fp = ctypes.POINTER(ctypes.c_float)
@@ -63,15 +68,18 @@ def _f32(a):
 
 
 class MLP:
-    """One network (cliffs_mlp_*)."""
+    """One network (cliffs_mlp_*): n_out dense outputs and, with map_side > 0,
+    a map_side x map_side map from the conv decoder (channels map_ch)."""
 
-    def __init__(self, n_in, width, depth, n_out, seed=0):
+    def __init__(self, n_in, width, depth, n_out, seed=0, map_side=0, map_ch=(32, 16, 8)):
         self.L = cg.load()
-        d = MlpDesc(n_in, width, depth, n_out, seed)
+        d = MlpDesc(n_in, width, depth, n_out, seed, map_side, (ctypes.c_int32 * 3)(*map_ch))
         h = ctypes.c_void_p()
         cg._chk(self.L.cliffs_mlp_create(ctypes.byref(d), ctypes.byref(h)), "mlp_create")
         self.h = h
         self.n_in, self.n_out = n_in, n_out
+        self.map_side = map_side
+        self.n_y = n_out + map_side * map_side
 
     def close(self):
         if getattr(self, "h", None):
@@ -110,7 +118,7 @@ class MLP:
 
     def predict(self, x):
         x = _f32(x)
-        y = np.zeros((x.shape[0], self.n_out), np.float32)
+        y = np.zeros((x.shape[0], self.n_y), np.float32)
         cg._chk(self.L.cliffs_mlp_predict(self.h, x.shape[0], x.ctypes.data_as(_fp), y.ctypes.data_as(_fp)),
                 "mlp_predict")
         return y
@@ -153,22 +161,24 @@ def source_of(p, L):
                 rise_time=p[7])
 
 
-def targets_of(maxe, I, J):
-    """Gauge maxima (64) and the pooled coastal window (32 x 32) from MaxE;
-    never-wet cells count as 0."""
+def targets_of(maxe, I, J, dep):
+    """Gauge maxima (64, never-wet gauges count as 0) and the maximum
+    inundation depth over the coastal window (128 x 128): MaxE + dep on land
+    cells (dep < 0) the sea reached, 0 elsewhere (sea cells, dry land)."""
     m = np.where(maxe > -1e30, maxe, 0.0).astype(np.float64)
     g = np.maximum(m[J - 1, I - 1], 0.0)
-    w = np.maximum(m[WIN], 0.0)
-    pooled = w.reshape(128 // POOL, POOL, 128 // POOL, POOL).mean(axis=(1, 3))
-    return g, pooled.ravel(), w
+    w, d = maxe[WIN].astype(np.float64), dep[WIN]
+    inund = np.where((d < 0) & (w > -1e30), np.maximum(w + d, 0.0), 0.0)
+    return g, inund
 
 
 def solve(params, base, steps, chunk=512):
-    """Runs of the batched solver; returns gauge maxima, pooled windows, full
-    windows, the solver time (s) and the number of runs with a non-finite state."""
+    """Runs of the batched solver; returns gauge maxima, inundation maps,
+    the solver time (s) and the number of runs with a non-finite state."""
     L = base["xcrd"][-1]
     I, J = base["gauges"]
-    G, P, F = [], [], []
+    dep = base["dep"].astype(np.float32).astype(np.float64)
+    G, M = [], []
     t_solve, bad = 0.0, 0
     for s in range(0, len(params), chunk):
         grids = []
@@ -185,36 +195,35 @@ def solve(params, base, steps, chunk=512):
             r, flags = g.status()
             bad += int(r != 0)
             me, _ = g.maxwave()
-            gg, pp, ww = targets_of(me, I, J)
+            gg, mm = targets_of(me, I, J, dep)
             G.append(gg)
-            P.append(pp)
-            F.append(ww)
+            M.append(mm.astype(np.float32))
             g.close()
         b.close()
-    return np.array(G), np.array(P), np.array(F), t_solve, bad
+    return np.array(G), np.array(M), t_solve, bad
 
 
 # ---- the surrogate ---------------------------------------------------------------
 
 class Norm:
     """Inputs to [-1, 1]; gauge maxima as standardised log(max + 0.01),
-    weighted x4 so that the 64 gauges weigh as much as the 1024 map cells;
-    map cells standardised.
+    weighted by GW against the map; inundation maps scaled by one number (the
+    RMS of the training maps).
 
-    per_amp: targets per metre of source amplitude (max / amp, window / amp).
+    per_amp: targets per metre of source amplitude (max / amp, map / amp).
     Offshore the response is close to linear in the amplitude, so the network
     then learns the shape of the response rather than its scale."""
 
-    GW = 4.0
+    GW = 2.0
 
-    def __init__(self, G, P, params=None, per_amp=True):
+    def __init__(self, G, M, params=None, per_amp=True):
         self.per_amp = per_amp
         if per_amp:
             a = params[:, 2:3]
-            G, P = G / a, P / a
+            G, M = G / a, M / a[:, :, None]
         lg = np.log(G + 0.01)
         self.gm, self.gs = lg.mean(0), lg.std(0) + 1e-6
-        self.pm, self.ps = P.mean(0), P.std(0) + 1e-3
+        self.ms = float(np.sqrt(np.mean(np.square(M)))) + 1e-6
 
     def x(self, params):
         """Features: the parameters scaled to [-1, 1], with the amplitude as its
@@ -224,31 +233,19 @@ class Norm:
         z[:, 2] = 2.0 * (la - np.log(LO[2])) / (np.log(HI[2]) - np.log(LO[2])) - 1.0
         return np.hstack([z[:, :5], np.cos(params[:, 5:6]), np.sin(params[:, 5:6]), z[:, 6:]])
 
-    def t(self, G, P, params=None):
+    def t(self, G, M, params=None):
         if self.per_amp:
             a = params[:, 2:3]
-            G, P = G / a, P / a
-        return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, (P - self.pm) / self.ps])
+            G, M = G / a, M / a[:, :, None]
+        return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, M.reshape(len(M), -1) / self.ms])
 
     def back(self, Y, params=None):
         g = np.exp(Y[:, :NGAUGES] / self.GW * self.gs + self.gm) - 0.01
-        p = Y[:, NGAUGES:] * self.ps + self.pm
+        m = Y[:, NGAUGES:].reshape(len(Y), MAP, MAP) * self.ms
         if self.per_amp:
             a = params[:, 2:3]
-            g, p = g * a, p * a
-        return np.maximum(g, 0.0), np.maximum(p, 0.0)
-
-
-def upsample(pooled):
-    """32 x 32 -> 128 x 128, bilinear on cell centres (edges held)."""
-    n = pooled.shape[0]
-    a = pooled.reshape(n, 128 // POOL, 128 // POOL)
-    c = (np.arange(128) + 0.5) / POOL - 0.5
-    i0 = np.clip(np.floor(c).astype(int), 0, 128 // POOL - 1)
-    i1 = np.clip(i0 + 1, 0, 128 // POOL - 1)
-    f = np.clip(c - i0, 0.0, 1.0)
-    r = a[:, i0, :] * (1 - f)[None, :, None] + a[:, i1, :] * f[None, :, None]
-    return r[:, :, i0] * (1 - f)[None, None, :] + r[:, :, i1] * f[None, None, :]
+            g, m = g * a, m * a[:, :, None]
+        return np.maximum(g, 0.0), np.maximum(m, 0.0)
 
 
 N_FEATURES = 9  # Norm.x
@@ -256,7 +253,7 @@ N_FEATURES = 9  # Norm.x
 
 class Ensemble:
     def __init__(self, members=4, width=512, depth=3, seed=0):
-        self.nets = [MLP(N_FEATURES, width, depth, NGAUGES + (128 // POOL) ** 2, seed=seed + 101 * k)
+        self.nets = [MLP(N_FEATURES, width, depth, NGAUGES, seed=seed + 101 * k, map_side=MAP, map_ch=MAP_CH)
                      for k in range(members)]
 
     def train(self, X, T, epochs, batch=512, lr=1e-3, seed=0, weight_decay=0.0):
@@ -266,12 +263,27 @@ class Ensemble:
     def predict(self, X, norm, params=None):
         outs = [norm.back(net.predict(X), params) for net in self.nets]
         G = np.stack([o[0] for o in outs])  # (members, n, 64)
-        P = np.stack([o[1] for o in outs])
-        return G.mean(0), P.mean(0), G
+        M = np.stack([o[1] for o in outs])  # (members, n, 128, 128)
+        return G.mean(0), M.mean(0), G
 
     def close(self):
         for n in self.nets:
             n.close()
+
+
+def forward_flop(width=512, depth=3):
+    """Multiply-add FLOPs of one network's forward pass for one sample: the
+    dense layers (the last emits the gauges and the latent grid) and the
+    decoder's three convolutions (3x3 taps on the upsampled grids)."""
+    s0 = MAP // 8
+    lat = s0 * s0 * MAP_CH[0]
+    dims = [N_FEATURES] + [width] * depth + [NGAUGES + lat]
+    fl = sum(2 * a * b for a, b in zip(dims[:-1], dims[1:]))
+    ch = list(MAP_CH) + [1]
+    for l in range(3):
+        side = 2 * s0 << l
+        fl += 2 * side * side * ch[l + 1] * 9 * ch[l]
+    return fl
 
 
 def spread(Gm, floor=0.05):
@@ -312,27 +324,47 @@ def make_data(n_train=4096, n_test=256, steps=2000, seed=0):
     Xall = sample_params(n_train, seed + 1)
     Xte = sample_params(n_test, seed + 2)
     t0 = time.perf_counter()
-    Gall, Pall, _, t_data, bad_tr = solve(Xall, base, steps)
+    Gall, Mall, t_data, bad_tr = solve(Xall, base, steps)
     t_gen = time.perf_counter() - t0
-    Gte, Pte, Fte, t_test_solve, bad_te = solve(Xte, base, steps)
-    return dict(base=base, steps=steps, Xall=Xall, Gall=Gall, Pall=Pall, Xte=Xte, Gte=Gte, Pte=Pte, Fte=Fte,
+    Gte, Mte, t_test_solve, bad_te = solve(Xte, base, steps)
+    return dict(base=base, steps=steps, Xall=Xall, Gall=Gall, Mall=Mall, Xte=Xte, Gte=Gte, Mte=Mte,
                 t_gen=t_gen, t_data=t_data, t_test_solve=t_test_solve, bad=int(bad_tr + bad_te))
 
 
+def map_errors(Mp, M, floor=0.05):
+    """The inundation maps against the solver's: mean absolute error over the
+    window (m), over the cells either inundates by more than `floor` m, the
+    relative error of each scenario's largest depth, and the intersection
+    over union of the inundated footprints (depth > floor)."""
+    a, b = Mp > floor, M > floor
+    either = a | b
+    inter = (a & b).sum(axis=(1, 2))
+    union = either.sum(axis=(1, 2))
+    iou = np.where(union > 0, inter / np.maximum(union, 1), 1.0)
+    mx = M.max(axis=(1, 2))
+    rel_max = np.abs(Mp.max(axis=(1, 2)) - mx) / np.maximum(mx, 1e-9)
+    has = mx > floor
+    return dict(map_abs_err_mean_m=float(np.abs(Mp - M).mean()),
+                map_abs_err_inundated_m=float(np.abs(Mp - M)[either].mean()) if either.any() else 0.0,
+                map_max_depth_mean_m=float(mx.mean()),
+                map_max_depth_rel_err_mean=float(rel_max[has].mean()) if has.any() else 0.0,
+                map_iou_mean=float(iou.mean()), map_scenarios_inundated=int(has.sum()))
+
+
 def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True, width=512, depth=3,
-                  members=4, single=None):
+                  members=4, single=None, batch=512, lr=1e-3):
     """Train the ensemble on the training runs, calibrate its gate on the
     validation split, judge it on the held-out runs against the solver.
     single: seconds of one one-at-a-time solve (measured here when None)."""
     base, steps = D["base"], D["steps"]
-    Xall, Gall, Pall, Xte, Gte, Fte = D["Xall"], D["Gall"], D["Pall"], D["Xte"], D["Gte"], D["Fte"]
+    Xall, Gall, Mall, Xte, Gte, Mte = D["Xall"], D["Gall"], D["Mall"], D["Xte"], D["Gte"], D["Mte"]
     n_test = len(Xte)
-    Xtr, Gtr, Ptr = Xall[n_val:], Gall[n_val:], Pall[n_val:]
+    Xtr, Gtr, Mtr = Xall[n_val:], Gall[n_val:], Mall[n_val:]
     Xva, Gva = Xall[:n_val], Gall[:n_val]
-    norm = Norm(Gtr, Ptr, Xtr, per_amp=per_amp)
+    norm = Norm(Gtr, Mtr, Xtr, per_amp=per_amp)
     ens = Ensemble(members=members, width=width, depth=depth, seed=seed)
     t0 = time.perf_counter()
-    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Ptr, Xtr), epochs)
+    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Mtr, Xtr), epochs, batch=batch, lr=lr)
     t_train = time.perf_counter() - t0
     # the gate, from the validation split
     Gv, _, Gvm = ens.predict(norm.x(Xva), norm, Xva)
@@ -340,13 +372,13 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
     thr = calibrate_gate(spread(Gvm), rel_v, mask_v, target)
     # the surrogate path on the test split: ensemble prediction, then the gate
     t0 = time.perf_counter()
-    Gp, Pp, Gm = ens.predict(norm.x(Xte), norm, Xte)
+    Gp, Mp, Gm = ens.predict(norm.x(Xte), norm, Xte)
     sp = spread(Gm)
     accept = sp <= thr
     t_pred = time.perf_counter() - t0
     rel, mask, _ = gauge_errors(Gp, Gte)
     rel_acc = rel[accept[:, None] & mask]
-    win_err = np.abs(upsample(Pp) - Fte)  # m, on the full 128 x 128 window
+    merr = map_errors(Mp, Mte)
     # one-at-a-time solves of a few test scenarios: the method without the surrogate
     if single is None:
         n_single = min(16, n_test)
@@ -371,12 +403,13 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
     t_fb = 0.0
     if n_fallback:
         t0 = time.perf_counter()
-        Gfb, _, _, _, _ = solve(Xte[rej], base, steps)
+        Gfb, _, _, _ = solve(Xte[rej], base, steps)
         t_fb = time.perf_counter() - t0
         assert np.array_equal(Gfb, Gte[rej])  # batching does not change a run
     t_gated = t_pred + t_fb
     res = dict(train=len(Xtr), validation=n_val, test=n_test, steps=steps, epochs=epochs, target=target,
-               per_amp=per_amp, width=width, depth=depth, members=members, nonfinite_runs=D["bad"],
+               per_amp=per_amp, width=width, depth=depth, members=members, map=[MAP, MAP], map_channels=MAP_CH,
+               nonfinite_runs=D["bad"],
                data_seconds=round(D["t_gen"], 2), solver_seconds_train=round(D["t_data"], 2),
                train_seconds=round(t_train, 2),
                final_loss=[round(float(l[-1]), 5) for l in losses],
@@ -387,9 +420,9 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
                gauge_rel_err_accepted_mean=round(float(rel_acc.mean()), 4) if rel_acc.size else None,
                gauge_rel_err_accepted_median=round(float(np.median(rel_acc)), 4) if rel_acc.size else None,
                gated_rel_err_mean=round(float(np.where(accept[:, None], rel, 0.0)[mask].mean()), 4),
-               window_abs_err_mean_m=round(float(win_err.mean()), 4),
-               window_max_mean_m=round(float(Fte.max(axis=(1, 2)).mean()), 4),
+               **{k: round(v, 4) if isinstance(v, float) else v for k, v in merr.items()},
                predict_ms=round(1e3 * t_pred, 3), fallback_solve_ms=round(1e3 * t_fb, 2),
+               predict_flop=int(forward_flop(width, depth) * members * n_test),
                single_solve_s=round(per_single, 4), batched_solve_s_per_scenario=round(per_batch, 5),
                surrogate_scenarios_per_s=round(n_test / t_pred, 1),
                gated_scenarios_per_s=round(n_test / t_gated, 1),

@@ -1,7 +1,8 @@
 /* cliffs_surrogate.h -- a learned surrogate of the solver for source studies.
  *
  * No reference counterpart: the reference is the solver only.  The surrogate
- * is a multilayer perceptron mapping a source's parameters to quantities of
+ * is a multilayer perceptron, with an optional conv decoder for a map,
+ * mapping a source's parameters to quantities of
  * interest of the run (gauge maxima, a coarse max-inundation map), trained on
  * runs of the batched solver (cliffs_batch_*) and used with an ensemble of
  * independently initialised members whose disagreement sends a scenario back
@@ -25,14 +26,28 @@ typedef struct cliffs_mlp_desc {
   int32_t n_in;   /* inputs (1..16) */
   int32_t width;  /* hidden width (multiple of 16, <= 4096) */
   int32_t depth;  /* hidden layers (1..16) */
-  int32_t n_out;  /* outputs (1..16384) */
+  int32_t n_out;  /* dense outputs (1..16384) */
   uint64_t seed;  /* weight initialisation (He uniform) */
+  /* Optional map decoder (map_side = 0: none).  The last dense layer then
+   * also emits a latent grid of (map_side/8)^2 cells with map_ch[0]
+   * channels; the decoder takes it through a ReLU and three levels, each a
+   * 2x nearest-neighbour upsampling and a 3x3 convolution (zero padding)
+   * with a bias: map_ch[0] -> map_ch[1] -> map_ch[2] channels with ReLUs,
+   * then map_ch[2] -> 1 channel, a map_side x map_side map.  map_side: a
+   * multiple of 8, <= 512; channels: multiples of 8, <= 64.  Convolutions
+   * run as BF16 tensor-core products (im2col, FP32 accumulation); their
+   * weight gradients as split-K tensor-core products, their input gradients
+   * as FP32 sums of BF16 products. */
+  int32_t map_side;
+  int32_t map_ch[3];
 } cliffs_mlp_desc;
 
 int cliffs_mlp_create(const cliffs_mlp_desc *d, cliffs_mlp **out);
 void cliffs_mlp_destroy(cliffs_mlp *m);
-/* Number of layers (depth + 1) and the shape of layer l's weight (rows =
- * outputs, cols = inputs). */
+/* Number of layers (depth + 1, plus 3 decoder levels with a map) and the
+ * shape of layer l's weight (rows = outputs, cols = inputs; a decoder level:
+ * rows = output channels, cols = 9 * input channels, the tap (ty*3 + tx)
+ * major and the input channel minor). */
 int cliffs_mlp_layers(const cliffs_mlp *m, int32_t *n_layers);
 int cliffs_mlp_shape(const cliffs_mlp *m, int32_t layer, int32_t *rows, int32_t *cols);
 
@@ -42,12 +57,15 @@ int cliffs_mlp_shape(const cliffs_mlp *m, int32_t layer, int32_t *rows, int32_t 
 int cliffs_mlp_get(const cliffs_mlp *m, int32_t layer, int32_t which, float *host, int64_t n);
 int cliffs_mlp_set(cliffs_mlp *m, int32_t layer, int32_t which, const float *host, int64_t n);
 
-/* y (batch x n_out) = f(x (batch x n_in)). */
+/* y (batch x n_y) = f(x (batch x n_in)); n_y = n_out, plus map_side^2 map
+ * cells (row-major) after the dense outputs with a map decoder. */
 int cliffs_mlp_predict(cliffs_mlp *m, int32_t batch, const float *x, float *y);
-/* Loss (mean squared error over batch and outputs) and gradients of every
- * parameter for one batch, without an update.  batch: multiple of 16. */
+/* Loss and gradients of every parameter for one batch, without an update.
+ * batch: multiple of 16.  Targets t: batch x n_y, laid out as y.  The loss
+ * is the mean squared error over the batch and the dense outputs, plus that
+ * over the batch and the map cells with a map decoder. */
 int cliffs_mlp_gradients(cliffs_mlp *m, int32_t batch, const float *x, const float *t, float *loss);
-/* Train with Adam on n samples (x: n x n_in, t: n x n_out): `epochs` passes
+/* Train with Adam on n samples (x: n x n_in, t: n x n_y): `epochs` passes
  * over a seeded shuffle in batches of `batch` (multiple of 16; the last
  * partial batch of an epoch is left out), learning rate lr with a cosine
  * decay to lr/20, decoupled weight decay weight_decay on the weights (not the

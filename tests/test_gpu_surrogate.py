@@ -12,7 +12,7 @@ import importlib
 import numpy as np
 import pytest
 
-from oracle.surrogate import MLPRef
+from oracle.surrogate import MapNetRef, MLPRef
 
 pytestmark = pytest.mark.gpu
 S = importlib.import_module("cliffs-src_gb300.surrogate")
@@ -44,6 +44,37 @@ def test_forward_and_gradients_against_oracle(shape, batch):
     for l in range(depth + 1):
         assert _rel(gW[l], rW[l]) <= 5e-3, l
         assert _rel(gb[l], rb[l]) <= 5e-3, l
+    net.close()
+
+
+@pytest.mark.parametrize("side,ch,batch", [(32, (16, 8, 8), 32), (128, (32, 16, 8), 16)])
+def test_map_decoder_against_oracle(side, ch, batch):
+    """The network with the conv map decoder: the dense outputs, the map and
+    every gradient (dense layers and decoder levels) against the FP64
+    restatement with the same BF16 roundings, within 5e-3 of the largest
+    magnitude; at a small shape and at the surrogate's (128 x 128 map)."""
+    n_in, width, depth, n_out = 9, 128, 2, 16
+    net = S.MLP(n_in, width, depth, n_out, seed=13, map_side=side, map_ch=ch)
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-1, 1, (batch, n_in)).astype(np.float32)
+    t = rng.normal(0, 0.5, (batch, n_out + side * side)).astype(np.float32)
+    n_layers = net.layers()
+    assert n_layers == depth + 1 + 3
+    Ws, bs = net.weights()
+    bs = [rng.normal(0, 0.05, b.shape).astype(np.float32) for b in bs]
+    for l, b in enumerate(bs):
+        net.set(l, 1, b)
+    ref = MapNetRef(Ws, bs, n_out, side, ch[0], bf16=True)
+    y = net.predict(x)
+    yr = ref.forward(x.astype(np.float64))[-1]
+    assert _rel(y[:, :n_out], yr[:, :n_out]) <= 5e-3
+    assert _rel(y[:, n_out:], yr[:, n_out:]) <= 5e-3
+    loss, gW, gb = net.gradients(x, t)
+    lr, rW, rb = ref.loss_and_grads(x.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - lr) <= 1e-3 * lr
+    for l in range(n_layers):
+        assert _rel(gW[l], rW[l]) <= 5e-3, (l, _rel(gW[l], rW[l]))
+        assert _rel(gb[l], rb[l]) <= 5e-3, (l, _rel(gb[l], rb[l]))
     net.close()
 
 
@@ -80,3 +111,5 @@ def test_pipeline_small():
     assert r["accepted"] + r["fallback"] == 16
     assert np.isfinite(r["gauge_rel_err_all_mean"])
     assert r["surrogate_scenarios_per_s"] > r["one_at_a_time_scenarios_per_s"]
+    # the 128 x 128 inundation maps of the conv decoder are judged too
+    assert r["map"] == [128, 128] and np.isfinite(r["map_abs_err_mean_m"]) and 0.0 <= r["map_iou_mean"] <= 1.0
