@@ -12,8 +12,10 @@
 // pass reads (row-major for dH = dY W, transposed for dW = dY^T H).  Sizes are
 // small (a few hundred to a few thousand rows); one 64x64 tile per block of
 // four warps, K in steps of 32 through shared memory.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -131,6 +133,12 @@ __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* 
       }
 }
 
+}  // namespace cliffs_nn
+
+#include "umma.cuh"
+
+namespace cliffs_nn {
+
 // Rows idx[r] (or r) of a row-major FP32 matrix into BF16 rows of length ld
 // (columns past `cols` zero) and, when dst_t is set, the transpose [ld][ldt].
 __global__ void k_pack(int rows, int cols, const float* __restrict__ src, const int* __restrict__ idx, bf16* dst,
@@ -185,15 +193,6 @@ __global__ void k_grad_pack(int B, int N, float* dyf, const bf16* __restrict__ H
   const bf16 h = __float2bfloat16(v);
   dyb[(size_t)r * ldb + c] = h;
   if (c < N) dyt[(size_t)c * ldt + r] = h;
-}
-
-// db[n] = sum over rows of dY[:, n], in row order (deterministic).
-__global__ void k_colsum(int B, int N, const float* __restrict__ dy, float* db) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= N) return;
-  float s = 0.f;
-  for (int r = 0; r < B; ++r) s += dy[(size_t)r * N + c];
-  db[c] = s;
 }
 
 // Adam with decoupled weight decay wd on an FP32 [rows][cols] parameter; W
@@ -269,28 +268,28 @@ struct cliffs_mlp {
   int dc[4] = {0, 0, 0, 1};
   bf16* X[3] = {nullptr, nullptr, nullptr};  // decoder level inputs, NHWC
   float* map = nullptr;                      // [cap][side2]
-  bf16* col = nullptr;                       // im2col [P][kp] and its transpose
-  bf16* colt = nullptr;
+  bf16* col = nullptr;                       // im2col [P][kp]
   float* dzf = nullptr;  // a level's output gradient, FP32 [P][Cout]
   bf16* dzb = nullptr;   // ... in BF16 [P][pad16(Cout)]
-  bf16* dzt = nullptr;   // ... transposed [pad16(Cout)][P]
   float* dxf = nullptr;  // a level's input gradient (levels 1, 2)
-  float* wpart = nullptr;  // split-K partials of a weight gradient
-  float* cpart = nullptr;  // column-sum partials of a bias gradient
+  float* wpart = nullptr;  // partials of a weight gradient over chunks of pixels
+  float* cpart = nullptr;  // partials of a bias gradient over chunks of pixels
   float* part2 = nullptr;  // map loss partial sums
+  unsigned* err = nullptr;  // set by a tensor-core product whose wait ran out
+  bool tc_failed = false;   // a tensor-core product could not be launched
 };
 
 namespace {
 
 constexpr int kLossBlocks = 64;
+constexpr int kMapLossBlocks = 1024;  // the map loss: B x side^2 values
 
 void free_decoder(cliffs_mlp* m) {
-  void* p[] = {m->X[0], m->X[1], m->X[2], m->map, m->col, m->colt, m->dzf, m->dzb, m->dzt, m->dxf, m->wpart,
-               m->cpart, m->part2};
+  void* p[] = {m->X[0], m->X[1], m->X[2], m->map, m->col, m->dzf, m->dzb, m->dxf, m->wpart, m->cpart, m->part2};
   for (void* q : p)
     if (q) cudaFree(q);
   m->X[0] = m->X[1] = m->X[2] = nullptr;
-  m->col = m->colt = m->dzb = m->dzt = nullptr;
+  m->col = m->dzb = nullptr;
   m->map = m->dzf = m->dxf = m->wpart = m->cpart = m->part2 = nullptr;
 }
 
@@ -305,9 +304,10 @@ void free_all(cliffs_mlp* m) {
     if (p) cudaFree(p);
   for (bf16* p : m->Ht)
     if (p) cudaFree(p);
-  void* p[] = {m->out, m->dyf, m->dh, m->dyb, m->dyt, m->part, m->xs, m->ts, m->idx};
+  void* p[] = {m->out, m->dyf, m->dh, m->dyb, m->dyt, m->part, m->xs, m->ts, m->idx, m->err};
   for (void* q : p)
     if (q) cudaFree(q);
+  m->err = nullptr;
   m->H.clear();
   m->Ht.clear();
   m->out = m->dyf = m->dh = m->part = m->xs = m->ts = nullptr;
@@ -319,10 +319,11 @@ int max_n(const cliffs_mlp* m) { return std::max(m->d.width, m->n_total); }
 
 // Decoder level l (0..2): input side, input and output channels, im2col width.
 struct Level {
-  int S, cin, cout, K, kp;
+  int lvl, S, cin, cout, K, kp;
 };
 Level level(const cliffs_mlp* m, int l) {
   Level v;
+  v.lvl = l;
   v.S = m->s0 << l;
   v.cin = m->dc[l];
   v.cout = m->dc[l + 1];
@@ -330,12 +331,25 @@ Level level(const cliffs_mlp* m, int l) {
   v.kp = pad16(v.K);
   return v;
 }
-constexpr int kWSplits = 128;  // split-K blocks of a decoder weight gradient
-constexpr int kCSplits = 256;  // row chunks of a decoder bias gradient
+constexpr int kDwChunk = 512;  // least output pixels per partial of a decoder weight gradient
+
+// Output pixels per partial of a level's weight gradient (P pixels) (a multiple of
+// kStage; at most ~2048 partials), and the number of partials.
+int dw_chunk(long long P) {
+  const long long c = std::max<long long>(kDwChunk, ((P + 2047) / 2048 + kStage - 1) / kStage * kStage);
+  return (int)c;
+}
+int dw_blocks(long long P) { return (int)((P + dw_chunk(P) - 1) / dw_chunk(P)); }
+
+// The direct kernels' output-channel class: CO >= cout of 1, 8, 16, 32, 64.
+int co_class(int cout) { return cout <= 1 ? 1 : cout <= 8 ? 8 : cout <= 16 ? 16 : cout <= 32 ? 32 : 64; }
 
 // Activation buffers for batches up to cap.
 int ensure_cap(cliffs_mlp* m, int cap) {
   if (cap <= m->cap) return CLIFFS_OK;
+  // the decoder kernels index pixels and values in 32 bits: at most 64
+  // channels at a quarter of the map's cells, 16 values per map cell
+  if (m->d.map_side > 0 && (long long)cap * m->side2 * 16 >= (1ll << 31)) return CLIFFS_ERR_ARG;
   for (bf16* p : m->H)
     if (p) cudaFree(p);
   for (bf16* p : m->Ht)
@@ -356,29 +370,90 @@ int ensure_cap(cliffs_mlp* m, int cap) {
     return CLIFFS_ERR_NOMEM;
   if (m->d.map_side > 0) {
     free_decoder(m);
-    size_t col = 0, dz = 0, dzp = 0, dx = 0, wp = 0;
+    size_t col = 0, dz = 0, dzp = 0, dx = 0, wp = 0, bp = 0;
     for (int l = 0; l < 3; ++l) {
       const Level v = level(m, l);
       const size_t P = (size_t)cap * 4 * v.S * v.S;
-      col = std::max(col, P * v.kp);
+      if (v.cout >= 16) col = std::max(col, P * v.kp);  // im2col of the tensor-core levels
       dz = std::max(dz, P * v.cout);
-      dzp = std::max(dzp, P * pad16(v.cout));
+      dzp = std::max(dzp, P * v.cout);
       if (l > 0) dx = std::max(dx, (size_t)cap * v.S * v.S * v.cin);
-      wp = std::max(wp, (size_t)kWSplits * v.cout * v.kp);
+      wp = std::max(wp, (size_t)dw_blocks((long long)P) * v.cout * v.K);
+      bp = std::max(bp, (size_t)dw_blocks((long long)P) * v.cout);
       if (dalloc(&m->X[l], (size_t)cap * v.S * v.S * v.cin)) return CLIFFS_ERR_NOMEM;
     }
-    if (dalloc(&m->map, (size_t)cap * m->side2) || dalloc(&m->col, col) || dalloc(&m->colt, col) ||
-        dalloc(&m->dzf, std::max(dz, dx)) || dalloc(&m->dzb, dzp) || dalloc(&m->dzt, dzp) ||
-        dalloc(&m->dxf, std::max(dz, dx)) || dalloc(&m->wpart, wp) || dalloc(&m->cpart, (size_t)kCSplits * 64) ||
-        dalloc(&m->part2, kLossBlocks))
+    if (dalloc(&m->map, (size_t)cap * m->side2) || dalloc(&m->col, col) ||
+        dalloc(&m->dzf, std::max(dz, dx)) || dalloc(&m->dzb, dzp) ||
+        dalloc(&m->dxf, std::max(dz, dx)) || dalloc(&m->wpart, wp) || dalloc(&m->cpart, bp) ||
+        dalloc(&m->part2, kMapLossBlocks))
       return CLIFFS_ERR_NOMEM;
   }
   m->cap = cap;
   return CLIFFS_OK;
 }
 
+PFN_cuTensorMapEncodeTiled_v12000 g_encode_bf16 = nullptr;
+
+// A 2-D BF16 tensor map over rows x k (k contiguous, rows ld elements apart)
+// with a box of 64 x box_rows in the 128-byte swizzled layout; elements
+// outside read 0.
+bool bf16_map(CUtensorMap* map, const bf16* base, int rows, int k, int ld, int box_rows) {
+  if (!g_encode_bf16) {
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    g_encode_bf16 = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
+  cuuint32_t box[2] = {(cuuint32_t)umma::BK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  return g_encode_bf16(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16*>(base), dims, strides, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+bool gemm_tc_launch(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb,
+                    const Epi& e) {
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_tc_smem<BN>()) !=
+        cudaSuccess)
+      return false;
+    attr = true;
+  }
+  CUtensorMap ta, tb;
+  if (!bf16_map(&ta, A, M, K, lda, umma::BM) || !bf16_map(&tb, B, N, K, ldb, BN)) return false;
+  const dim3 grid((M + umma::BM - 1) / umma::BM, (N + BN - 1) / BN);
+  gemm_tc<BN><<<grid, umma::THREADS, gemm_tc_smem<BN>(), m->stream>>>(ta, tb, M, N, K, e, m->err);
+  ++m->launches;
+  return cudaGetLastError() == cudaSuccess;
+}
+
+// C = A B^T.  Unsplit products of at least 128 rows, 16 columns and a
+// reduction of 64 whose operands suit the tensor-memory path (16-byte aligned
+// rows, 128-byte aligned bases) run as gemm_tc, with the widest tile of 16,
+// 64 or 128 columns that N fills; the others run as gemm_tn: small batches,
+// the first layer (9 inputs), the decoder's narrow levels (8 and 1 output
+// channels) and its split-K weight gradients (a few output rows reduced over
+// millions of pixels).
 void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e,
           int splits = 1) {
+  // every tensor-map box lies within its operand's extent: M >= 128 rows,
+  // K >= 64, and a tile width of at most N (16, 64 or 128)
+  const bool tc_ok = splits == 1 && M >= umma::BM && N >= 16 && K >= umma::BK && lda % 8 == 0 && ldb % 8 == 0 &&
+                     ((uintptr_t)A % 128) == 0 && ((uintptr_t)B % 128) == 0;
+  if (tc_ok) {
+    const bool launched = N >= 128  ? gemm_tc_launch<128>(m, M, N, K, A, lda, B, ldb, e)
+                          : N >= 64 ? gemm_tc_launch<64>(m, M, N, K, A, lda, B, ldb, e)
+                                    : gemm_tc_launch<16>(m, M, N, K, A, lda, B, ldb, e);
+    if (!launched) m->tc_failed = true;  // reported by the call (CLIFFS_ERR_CUDA)
+    return;
+  }
   // split K: kc a multiple of BK, every split non-empty
   const int kc = splits > 1 ? ((K + splits - 1) / splits + BK - 1) / BK * BK : K;
   if (splits > 1) splits = (K + kc - 1) / kc;
@@ -390,6 +465,43 @@ void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16
 // Blocks of 256 threads covering n elements.
 inline unsigned blocks256(long long n) { return (unsigned)((n + 255) / 256); }
 
+// Shared memory above the default 48 KB for a kernel (once per kernel).
+template <typename Kernel>
+void smem_limit(Kernel* k, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <int CO>
+void dec_conv_launch(cliffs_mlp* m, int B, const Level& v, const Layer& y, bf16* out16, float* out32) {
+  const long long P = (long long)B * 4 * v.S * v.S;
+  const size_t sh = (size_t)9 * v.cin * CO * 4;
+  smem_limit(k_dec_conv<CO>, sh);
+  k_dec_conv<CO><<<blocks256(P), 256, sh, m->stream>>>(B, v.S, v.cin, v.cout, m->X[v.lvl], y.W, y.kp, y.b, out16,
+                                                       out32);
+}
+
+template <int CO>
+void dec_dw_launch(cliffs_mlp* m, int B, const Level& v) {
+  constexpr int G = dec_group<CO>();
+  const long long P = (long long)B * 4 * v.S * v.S;
+  const int KG = v.K / G, KGb = std::min(KG, 256), threads = KGb * std::max(1, 256 / KGb);
+  const size_t sh = dec_dw_smem<CO>(v.cin);
+  smem_limit(k_dec_dw<CO>, sh);
+  const dim3 grid(dw_blocks(P), (KG + KGb - 1) / KGb);
+  k_dec_dw<CO><<<grid, threads, sh, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, v.cout, m->X[v.lvl],
+                                                 dw_chunk(P), m->wpart, m->cpart);
+}
+
+template <int CO>
+void dec_dx_launch(cliffs_mlp* m, int B, const Level& v, const Layer& y, float* dx, int ld, int col0) {
+  constexpr int G = dec_group<CO>();
+  const long long n = (long long)B * v.S * v.S * (v.cin / G);
+  const size_t sh = (size_t)9 * v.cin * CO * 4;
+  smem_limit(k_dec_dx<CO>, sh);
+  k_dec_dx<CO><<<blocks256(n), 256, sh, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, v.cout, y.W, y.kp,
+                                                     m->X[v.lvl], dx, ld, col0);
+}
+
 // The map decoder's forward pass for rows [0, B): latent columns of out -> map.
 void decoder_forward(cliffs_mlp* m, int B) {
   k_dec_input<<<blocks256((long long)B * m->lat), 256, 0, m->stream>>>(B, m->lat, m->out, m->n_total, m->d.n_out,
@@ -398,18 +510,27 @@ void decoder_forward(cliffs_mlp* m, int B) {
   for (int l = 0; l < 3; ++l) {
     const Level v = level(m, l);
     const Layer& y = m->L[m->nd + l];
+    bf16* out16 = l < 2 ? m->X[l + 1] : nullptr;  // ReLU and BF16 NHWC, or the FP32 map
+    float* out32 = l < 2 ? nullptr : m->map;
+    if (v.cout < 16) {  // below the tensor cores' narrowest tile: direct
+      if (v.cout == 1)
+        dec_conv_launch<1>(m, B, v, y, out16, out32);
+      else
+        dec_conv_launch<8>(m, B, v, y, out16, out32);
+      ++m->launches;
+      continue;
+    }
     const int P = B * 4 * v.S * v.S;
-    k_im2col_up<<<blocks256((long long)P * v.kp), 256, 0, m->stream>>>(B, v.S, v.cin, m->X[l], v.kp, m->col,
-                                                                       nullptr, 0);
+    k_im2col_up<<<(P + 7) / 8, dim3(32, 8), 0, m->stream>>>(B, v.S, v.cin, m->X[l], v.kp, m->col);
     ++m->launches;
     Epi e{};
     e.bias = y.b;
     if (l < 2) {
       e.relu = 1;
-      e.b16 = m->X[l + 1];
+      e.b16 = out16;
       e.ldb = v.cout;
     } else {
-      e.f32 = m->map;
+      e.f32 = out32;
       e.ldf = 1;
     }
     gemm(m, P, v.cout, v.kp, m->col, v.kp, y.W, y.kp, e);
@@ -424,36 +545,33 @@ void decoder_backward(cliffs_mlp* m, int B) {
     const Level v = level(m, l);
     Layer& y = m->L[m->nd + l];
     const int P = B * 4 * v.S * v.S;
-    const int cp = pad16(v.cout);
-    // the output gradient in BF16, rows and transpose (ReLU masks applied by
+    // the output gradient in BF16 rows of cout values (ReLU masks applied by
     // the level above's input gradient)
-    k_pack_grad<<<blocks256((long long)P * cp), 256, 0, m->stream>>>(P, v.cout, cp, m->dzf, m->dzb, m->dzt);
-    // bias gradient: column sums in two stages
-    const int chunk = (P + kCSplits - 1) / kCSplits;
-    k_colsum_part<<<dim3((v.cout + 127) / 128, kCSplits), 128, 0, m->stream>>>(P, v.cout, chunk, m->dzf, m->cpart);
-    k_reduce_splits<<<(v.cout + 127) / 128, 128, 0, m->stream>>>(v.cout, kCSplits, m->cpart, y.gb);
-    // weight gradient dZ^T im2col, split over the pixels
-    k_im2col_up<<<blocks256((long long)P * v.kp), 256, 0, m->stream>>>(B, v.S, v.cin, m->X[l], v.kp, m->col,
-                                                                       m->colt, P);
-    Epi ew{};
-    ew.f32 = m->wpart;
-    ew.ldf = v.kp;
-    ew.zstride = (long long)v.cout * v.kp;
-    gemm(m, v.cout, v.kp, P, m->dzt, P, m->colt, P, ew, kWSplits);
-    const int kc = ((P + kWSplits - 1) / kWSplits + BK - 1) / BK * BK;
-    const int splits = (P + kc - 1) / kc;
-    k_reduce_wgrad<<<blocks256((long long)v.cout * v.K), 256, 0, m->stream>>>(v.cout, v.K, v.kp, splits, m->wpart,
-                                                                              y.gw);
+    k_to_bf16<<<blocks256((long long)P * v.cout), 256, 0, m->stream>>>(P * v.cout, m->dzf, m->dzb);
+    // weight and bias gradients: partial sums over chunks of pixels, then
+    // over the chunks in order
+    switch (co_class(v.cout)) {
+      case 1: dec_dw_launch<1>(m, B, v); break;
+      case 8: dec_dw_launch<8>(m, B, v); break;
+      case 16: dec_dw_launch<16>(m, B, v); break;
+      case 32: dec_dw_launch<32>(m, B, v); break;
+      default: dec_dw_launch<64>(m, B, v); break;
+    }
+    const int nb = dw_blocks(P);
+    k_reduce_wgrad<<<(v.cout * v.K + 31) / 32, 32 * kStrands, 0, m->stream>>>(v.cout, v.K, v.K, nb, m->wpart, y.gw);
+    k_reduce_wgrad<<<(v.cout + 31) / 32, 32 * kStrands, 0, m->stream>>>(1, v.cout, v.cout, nb, m->cpart, y.gb);
     // input gradient, masked by the level input's ReLU; level 0's goes to
     // the latent columns of the dense output gradient
-    const long long nin = (long long)B * v.S * v.S * v.cin;
-    if (l > 0)
-      k_dec_dx<<<blocks256(nin), 256, 0, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, cp, y.W, y.kp, m->X[l],
-                                                      m->dxf, v.S * v.S * v.cin, 0);
-    else
-      k_dec_dx<<<blocks256(nin), 256, 0, m->stream>>>(B, v.S, v.cin, v.cout, m->dzb, cp, y.W, y.kp, m->X[0],
-                                                      m->dyf, m->n_total, m->d.n_out);
-    m->launches += 6;
+    float* dx = l > 0 ? m->dxf : m->dyf;
+    const int ld = l > 0 ? v.S * v.S * v.cin : m->n_total, col0 = l > 0 ? 0 : m->d.n_out;
+    switch (co_class(v.cout)) {
+      case 1: dec_dx_launch<1>(m, B, v, y, dx, ld, col0); break;
+      case 8: dec_dx_launch<8>(m, B, v, y, dx, ld, col0); break;
+      case 16: dec_dx_launch<16>(m, B, v, y, dx, ld, col0); break;
+      case 32: dec_dx_launch<32>(m, B, v, y, dx, ld, col0); break;
+      default: dec_dx_launch<64>(m, B, v, y, dx, ld, col0); break;
+    }
+    m->launches += 5;
     if (l > 0) std::swap(m->dzf, m->dxf);  // the input gradient is the next level's output gradient
   }
 }
@@ -496,7 +614,7 @@ void backward(cliffs_mlp* m, int B, const float* t_dev, const int* idx) {
     // decoder's backward pass fills the latent columns of dY
     k_mse_block<<<kLossBlocks, 256, 0, m->stream>>>(B, no, m->out, m->n_total, 0, t_dev, m->n_y, 0, idx, m->dyf,
                                                     m->n_total, 0, 2.f / ((float)B * no), m->part);
-    k_mse_block<<<kLossBlocks, 256, 0, m->stream>>>(B, m->side2, m->map, m->side2, 0, t_dev, m->n_y, no, idx,
+    k_mse_block<<<kMapLossBlocks, 256, 0, m->stream>>>(B, m->side2, m->map, m->side2, 0, t_dev, m->n_y, no, idx,
                                                     m->dzf, m->side2, 0, 2.f / ((float)B * m->side2), m->part2);
     m->launches += 2;
     decoder_backward(m, B);
@@ -514,7 +632,7 @@ void backward(cliffs_mlp* m, int B, const float* t_dev, const int* idx) {
     const int ldH = l < nl - 1 ? m->L[l + 1].kp : 0;
     k_grad_pack<<<dim3((Np + 127) / 128, B), 128, 0, m->stream>>>(B, N, m->dyf, Hmask, ldH, m->dyb, Np, m->dyt,
                                                                   m->cap);
-    k_colsum<<<(N + 127) / 128, 128, 0, m->stream>>>(B, N, m->dyf, y.gb);
+    k_reduce_wgrad<<<(N + 31) / 32, 32 * kStrands, 0, m->stream>>>(1, N, N, B, m->dyf, y.gb);  // column sums
     m->launches += 2;
     // dW = dY^T H_l: (N x B) (B x cols), reduction over the batch
     Epi ew{};
@@ -583,10 +701,31 @@ int stage_data(cliffs_mlp* m, int n, const float* x, const float* t) {
   return CLIFFS_OK;
 }
 
+// The products' status since the last call: CLIFFS_ERR_TIMEOUT when a
+// tensor-core product's wait ran out (cleared), CLIFFS_ERR_CUDA when one could
+// not be launched; synchronises.
+int products_status(cliffs_mlp* m) {
+  unsigned e = 0;
+  if (cudaMemcpyAsync(&e, m->err, sizeof(e), cudaMemcpyDeviceToHost, m->stream) != cudaSuccess ||
+      cudaStreamSynchronize(m->stream) != cudaSuccess)
+    return CLIFFS_ERR_CUDA;
+  if (e) {
+    cudaMemsetAsync(m->err, 0, sizeof(unsigned), m->stream);
+    return CLIFFS_ERR_TIMEOUT;
+  }
+  if (m->tc_failed) {
+    m->tc_failed = false;
+    return CLIFFS_ERR_CUDA;
+  }
+  return CLIFFS_OK;
+}
+
 float loss_of(cliffs_mlp* m, int B) {
-  float part[kLossBlocks], part2[kLossBlocks];
+  float part[kLossBlocks];
+  std::vector<float> part2(kMapLossBlocks);
   cudaMemcpyAsync(part, m->part, sizeof(part), cudaMemcpyDeviceToHost, m->stream);
-  if (m->d.map_side > 0) cudaMemcpyAsync(part2, m->part2, sizeof(part2), cudaMemcpyDeviceToHost, m->stream);
+  if (m->d.map_side > 0)
+    cudaMemcpyAsync(part2.data(), m->part2, part2.size() * sizeof(float), cudaMemcpyDeviceToHost, m->stream);
   cudaStreamSynchronize(m->stream);
   double s = 0, s2 = 0;
   for (float p : part) s += p;
@@ -628,6 +767,7 @@ int cliffs_mlp_create(const cliffs_mlp_desc* d, cliffs_mlp** out) {
     return r;
   };
   if (cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
+  if (dalloc(&m->err, 1)) return fail(CLIFFS_ERR_NOMEM);
   std::mt19937_64 rng(d->seed);
   const int nlayers = m->nd + (d->map_side > 0 ? 3 : 0);
   for (int l = 0; l < nlayers; ++l) {
@@ -742,6 +882,7 @@ int cliffs_mlp_predict(cliffs_mlp* m, int32_t batch, const float* x, float* y) {
   }
   if (cudaStreamSynchronize(m->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   if (!r && cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  if (!r) r = products_status(m);
   return r;
 }
 
@@ -755,7 +896,8 @@ int cliffs_mlp_gradients(cliffs_mlp* m, int32_t batch, const float* x, const flo
   backward(m, batch, m->ts, nullptr);
   const float l = loss_of(m, batch);
   if (loss) *loss = l;
-  return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return CLIFFS_ERR_CUDA;
+  return products_status(m);
 }
 
 int cliffs_mlp_train(cliffs_mlp* m, int32_t n, const float* x, const float* t, int32_t epochs, int32_t batch,
@@ -793,6 +935,7 @@ int cliffs_mlp_train(cliffs_mlp* m, int32_t n, const float* x, const float* t, i
     if (cudaStreamSynchronize(m->stream) != cudaSuccess) r = CLIFFS_ERR_CUDA;
   }
   if (!r && cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
+  if (!r) r = products_status(m);
   return r;
 }
 

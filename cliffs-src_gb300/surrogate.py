@@ -3,27 +3,39 @@
 The surrogate maps eight source parameters to the quantities a hazard study
 reads from a run: the maximum elevation at 64 gauges and the maximum
 inundation depth (the largest flow depth over ground, MaxE + dep on land,
-0 where the sea never reached) over a 128 x 128 window of the coast.  A
-4-layer MLP (width 512) gives the gauge maxima and a latent 16 x 16 x 32 grid,
-which a conv decoder (three 2x upsampling + 3x3 convolution levels) turns
-into the 128 x 128 map.  Its training data are runs of the batched
-solver (cliffs_batch_*) on one 512 x 512 shelf/slope grid at 100 m, every
-source applied on the device (cliffs_gpu_add_source, rising over its rise
-time); the network is trained on the GPU by the library's own kernels (BF16
-tensor-core products, FP32 accumulation, Adam).  An ensemble of members
-trained from different seeds answers together; where their gauge predictions
-disagree by more than a relative spread, the scenario goes back to the
-solver.  The spread threshold is calibrated on a validation split of the
-training runs as the largest that keeps the accepted scenarios' mean gauge
-error within the target; the solver then judges the surrogate's error on
-held-out scenarios.
+0 where the sea never reached) over a 128 x 128 window of the coast.
+
+- Gauges: an ensemble of 4-layer MLPs (9 features -> 3 x 512 ReLU -> 64),
+  trained from different seeds.  Their mean is the prediction, their
+  disagreement the gate.
+- Map: an MLP of the same shape whose last layer also emits a latent
+  16 x 16 x 32 grid, which a conv decoder (three 2x upsampling + 3x3
+  convolution levels) turns into the 128 x 128 map; the mean of the map
+  members is the prediction.
+
+The training data are runs of the batched solver (cliffs_batch_*) on one
+512 x 512 shelf/slope grid at 100 m, every source applied on the device
+(cliffs_gpu_add_source, rising over its rise time); the networks are
+trained on the GPU by the library's own kernels (BF16 tensor-core products
+on tcgen05 with FP32 accumulation in tensor memory, direct convolutions for
+the decoder's narrow levels, Adam).  Where the gauge members disagree by
+more than a relative spread, the scenario goes back to the solver.  The
+spread threshold is calibrated on a validation split of the training runs
+as the largest that keeps the accepted scenarios' mean gauge error within
+the target; the solver then judges the surrogate's error on held-out
+scenarios.
 
     python cliffs-src_gb300/surrogate.py [--train 4096] [--test 256] [--steps 2000]
-                                         [--epochs 1500] [--target 0.045]
+                                         [--epochs 1500] [--map-epochs 600] [--target 0.045]
 
 prints one JSON line: data generation time, training losses, accuracy of the
 gated ensemble against the solver, and scenarios per second of the surrogate
 path against one-at-a-time solves.
+
+    python cliffs-src_gb300/surrogate.py --infer 4096
+
+times the networks' inference alone (untrained weights, no data): the
+4 gauge networks and the map network on 4096 fresh parameter sets, twice.
 """
 import argparse
 import ctypes
@@ -225,7 +237,8 @@ class Norm:
         self.gm, self.gs = lg.mean(0), lg.std(0) + 1e-6
         self.ms = float(np.sqrt(np.mean(np.square(M)))) + 1e-6
 
-    def x(self, params):
+    @staticmethod
+    def x(params):
         """Features: the parameters scaled to [-1, 1], with the amplitude as its
         logarithm and the angle as its cosine and sine (rotations wrap)."""
         z = 2.0 * (params - LO) / (HI - LO) - 1.0
@@ -239,50 +252,72 @@ class Norm:
             G, M = G / a, M / a[:, :, None]
         return np.hstack([self.GW * (np.log(G + 0.01) - self.gm) / self.gs, M.reshape(len(M), -1) / self.ms])
 
-    def back(self, Y, params=None):
+    def back_gauges(self, Y, params=None):
+        """Gauge maxima (m) from network outputs (the first NGAUGES columns)."""
         g = np.exp(Y[:, :NGAUGES] / self.GW * self.gs + self.gm) - 0.01
+        if self.per_amp:
+            g = g * params[:, 2:3]
+        return np.maximum(g, 0.0)
+
+    def back_maps(self, Y, params=None):
+        """Inundation maps (m) from a map network's outputs."""
         m = Y[:, NGAUGES:].reshape(len(Y), MAP, MAP) * self.ms
         if self.per_amp:
-            a = params[:, 2:3]
-            g, m = g * a, m * a[:, :, None]
-        return np.maximum(g, 0.0), np.maximum(m, 0.0)
+            m = m * params[:, 2:3, None]
+        return np.maximum(m, 0.0)
 
 
 N_FEATURES = 9  # Norm.x
 
 
 class Ensemble:
-    def __init__(self, members=4, width=512, depth=3, seed=0):
-        self.nets = [MLP(N_FEATURES, width, depth, NGAUGES, seed=seed + 101 * k, map_side=MAP, map_ch=MAP_CH)
-                     for k in range(members)]
+    """`members` gauge networks (MLP 9 -> width x depth -> 64) and
+    `map_members` map networks (the same MLP emitting the gauges and the
+    decoder's latent grid, then the 128 x 128 map)."""
 
-    def train(self, X, T, epochs, batch=512, lr=1e-3, seed=0, weight_decay=0.0):
+    def __init__(self, members=4, width=512, depth=3, seed=0, map_members=1):
+        self.nets = [MLP(N_FEATURES, width, depth, NGAUGES, seed=seed + 101 * k) for k in range(members)]
+        self.maps = [MLP(N_FEATURES, width, depth, NGAUGES, seed=seed + 211 + 101 * k, map_side=MAP, map_ch=MAP_CH)
+                     for k in range(map_members)]
+
+    def train(self, X, T, epochs, map_epochs, batch=512, lr=1e-3, seed=0, weight_decay=0.0):
+        """T: normalised gauge columns, then the map; returns the loss
+        curves of the gauge and of the map members."""
         batch = max(16, min(batch, len(X) // 16 * 16))
-        return [net.train(X, T, epochs, batch, lr, seed + 7 * k, weight_decay) for k, net in enumerate(self.nets)]
+        Tg = np.ascontiguousarray(T[:, :NGAUGES])
+        lg = [net.train(X, Tg, epochs, batch, lr, seed + 7 * k, weight_decay) for k, net in enumerate(self.nets)]
+        lm = [net.train(X, T, map_epochs, batch, lr, seed + 13 + 7 * k, weight_decay)
+              for k, net in enumerate(self.maps)] if map_epochs > 0 else []
+        return lg, lm
 
-    def predict(self, X, norm, params=None):
-        outs = [norm.back(net.predict(X), params) for net in self.nets]
-        G = np.stack([o[0] for o in outs])  # (members, n, 64)
-        M = np.stack([o[1] for o in outs])  # (members, n, 128, 128)
-        return G.mean(0), M.mean(0), G
+    def predict(self, X, norm, params=None, maps=True):
+        """Mean gauge maxima, mean map (None without maps) and the members'
+        gauge maxima (members, n, 64)."""
+        G = np.stack([norm.back_gauges(net.predict(X), params) for net in self.nets])
+        M = None
+        if maps and self.maps:
+            M = np.mean([norm.back_maps(net.predict(X), params) for net in self.maps], axis=0)
+        return G.mean(0), M, G
 
     def close(self):
-        for n in self.nets:
+        for n in self.nets + self.maps:
             n.close()
 
 
-def forward_flop(width=512, depth=3):
+def forward_flop(width=512, depth=3, with_map=False):
     """Multiply-add FLOPs of one network's forward pass for one sample: the
-    dense layers (the last emits the gauges and the latent grid) and the
-    decoder's three convolutions (3x3 taps on the upsampled grids)."""
+    dense layers and, for a map network (whose last layer also emits the
+    latent grid), the decoder's three convolutions (3x3 taps on the
+    upsampled grids)."""
     s0 = MAP // 8
-    lat = s0 * s0 * MAP_CH[0]
+    lat = s0 * s0 * MAP_CH[0] if with_map else 0
     dims = [N_FEATURES] + [width] * depth + [NGAUGES + lat]
     fl = sum(2 * a * b for a, b in zip(dims[:-1], dims[1:]))
-    ch = list(MAP_CH) + [1]
-    for l in range(3):
-        side = 2 * s0 << l
-        fl += 2 * side * side * ch[l + 1] * 9 * ch[l]
+    if with_map:
+        ch = list(MAP_CH) + [1]
+        for l in range(3):
+            side = 2 * s0 << l
+            fl += 2 * side * side * ch[l + 1] * 9 * ch[l]
     return fl
 
 
@@ -351,34 +386,59 @@ def map_errors(Mp, M, floor=0.05):
                 map_iou_mean=float(iou.mean()), map_scenarios_inundated=int(has.sum()))
 
 
-def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True, width=512, depth=3,
-                  members=4, single=None, batch=512, lr=1e-3):
+def fit_and_judge(D, epochs=1500, map_epochs=600, target=0.045, seed=0, n_val=256, per_amp=True, width=512,
+                  depth=3, members=4, map_members=1, single=None, batch=512, lr=1e-3, repeats=1, infer_batch=4096):
     """Train the ensemble on the training runs, calibrate its gate on the
     validation split, judge it on the held-out runs against the solver.
-    single: seconds of one one-at-a-time solve (measured here when None)."""
+
+    The gated path (gauge and map predictions of the held-out scenarios, the
+    gate, one batched solve of the rejected ones) is timed `repeats` times
+    (medians reported); the surrogate alone is also timed at an inference
+    batch of `infer_batch` fresh scenarios.  single: seconds of one
+    one-at-a-time solve (measured here when None)."""
     base, steps = D["base"], D["steps"]
     Xall, Gall, Mall, Xte, Gte, Mte = D["Xall"], D["Gall"], D["Mall"], D["Xte"], D["Gte"], D["Mte"]
     n_test = len(Xte)
     Xtr, Gtr, Mtr = Xall[n_val:], Gall[n_val:], Mall[n_val:]
     Xva, Gva = Xall[:n_val], Gall[:n_val]
     norm = Norm(Gtr, Mtr, Xtr, per_amp=per_amp)
-    ens = Ensemble(members=members, width=width, depth=depth, seed=seed)
+    ens = Ensemble(members=members, width=width, depth=depth, seed=seed, map_members=map_members)
     t0 = time.perf_counter()
-    losses = ens.train(norm.x(Xtr), norm.t(Gtr, Mtr, Xtr), epochs, batch=batch, lr=lr)
+    lg, lm = ens.train(norm.x(Xtr), norm.t(Gtr, Mtr, Xtr), epochs, map_epochs, batch=batch, lr=lr)
     t_train = time.perf_counter() - t0
-    # the gate, from the validation split
-    Gv, _, Gvm = ens.predict(norm.x(Xva), norm, Xva)
+    # the gate, from the validation split (gauge members)
+    Gv, _, Gvm = ens.predict(norm.x(Xva), norm, Xva, maps=False)
     rel_v, mask_v, _ = gauge_errors(Gv, Gva)
     thr = calibrate_gate(spread(Gvm), rel_v, mask_v, target)
-    # the surrogate path on the test split: ensemble prediction, then the gate
-    t0 = time.perf_counter()
-    Gp, Mp, Gm = ens.predict(norm.x(Xte), norm, Xte)
-    sp = spread(Gm)
-    accept = sp <= thr
-    t_pred = time.perf_counter() - t0
+    # the gated path on the test split: predictions, the gate, the solver for
+    # the rejected scenarios as one batch, timed whole (grid set-up, sources,
+    # steps, max-wave download)
+    t_preds, t_fbs = [], []
+    for _ in range(max(1, repeats)):
+        t0 = time.perf_counter()
+        Gp, Mp, Gm = ens.predict(norm.x(Xte), norm, Xte)
+        sp = spread(Gm)
+        accept = sp <= thr
+        t_preds.append(time.perf_counter() - t0)
+        rej = np.flatnonzero(~accept)
+        t_fb = 0.0
+        if rej.size:
+            t0 = time.perf_counter()
+            Gfb, _, _, _ = solve(Xte[rej], base, steps)
+            t_fb = time.perf_counter() - t0
+            assert np.array_equal(Gfb, Gte[rej])  # batching does not change a run
+        t_fbs.append(t_fb)
+    t_pred, t_fb = float(np.median(t_preds)), float(np.median(t_fbs))
+    n_fallback = int((~accept).sum())
     rel, mask, _ = gauge_errors(Gp, Gte)
     rel_acc = rel[accept[:, None] & mask]
-    merr = map_errors(Mp, Mte)
+    merr = map_errors(Mp, Mte) if Mp is not None else {}
+    # the surrogate alone at the inference batch: fresh scenarios, gauges and maps
+    Xinf = sample_params(infer_batch, seed + 99)
+    ens.predict(norm.x(Xinf), norm, Xinf)  # buffers at this batch
+    t0 = time.perf_counter()
+    ens.predict(norm.x(Xinf), norm, Xinf)
+    t_inf = time.perf_counter() - t0
     # one-at-a-time solves of a few test scenarios: the method without the surrogate
     if single is None:
         n_single = min(16, n_test)
@@ -396,24 +456,15 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
         single = t_single / n_single
     per_single = single
     per_batch = D["t_test_solve"] / n_test
-    # the rejected scenarios go to the batched solver, as one batch, timed
-    # whole (grid set-up, sources, steps, max-wave download)
-    rej = np.flatnonzero(~accept)
-    n_fallback = int(rej.size)
-    t_fb = 0.0
-    if n_fallback:
-        t0 = time.perf_counter()
-        Gfb, _, _, _ = solve(Xte[rej], base, steps)
-        t_fb = time.perf_counter() - t0
-        assert np.array_equal(Gfb, Gte[rej])  # batching does not change a run
     t_gated = t_pred + t_fb
-    res = dict(train=len(Xtr), validation=n_val, test=n_test, steps=steps, epochs=epochs, target=target,
-               per_amp=per_amp, width=width, depth=depth, members=members, map=[MAP, MAP], map_channels=MAP_CH,
-               nonfinite_runs=D["bad"],
+    flop = members * forward_flop(width, depth) + map_members * forward_flop(width, depth, with_map=True)
+    res = dict(train=len(Xtr), validation=n_val, test=n_test, steps=steps, epochs=epochs, map_epochs=map_epochs,
+               target=target, per_amp=per_amp, width=width, depth=depth, members=members, map_members=map_members,
+               map=[MAP, MAP], map_channels=MAP_CH, nonfinite_runs=D["bad"],
                data_seconds=round(D["t_gen"], 2), solver_seconds_train=round(D["t_data"], 2),
                train_seconds=round(t_train, 2),
-               final_loss=[round(float(l[-1]), 5) for l in losses],
-               first_loss=[round(float(l[0]), 5) for l in losses],
+               final_loss=[round(float(l[-1]), 5) for l in lg], first_loss=[round(float(l[0]), 5) for l in lg],
+               map_final_loss=[round(float(l[-1]), 5) for l in lm],
                gate_threshold=round(thr, 4), accepted=int(accept.sum()), fallback=n_fallback,
                gauge_rel_err_all_mean=round(float(rel[mask].mean()), 4),
                gauge_rel_err_all_p90=round(float(np.quantile(rel[mask], 0.9)), 4),
@@ -421,10 +472,12 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
                gauge_rel_err_accepted_median=round(float(np.median(rel_acc)), 4) if rel_acc.size else None,
                gated_rel_err_mean=round(float(np.where(accept[:, None], rel, 0.0)[mask].mean()), 4),
                **{k: round(v, 4) if isinstance(v, float) else v for k, v in merr.items()},
-               predict_ms=round(1e3 * t_pred, 3), fallback_solve_ms=round(1e3 * t_fb, 2),
-               predict_flop=int(forward_flop(width, depth) * members * n_test),
+               repeats=len(t_preds), predict_ms=round(1e3 * t_pred, 3), fallback_solve_ms=round(1e3 * t_fb, 2),
+               predict_flop=int(flop * n_test),
                single_solve_s=round(per_single, 4), batched_solve_s_per_scenario=round(per_batch, 5),
                surrogate_scenarios_per_s=round(n_test / t_pred, 1),
+               infer_batch=infer_batch, infer_ms=round(1e3 * t_inf, 2),
+               infer_scenarios_per_s=round(infer_batch / t_inf, 1),
                gated_scenarios_per_s=round(n_test / t_gated, 1),
                one_at_a_time_scenarios_per_s=round(1.0 / per_single, 2),
                gated_speedup_vs_one_at_a_time=round(per_single * n_test / t_gated, 1),
@@ -433,12 +486,14 @@ def fit_and_judge(D, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
     return res
 
 
-def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True):
+def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
+        map_epochs=600, infer_batch=4096):
     """Data from the batched solver, the ensemble trained on n_train - n_val
     runs, its gate calibrated on the n_val others, judged on n_test held-out
     runs against the solver."""
     D = make_data(n_train, n_test, steps, seed)
-    return fit_and_judge(D, epochs=epochs, target=target, seed=seed, n_val=n_val, per_amp=per_amp)
+    return fit_and_judge(D, epochs=epochs, map_epochs=map_epochs, target=target, seed=seed, n_val=n_val,
+                         per_amp=per_amp, infer_batch=infer_batch)
 
 
 def main():
@@ -447,13 +502,28 @@ def main():
     ap.add_argument("--test", type=int, default=256)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--map-epochs", type=int, default=600)
     ap.add_argument("--target", type=float, default=0.045)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-per-amp", action="store_true", help="targets in metres, not per metre of amplitude")
+    ap.add_argument("--infer", type=int, default=0, help="time inference of N scenarios alone (untrained)")
     a = ap.parse_args()
     pkg.build.build()
-    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=not a.no_per_amp)),
-          flush=True)
+    if a.infer:
+        ens = Ensemble(members=4, map_members=1, seed=a.seed)
+        X = Norm.x(sample_params(a.infer, a.seed))
+        out = {}
+        for k in range(2):
+            t0 = time.perf_counter()
+            G = [net.predict(X) for net in ens.nets]
+            M = [net.predict(X) for net in ens.maps]
+            out[f"pass{k}_ms"] = round(1e3 * (time.perf_counter() - t0), 2)
+        out.update(scenarios=a.infer, finite=bool(np.isfinite(G[0]).all() and np.isfinite(M[0]).all()))
+        ens.close()
+        print(json.dumps(out), flush=True)
+        return
+    print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=not a.no_per_amp,
+                         map_epochs=a.map_epochs)), flush=True)
 
 
 if __name__ == "__main__":

@@ -106,7 +106,7 @@ def test_parameters_round_trip():
 
 
 def test_pipeline_small():
-    r = S.run(n_train=96, n_test=16, steps=150, epochs=10, target=0.5, seed=1, n_val=32)
+    r = S.run(n_train=96, n_test=16, steps=150, epochs=10, target=0.5, seed=1, n_val=32, map_epochs=5, infer_batch=64)
     assert r["nonfinite_runs"] == 0
     assert r["accepted"] + r["fallback"] == 16
     assert np.isfinite(r["gauge_rel_err_all_mean"])
