@@ -38,9 +38,8 @@ inline int pad16(int n) { return (n + 15) & ~15; }
 struct Epi {
   const float* bias;  // [N] or null
   int relu;
-  float* f32;         // [M][ldf] or null; split z of a split-K product at f32 + z * zstride
+  float* f32;         // [M][ldf] or null
   int ldf;
-  long long zstride;
   bf16* b16;          // [M][ldb] or null
   int ldb;
   bf16* b16t;         // [N][ldt] (transposed) or null
@@ -59,11 +58,11 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 // dimensions lda, ldb, multiples of 8, 16-byte aligned rows); K is a multiple
 // of 16 and both operands hold zeros in [K, round_up(K, 32)) or that range is
 // past the end of the tile load (guarded).  M and N are arbitrary; M tiles
-// run along grid x.  Split K (gridDim.z > 1): block z reduces K range
-// [z kc, (z+1) kc) (kc a multiple of BK) and writes its partial product to
-// e.f32 + z * e.zstride.
+// run along grid x.  The products too small for gemm_tc (the first layer's
+// 9 inputs, its weight gradient's 9 columns, batches under 128 rows) run
+// here on mma.sync.
 __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* __restrict__ A, int lda,
-                                               const bf16* __restrict__ B, int ldb, Epi e, int kc) {
+                                               const bf16* __restrict__ B, int ldb, Epi e) {
   __shared__ __align__(16) bf16 sA[BM][BK + PAD];
   __shared__ __align__(16) bf16 sB[BN][BK + PAD];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -77,8 +76,8 @@ __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* 
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
-  for (int k0 = kb; k0 < ke; k0 += BK) {
+  const int ke = K;
+  for (int k0 = 0; k0 < ke; k0 += BK) {
     // 64 rows x 32 columns per operand: 256 chunks of 8 elements (16 B)
     for (int c = tid; c < 256; c += 128) {
       const int r = c >> 2, col = (c & 3) * 8;
@@ -126,7 +125,7 @@ __global__ void __launch_bounds__(128) gemm_tn(int M, int N, int K, const bf16* 
         float v = acc[i][j][q];
         if (e.bias) v += e.bias[col];
         if (e.relu) v = fmaxf(v, 0.f);
-        if (e.f32) e.f32[(size_t)blockIdx.z * e.zstride + (size_t)row * e.ldf + col] = v;
+        if (e.f32) e.f32[(size_t)row * e.ldf + col] = v;
         const bf16 h = __float2bfloat16(v);
         if (e.b16) e.b16[(size_t)row * e.ldb + col] = h;
         if (e.b16t) e.b16t[(size_t)col * e.ldt + row] = h;
@@ -434,18 +433,15 @@ bool gemm_tc_launch(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, 
   return cudaGetLastError() == cudaSuccess;
 }
 
-// C = A B^T.  Unsplit products of at least 128 rows, 16 columns and a
-// reduction of 64 whose operands suit the tensor-memory path (16-byte aligned
-// rows, 128-byte aligned bases) run as gemm_tc, with the widest tile of 16,
-// 64 or 128 columns that N fills; the others run as gemm_tn: small batches,
-// the first layer (9 inputs), the decoder's narrow levels (8 and 1 output
-// channels) and its split-K weight gradients (a few output rows reduced over
-// millions of pixels).
-void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e,
-          int splits = 1) {
+// C = A B^T.  Products of at least 128 rows, 16 columns and a reduction of
+// 64 whose operands suit the tensor-memory path (16-byte aligned rows,
+// 128-byte aligned bases) run as gemm_tc, with the widest tile of 16, 64 or
+// 128 columns that N fills; the others (small batches, the first layer's 9
+// inputs) run as gemm_tn.
+void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, const Epi& e) {
   // every tensor-map box lies within its operand's extent: M >= 128 rows,
   // K >= 64, and a tile width of at most N (16, 64 or 128)
-  const bool tc_ok = splits == 1 && M >= umma::BM && N >= 16 && K >= umma::BK && lda % 8 == 0 && ldb % 8 == 0 &&
+  const bool tc_ok = M >= umma::BM && N >= 16 && K >= umma::BK && lda % 8 == 0 && ldb % 8 == 0 &&
                      ((uintptr_t)A % 128) == 0 && ((uintptr_t)B % 128) == 0;
   if (tc_ok) {
     const bool launched = N >= 128  ? gemm_tc_launch<128>(m, M, N, K, A, lda, B, ldb, e)
@@ -454,11 +450,8 @@ void gemm(cliffs_mlp* m, int M, int N, int K, const bf16* A, int lda, const bf16
     if (!launched) m->tc_failed = true;  // reported by the call (CLIFFS_ERR_CUDA)
     return;
   }
-  // split K: kc a multiple of BK, every split non-empty
-  const int kc = splits > 1 ? ((K + splits - 1) / splits + BK - 1) / BK * BK : K;
-  if (splits > 1) splits = (K + kc - 1) / kc;
-  const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, splits);
-  gemm_tn<<<grid, 128, 0, m->stream>>>(M, N, K, A, lda, B, ldb, e, splits > 1 ? kc : K);
+  const dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  gemm_tn<<<grid, 128, 0, m->stream>>>(M, N, K, A, lda, B, ldb, e);
   ++m->launches;
 }
 

@@ -224,22 +224,69 @@ __global__ void __launch_bounds__(umma::THREADS, 1)
   if (!fin && threadIdx.x == 0) atomicOr(err, 1u);
   if (s_ok && fin) {
     const int row = m0 + 32 * warp + lane;
+    // a thread's 16 consecutive columns go out as 16-byte stores where the
+    // rows allow it (the transposed copy is coalesced across the warp as is)
+    const bool vf = e.f32 && e.ldf % 4 == 0 && ((uintptr_t)e.f32 & 15) == 0;
+    const bool vb = e.b16 && e.ldb % 8 == 0 && ((uintptr_t)e.b16 & 15) == 0;
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
       float v[16];
       umma::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-      if (row < M) {
+      const int cb = n0 + c0;
+      if (row < M && cb + 16 <= N) {
+        if (e.bias) {
+          const float4* b4 = reinterpret_cast<const float4*>(e.bias + cb);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const float4 b = __ldg(b4 + q);
+            v[4 * q] += b.x;
+            v[4 * q + 1] += b.y;
+            v[4 * q + 2] += b.z;
+            v[4 * q + 3] += b.w;
+          }
+        }
+        if (e.relu)
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j], 0.f);
+        if (vf) {
+          float4* o = reinterpret_cast<float4*>(e.f32 + (size_t)row * e.ldf + cb);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else if (e.f32) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) e.f32[(size_t)row * e.ldf + cb + j] = v[j];
+        }
+        if (e.b16 || e.b16t) {
+          uint32_t h[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const __nv_bfloat162 t = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);  // .x = low half
+            h[q] = *reinterpret_cast<const uint32_t*>(&t);
+          }
+          if (vb) {
+            uint4* o = reinterpret_cast<uint4*>(e.b16 + (size_t)row * e.ldb + cb);
+            o[0] = make_uint4(h[0], h[1], h[2], h[3]);
+            o[1] = make_uint4(h[4], h[5], h[6], h[7]);
+          } else if (e.b16) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) e.b16[(size_t)row * e.ldb + cb + j] = __float2bfloat16(v[j]);
+          }
+          if (e.b16t)
+#pragma unroll
+            for (int j = 0; j < 16; ++j) e.b16t[(size_t)(cb + j) * e.ldt + row] = __float2bfloat16(v[j]);
+        }
+      } else if (row < M) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int col = n0 + c0 + j;
+          const int col = cb + j;
           if (col >= N) break;
           float x = v[j];
           if (e.bias) x += e.bias[col];
           if (e.relu) x = fmaxf(x, 0.f);
           if (e.f32) e.f32[(size_t)row * e.ldf + col] = x;
-          const __nv_bfloat16 h = __float2bfloat16(x);
-          if (e.b16) e.b16[(size_t)row * e.ldb + col] = h;
-          if (e.b16t) e.b16t[(size_t)col * e.ldt + row] = h;
+          const __nv_bfloat16 hb = __float2bfloat16(x);
+          if (e.b16) e.b16[(size_t)row * e.ldb + col] = hb;
+          if (e.b16t) e.b16t[(size_t)col * e.ldt + row] = hb;
         }
       }
     }

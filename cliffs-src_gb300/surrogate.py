@@ -26,7 +26,8 @@ the target; the solver then judges the surrogate's error on held-out
 scenarios.
 
     python cliffs-src_gb300/surrogate.py [--train 4096] [--test 256] [--steps 2000]
-                                         [--epochs 1500] [--map-epochs 600] [--target 0.045]
+                                         [--epochs 1500] [--map-epochs 600] [--map-members 1]
+                                         [--target 0.045]
 
 prints one JSON line: data generation time, training losses, accuracy of the
 gated ensemble against the solver, and scenarios per second of the surrogate
@@ -487,13 +488,13 @@ def fit_and_judge(D, epochs=1500, map_epochs=600, target=0.045, seed=0, n_val=25
 
 
 def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
-        map_epochs=600, infer_batch=4096):
+        map_epochs=600, infer_batch=4096, map_members=1):
     """Data from the batched solver, the ensemble trained on n_train - n_val
     runs, its gate calibrated on the n_val others, judged on n_test held-out
     runs against the solver."""
     D = make_data(n_train, n_test, steps, seed)
     return fit_and_judge(D, epochs=epochs, map_epochs=map_epochs, target=target, seed=seed, n_val=n_val,
-                         per_amp=per_amp, infer_batch=infer_batch)
+                         per_amp=per_amp, infer_batch=infer_batch, map_members=map_members)
 
 
 def main():
@@ -503,6 +504,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=1500)
     ap.add_argument("--map-epochs", type=int, default=600)
+    ap.add_argument("--map-members", type=int, default=1)
     ap.add_argument("--target", type=float, default=0.045)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-per-amp", action="store_true", help="targets in metres, not per metre of amplitude")
@@ -523,7 +525,7 @@ def main():
         print(json.dumps(out), flush=True)
         return
     print(json.dumps(run(a.train, a.test, a.steps, a.epochs, a.target, a.seed, per_amp=not a.no_per_amp,
-                         map_epochs=a.map_epochs)), flush=True)
+                         map_epochs=a.map_epochs, map_members=a.map_members)), flush=True)
 
 
 if __name__ == "__main__":

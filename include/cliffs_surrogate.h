@@ -3,15 +3,17 @@
  * No reference counterpart: the reference is the solver only.  The surrogate
  * is a multilayer perceptron, with an optional conv decoder for a map,
  * mapping a source's parameters to quantities of
- * interest of the run (gauge maxima, a coarse max-inundation map), trained on
+ * interest of the run (gauge maxima, a max-inundation map), trained on
  * runs of the batched solver (cliffs_batch_*) and used with an ensemble of
  * independently initialised members whose disagreement sends a scenario back
  * to the solver.  Training and inference run on the GPU in hand-written
  * kernels: BF16 tensor-core matrix products with FP32 accumulation
- * (mma.sync m16n8k16), fused bias and ReLU, Adam in FP32 with BF16 copies of
- * the weights.  Data are plain row-major FP32 host arrays; the library keeps
- * its own device copies.  Every call returns a CLIFFS_* status
- * (cliffs_gpu.h). */
+ * (tcgen05.mma with accumulators in tensor memory and TMA-staged operands for
+ * products of at least 128 rows, 16 columns and a 64-wide reduction;
+ * mma.sync m16n8k16 for smaller ones), fused bias and ReLU, Adam in FP32
+ * with BF16 copies of the weights.  Data are plain row-major FP32 host
+ * arrays; the library keeps its own device copies.  Every call returns a
+ * CLIFFS_* status (cliffs_gpu.h). */
 #ifndef CLIFFS_SURROGATE_H
 #define CLIFFS_SURROGATE_H
 #include <stdint.h>
@@ -34,10 +36,12 @@ typedef struct cliffs_mlp_desc {
    * 2x nearest-neighbour upsampling and a 3x3 convolution (zero padding)
    * with a bias: map_ch[0] -> map_ch[1] -> map_ch[2] channels with ReLUs,
    * then map_ch[2] -> 1 channel, a map_side x map_side map.  map_side: a
-   * multiple of 8, <= 512; channels: multiples of 8, <= 64.  Convolutions
-   * run as BF16 tensor-core products (im2col, FP32 accumulation); their
-   * weight gradients as split-K tensor-core products, their input gradients
-   * as FP32 sums of BF16 products. */
+   * multiple of 8, <= 512; channels: multiples of 8, <= 64.  A level with 16
+   * or more output channels runs as a BF16 tensor-core product (im2col,
+   * FP32 accumulation), one with fewer as a direct convolution (FP32 sums of
+   * BF16 products); weight and input gradients are direct FP32 sums of BF16
+   * products in a fixed order.  Batches with a map are limited to
+   * batch * map_side^2 * 16 < 2^31 (CLIFFS_ERR_ARG otherwise). */
   int32_t map_side;
   int32_t map_ch[3];
 } cliffs_mlp_desc;
