@@ -404,8 +404,10 @@ void cliffs_batch_destroy(cliffs_batch *b);
 int cliffs_batch_set_plan(cliffs_batch *b, const cliffs_batch_plan *plan);
 int cliffs_batch_get_plan(const cliffs_batch *b, cliffs_batch_plan *plan);
 /* Advance every context nsteps steps; synchronises at the end.  Returns
- * CLIFFS_ERR_TIMEOUT if a grid barrier wait ran out (the state is then
- * partial). */
+ * CLIFFS_ERR_TIMEOUT if a grid barrier wait ran out: some blocks may then
+ * have written later phases than others, so every context's state is
+ * undefined (a mix of steps, its step count not advanced) until the caller
+ * uploads a state again (cliffs_gpu_upload_state). */
 int cliffs_batch_step(cliffs_batch *b, int32_t nsteps);
 /* Time the candidate plans from a snapshot of the state, restore the
  * snapshot and keep the fastest plan; *ms_per_step gets its time per step.
