@@ -439,7 +439,7 @@ def run_ensemble(args):
         r = E.run(n, steps, seed=0, warmup=max(3, args.warmup))
     if not r["status_ok"]:
         raise RuntimeError("a scenario reported a non-zero status")
-    e2e = ensemble_e2e(pkg, E, n, steps)
+    e2e = ensemble_e2e(pkg, E, n, steps, r["plan"])
     peak, peak_kind = _peaks()
     ms = r["batched_ms_per_step"]
     achieved = B_STEP * cells / (ms / 1e3) / 1e9
@@ -498,13 +498,15 @@ def ensemble_cpu_baseline(E, scs, threads, steps=10):
             "rates_mcell_per_s": {str(k): round(v / 1e6, 1) for k, v in rate.items()}}
 
 
-def ensemble_e2e(pkg, E, n, steps):
+def ensemble_e2e(pkg, E, n, steps, plan):
     """The ensemble end to end through the public API: grids created from the
     host's FP64 bathymetry and initial state (pinned arrays), sources applied
     on the device, the batch and its gauges set up, `steps` steps with the
     gauge records every 10 steps, and every scenario's max-wave fields back
-    to pinned host arrays.  Unit: 2000-step scenarios per second, with the
-    set-up counted once per `steps` steps."""
+    to pinned host arrays.  plan: the device-resident run's plan (the tile
+    shape the autotuner chose there, graphs of 10 steps; no autotuning inside
+    the timed region).  Unit: 2000-step scenarios per second, with the set-up
+    counted once per `steps` steps."""
     import numpy as np
 
     base = E.bathymetries(0)
@@ -533,7 +535,8 @@ def ensemble_e2e(pkg, E, n, steps):
         grids.append(g)
     b = pkg.Batch(grids)
     b.set_gauges(gauges)
-    b.set_plan(pkg.cliffs_gpu.GRAPH, graph_steps=10, x_rows=2, y_groups=2)
+    xr, yg = plan.get("x_rows", 1), plan.get("y_groups", 1)
+    b.set_plan(pkg.cliffs_gpu.GRAPH, graph_steps=10, x_rows=xr, y_groups=yg)
     for s0 in range(0, steps, 10):
         b.step(min(10, steps - s0))
         b.gauges(out=rec)
@@ -548,7 +551,7 @@ def ensemble_e2e(pkg, E, n, steps):
     return {"value": round(n * steps / (E.RUN_STEPS * t), 3), "unit": f"scenarios/s ({E.RUN_STEPS}-step scenarios)",
             "h2d_bytes_per_step": int(h2d // steps), "d2h_bytes_per_step": int(d2h // steps),
             "ms": round(1e3 * t, 1), "gcell_per_s": round(cells * steps / t / 1e9, 2),
-            "plan": "graph of 10 steps, tile shape 2 x 2 (no autotuning inside the timed region)"}
+            "plan": f"graph of 10 steps, tile shape {xr} x {yg} (no autotuning inside the timed region)"}
 
 
 def run_surrogate(args):

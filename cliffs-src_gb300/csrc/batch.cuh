@@ -59,8 +59,10 @@ __device__ __forceinline__ int batch_scenario(const int* off, int n, int t) {
 // all scenarios.  An entry is B.span[DIR] single-grid tiles along the rows: x,
 // span consecutive rows of one 512-cell column chunk; y, span consecutive
 // 16-row groups of one 32-column group.  The scenario's arguments are staged
-// in shared memory once per entry.
-template <int DIR, bool COH, bool MAXOUT>
+// in shared memory once per entry.  MULTI = false: entries of one tile
+// (span 1), with no loop around the tile's code, which keeps the loop's
+// state out of the tile's register budget.
+template <int DIR, bool COH, bool MAXOUT, bool MULTI = true>
 __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int stride) {
   __shared__ SweepArgs sA;
   const int* off = B.off + DIR * (B.n + 1);
@@ -73,7 +75,9 @@ __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int s
     __syncthreads();  // the previous tile is done with sA and its shared list
     if (threadIdx.x == 0) sA = B.args[2 * k + DIR];
     __syncthreads();
-    if (DIR == 0) {  // g: column chunks; rows (local / g) * span ...
+    if (!MULTI) {
+      sweep_tile<DIR, true, COH, true, MAXOUT>(sA, local % g, local / g);
+    } else if (DIR == 0) {  // g: column chunks; rows (local / g) * span ...
       const int bx = local % g, by0 = (local / g) * span;
       for (int r = 0; r < span && by0 + r < sA.nlines; ++r) sweep_tile<0, true, COH, true, MAXOUT>(sA, bx, by0 + r);
     } else {  // g: entries along the column, each span row groups of 16
@@ -146,10 +150,12 @@ __global__ void __launch_bounds__(kBatchThreads, 6) batch_persistent(const Batch
 
 // 64 registers, 8 blocks per SM: with the max-wave fold this measured 3 %
 // faster than 80 registers and 6 blocks (2.34 against 2.41 ms per step on the
-// 256-scenario ensemble), spills included.
-template <int DIR, bool MAXOUT>
+// 256-scenario ensemble), spills included.  MULTI: entries of more than one
+// tile (B.span[DIR] > 1); the one-tile variant has no loop around the tile
+// (2.34 against 2.70 ms per step with the loop at span 1).
+template <int DIR, bool MAXOUT, bool MULTI>
 __global__ void __launch_bounds__(kBatchThreads, 8) batch_phase(const BatchArgs B) {
-  batch_tiles<DIR, false, MAXOUT>(B, blockIdx.x, gridDim.x);
+  batch_tiles<DIR, false, MAXOUT, MULTI>(B, blockIdx.x, gridDim.x);
 }
 
 }  // namespace cliffs

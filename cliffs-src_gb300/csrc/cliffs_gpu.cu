@@ -2625,12 +2625,23 @@ int cliffs_batch_launch_count(const cliffs_batch* b, int64_t* n) {
 
 static int batch_launch_phases(cliffs_batch* b, int steps, bool fold) {
   const BatchArgs B = batch_args(b, 1, fold);
+  const bool mx = B.span[0] > 1, my = B.span[1] > 1;
   for (int s = 0; s < steps; ++s) {
-    batch_phase<0, false><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
-    if (fold)
-      batch_phase<1, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    if (mx)
+      batch_phase<0, false, true><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
     else
-      batch_phase<1, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      batch_phase<0, false, false><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
+    if (fold) {
+      if (my)
+        batch_phase<1, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      else
+        batch_phase<1, false, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    } else {
+      if (my)
+        batch_phase<1, true, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      else
+        batch_phase<1, true, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+    }
     b->launches += 2;
   }
   return cudaGetLastError() == cudaSuccess ? CLIFFS_OK : CLIFFS_ERR_CUDA;
