@@ -4,9 +4,12 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py, never by the product package.  The C library is
 an FP64 restatement of the reference (cliffs.f, cliffs_main.f time loop,
 MasterGrid.f metrics, NestedGrid.f/feed_children_grid.f nesting,
-apply_initial_conditions.f, output_*.f conversions).  Bit-level parity with the
-Fortran build is unpinned (no Fortran compiler here); physics-level parity is
-pinned against the analytic profiles of Examples/slpbeach.zip.
+apply_initial_conditions.f, output_*.f conversions).  Its line update is
+pinned bit for bit to the reference's own subroutine cliffs, translated from
+the checkout's Fortran to C and compiled by oracle/ref_f2c.py
+(tests/test_oracle_reference.py); the time loop around it is checked by
+reading, and physics-level parity against the analytic profiles of
+Examples/slpbeach.zip.
 
 Grids are numpy arrays of shape (ny, nx) in C order, i.e. the Fortran
 (nx, ny) column-major layout with x fastest.

@@ -2,10 +2,11 @@
  * cliffs_oracle.c -- FP64 CPU restatement of the Cliffs hot path.
  *
  * TEST INFRASTRUCTURE ONLY (see cliffs_oracle.h): the checker for the CUDA
- * library and the timed CPU baseline.  Parity with the Fortran reference is
- * unpinned at bit level (the reference cannot be compiled here); the
- * restatement is pinned at physics level against the analytic runup profiles
- * shipped in Examples/slpbeach.zip.
+ * library and the timed CPU baseline.  The line update (orc_line) is pinned
+ * bit for bit to the reference's own subroutine cliffs (cliffs.f:17-346),
+ * translated from the checkout's Fortran and compiled by oracle/ref_f2c.py;
+ * the whole restatement is pinned at physics level against the analytic
+ * runup profiles shipped in Examples/slpbeach.zip.
  *
  * Every function names the reference lines it follows.  Expressions keep the
  * reference's operand order; build with -ffp-contract=off so that no fused
