@@ -668,6 +668,7 @@ SweepArgs sweep_args(const cliffs_ctx* c, int iu, bool fuse_max, int s) {
 // the previous launch when c->pdl is set.
 template <int DIR, bool MAXOUT>
 cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArgs& A) {
+  const bool flat = A.geo_uniform && A.scl == nullptr;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
@@ -678,7 +679,8 @@ cudaError_t launch_fast(cliffs_ctx* c, dim3 grid, unsigned block, const SweepArg
   cfg.stream = c->stream;
   cfg.attrs = at;
   cfg.numAttrs = c->pdl ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT>, A);
+  return flat ? cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT, true>, A)
+              : cudaLaunchKernelEx(&cfg, fast_kernel<DIR, true, MAXOUT, false>, A);
 }
 
 // Max-wave handling of one sweep: none, the update with its outputs (the last

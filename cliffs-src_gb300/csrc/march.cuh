@@ -74,6 +74,49 @@ CL_HD float fsqrt0(float x) {
 }
 CL_HD double fsqrt0(double x) { return csqrt(x); }
 
+// Single operations, each rounded once, as written: on the GPU they are
+// intrinsics, which the compiler neither fuses nor splits, so every kernel
+// that inlines the interior update (flat or general geometry, single grid or
+// batched) rounds it the same way.
+CL_HD float add_rn(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(x, y);
+#else
+  return x + y;
+#endif
+}
+CL_HD float sub_rn(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(x, y);
+#else
+  return x - y;
+#endif
+}
+CL_HD float mul_rn(float x, float y) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(x, y);
+#else
+  return x * y;
+#endif
+}
+CL_HD float fma_rn(float a, float b, float c) {  // a * b + c
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return std::fma(a, b, c);
+#endif
+}
+CL_HD double add_rn(double x, double y) { return x + y; }
+CL_HD double sub_rn(double x, double y) { return x - y; }
+CL_HD double mul_rn(double x, double y) { return x * y; }
+CL_HD double fma_rn(double a, double b, double c) {
+#ifdef __CUDA_ARCH__
+  return __fma_rn(a, b, c);
+#else
+  return std::fma(a, b, c);
+#endif
+}
+
 // x / y where ~2 ulp is enough (y away from 0 and from huge values)
 CL_HD float fdiv(float x, float y) {
 #ifdef __CUDA_ARCH__
@@ -144,17 +187,17 @@ template <typename R>
 CL_HD void face_flux(R ul, R cl, R el, R ur, R cr, R er, const Phys<R>& p,
                      R& FP, R& FQ) {
   // (1/8)(e_l+e_r)(P_r-P_l) - g(d_r-d_l), e = 3P+Q = 4(u+c), and the Q analogue
-  const R U = ul + ur, C = cl + cr, du = ur - ul, dc = cr - cl;
-  const R gde = p.g * (er - el);
-  const R Udc = U * dc;
-  FP = gde + Udc + R(0.5) * (U + C) * du;
-  FQ = gde - Udc + R(0.5) * (U - C) * du;
+  const R U = add_rn(ul, ur), C = add_rn(cl, cr), du = sub_rn(ur, ul), dc = sub_rn(cr, cl);
+  const R gde = mul_rn(p.g, sub_rn(er, el));
+  const R Udc = mul_rn(U, dc);
+  FP = fma_rn(mul_rn(R(0.5), add_rn(U, C)), du, add_rn(gde, Udc));
+  FQ = fma_rn(mul_rn(R(0.5), sub_rn(U, C)), du, sub_rn(gde, Udc));
 }
 
 // Surface state of celerity c (sign kept: H = c|c|/g).
 template <typename R>
 CL_HD R state_from_c(R c, R d, const Phys<R>& p) {
-  return state_from_depth(c * (c < R(0) ? -c : c) * p.ginv, d);
+  return state_from_depth(mul_rn(mul_rn(c, c < R(0) ? -c : c), p.ginv), d);
 }
 
 // State of one cell as the interior update sees it (after flooding).  e and H
@@ -169,8 +212,8 @@ struct CellState {
 // are positive.
 template <typename R>
 CL_HD R state_step(const CellState<R>& j, R dc, const Phys<R>& p) {
-  const R c0 = j.c, c1 = c0 + dc;
-  if (c0 > R(0) && c1 > R(0)) return (j.d < R(0) ? j.H : j.e) + dc * (R(2) * c0 + dc) * p.ginv;
+  const R c0 = j.c, c1 = add_rn(c0, dc);
+  if (c0 > R(0) && c1 > R(0)) return fma_rn(mul_rn(dc, fma_rn(R(2), c0, dc)), p.ginv, j.d < R(0) ? j.H : j.e);
   return state_from_c(c1, j.d, p);
 }
 
@@ -181,39 +224,48 @@ struct NoFlux {};
 // fluxes (a,j) and (j,b).  Returns the new (s, u, v); *cn gets the new
 // celerity.  TC = false leaves out the transcritical-point test, for callers
 // that know no neighbour is supercritical (|u| <= c), where it cannot fire.
-template <typename R, bool TC = true>
+// SPH = false leaves out the metric term, for lines without one (geo.scl 0:
+// the term is then a zero, and leaving it out can change at most the sign
+// of a zero result).
+template <typename R, bool TC = true, bool SPH = true>
 CL_HD OutCell<R> interior_update(const CellState<R>& a, const CellState<R>& j, const CellState<R>& b,
                                  R FPl, R FQl, R FPr, R FQr, const Geo<R>& geo, const Phys<R>& p,
                                  R* cn_out) {
   const R uj = j.u, cj = j.c, vj = j.v, dj = j.d;
   const R inv_fm = geo.inv_fm, inv_fp = geo.inv_fp, dtx = geo.dtx;
   const R r = frsqrt(j.H);  // sqrt((u^2+v^2)/H)/H = |u,v| / H^1.5 (cliffs.f:204)
-  const R cc = p.gcrough * uj * fsqrt0(uj * uj + vj * vj) * (r * r * r);
-  const R sphr = R(8) * cj * uj * geo.scl;  // (P-Q)(P+Q)*scl
-  const R ejP = uj + cj, ejQ = uj - cj;
-  const R QpP = FPr * inv_fp, QmP = FPl * inv_fm;
-  const R QpQ = FQr * inv_fp, QmQ = FQl * inv_fm;
-  R QsP = R(0.5) * (QpP + QmP);
-  R QsQ = R(0.5) * (QpQ + QmQ);
+  const R cc = mul_rn(mul_rn(mul_rn(p.gcrough, uj), fsqrt0(fma_rn(uj, uj, mul_rn(vj, vj)))),
+                      mul_rn(mul_rn(r, r), r));
+  const R sphr = SPH ? mul_rn(mul_rn(mul_rn(R(8), cj), uj), geo.scl) : R(0);  // (P-Q)(P+Q)*scl
+  const R ejP = add_rn(uj, cj), ejQ = sub_rn(uj, cj);
+  const R QpP = mul_rn(FPr, inv_fp), QmP = mul_rn(FPl, inv_fm);
+  const R QpQ = mul_rn(FQr, inv_fp), QmQ = mul_rn(FQl, inv_fm);
+  R QsP = mul_rn(R(0.5), add_rn(QpP, QmP));
+  R QsQ = mul_rn(R(0.5), add_rn(QpQ, QmQ));
   const bool sonP = TC && (a.u + a.c < R(0)) && (b.u + b.c > R(0));
   const bool sonQ = TC && (a.u - a.c < R(0)) && (b.u - b.c > R(0));
   if ((sonP || sonQ) && (dj > p.ground) && (a.d > p.ground) && (b.d > p.ground)) {
     // transcritical point (cliffs.f:228-232, 241-245)
-    const R isum = dtx * p.idt;
-    const R sdiff = R(2) * p.g * (fsqrt_pos(dj * b.d) - fsqrt_pos(dj * a.d));
-    if (sonP) QsP = (ejP * ((b.u - a.u) + R(2) * (b.c - a.c)) - sdiff) * isum;
-    if (sonQ) QsQ = (ejQ * ((b.u - a.u) - R(2) * (b.c - a.c)) - sdiff) * isum;
+    const R isum = mul_rn(dtx, p.idt);
+    const R sdiff = mul_rn(mul_rn(R(2), p.g), sub_rn(fsqrt_pos(mul_rn(dj, b.d)), fsqrt_pos(mul_rn(dj, a.d))));
+    const R du = sub_rn(b.u, a.u), dcl = sub_rn(b.c, a.c);
+    if (sonP) QsP = mul_rn(sub_rn(mul_rn(ejP, fma_rn(R(2), dcl, du)), sdiff), isum);
+    if (sonQ) QsQ = mul_rn(sub_rn(mul_rn(ejQ, fma_rn(R(-2), dcl, du)), sdiff), isum);
   }
-  QsP = QsP + ejP * dtx * (QmP - QpP);
-  QsQ = QsQ + ejQ * dtx * (QmQ - QpQ);
-  const R dP = -p.dt * (QsP + cc - sphr);
-  const R dQ = -p.dt * (QsQ + cc + sphr);
-  const R Qv = (b.v - vj) * inv_fp - (vj - a.v) * inv_fm;
+  QsP = fma_rn(mul_rn(ejP, dtx), sub_rn(QmP, QpP), QsP);
+  QsQ = fma_rn(mul_rn(ejQ, dtx), sub_rn(QmQ, QpQ), QsQ);
+  // -dt (Qs + cc -/+ sphr); without the metric term the zero is left out
+  const R qcP = add_rn(QsP, cc), qcQ = add_rn(QsQ, cc);
+  const R mdt = -p.dt;
+  const R dP = mul_rn(mdt, SPH ? sub_rn(qcP, sphr) : qcP);
+  const R dQ = mul_rn(mdt, SPH ? add_rn(qcQ, sphr) : qcQ);
+  const R Qv = fma_rn(sub_rn(b.v, vj), inv_fp, -mul_rn(sub_rn(vj, a.v), inv_fm));
   OutCell<R> o;
-  o.v = vj - uj * dtx * ((b.v - a.v) - Qv * (uj * p.dt + geo.dfpm));
-  const R dc = R(0.25) * (dP - dQ);
-  *cn_out = cj + dc;
-  o.u = uj + R(0.5) * (dP + dQ);
+  const R vx = fma_rn(-Qv, fma_rn(uj, p.dt, geo.dfpm), sub_rn(b.v, a.v));
+  o.v = fma_rn(-mul_rn(uj, dtx), vx, vj);
+  const R dc = mul_rn(R(0.25), sub_rn(dP, dQ));
+  *cn_out = add_rn(cj, dc);
+  o.u = fma_rn(R(0.5), add_rn(dP, dQ), uj);
   o.s = state_step(j, dc, p);
   return o;
 }
@@ -225,14 +277,14 @@ CL_HD void edge_left(const CellState<R>& C, const CellState<R>& B, const EdgeVal
                      const Phys<R>& p, R& cn, R& un, R& vn, R& sn) {
   R FP, FQ;
   face_flux(C.u, C.c, C.e, B.u, B.c, B.e, p, FP, FQ);
-  const R sphr = R(8) * C.c * C.u * scl1;
-  const R dQ = -p.dt * (FQ * inv_dx1 + sphr);
-  const R cbnd = fsqrt_pos(p.g * (C.d + e.eta));  // C.d + e.eta > ground: the caller's edge condition
-  const R dP = (e.un - C.u) + fdiv(R(2) * p.g * (e.eta - C.e), cbnd + C.c);
-  vn = (C.u < R(0)) ? C.v - p.dt * (B.v - C.v) * C.u * inv_dx1 : e.vt;
-  const R dc = R(0.25) * (dP - dQ);
-  cn = C.c + dc;
-  un = C.u + R(0.5) * (dP + dQ);
+  const R sphr = mul_rn(mul_rn(mul_rn(R(8), C.c), C.u), scl1);
+  const R dQ = mul_rn(-p.dt, fma_rn(FQ, inv_dx1, sphr));
+  const R cbnd = fsqrt_pos(mul_rn(p.g, add_rn(C.d, e.eta)));  // C.d + e.eta > ground: the caller's edge condition
+  const R dP = add_rn(sub_rn(e.un, C.u), fdiv(mul_rn(mul_rn(R(2), p.g), sub_rn(e.eta, C.e)), add_rn(cbnd, C.c)));
+  vn = (C.u < R(0)) ? sub_rn(C.v, mul_rn(mul_rn(mul_rn(p.dt, sub_rn(B.v, C.v)), C.u), inv_dx1)) : e.vt;
+  const R dc = mul_rn(R(0.25), sub_rn(dP, dQ));
+  cn = add_rn(C.c, dc);
+  un = fma_rn(R(0.5), add_rn(dP, dQ), C.u);
   sn = state_step(C, dc, p);
 }
 
@@ -243,14 +295,14 @@ CL_HD void edge_right(const CellState<R>& D, const CellState<R>& C, const EdgeVa
                       const Phys<R>& p, R& cn, R& un, R& vn, R& sn) {
   R FP, FQ;
   face_flux(D.u, D.c, D.e, C.u, C.c, C.e, p, FP, FQ);
-  const R sphr = R(8) * C.c * C.u * scln;
-  const R dP = -p.dt * (FP * inv_dxn1 - sphr);
-  const R cbnd = fsqrt_pos(p.g * (C.d + e.eta));  // C.d + e.eta > ground: the caller's edge condition
-  const R dQ = (e.un - C.u) - fdiv(R(2) * p.g * (e.eta - C.e), cbnd + C.c);
-  vn = (C.u > R(0)) ? C.v - p.dt * (C.v - D.v) * C.u * inv_dxn1 : e.vt;
-  const R dc = R(0.25) * (dP - dQ);
-  cn = C.c + dc;
-  un = C.u + R(0.5) * (dP + dQ);
+  const R sphr = mul_rn(mul_rn(mul_rn(R(8), C.c), C.u), scln);
+  const R dP = mul_rn(-p.dt, fma_rn(FP, inv_dxn1, -sphr));
+  const R cbnd = fsqrt_pos(mul_rn(p.g, add_rn(C.d, e.eta)));  // C.d + e.eta > ground: the caller's edge condition
+  const R dQ = sub_rn(sub_rn(e.un, C.u), fdiv(mul_rn(mul_rn(R(2), p.g), sub_rn(e.eta, C.e)), add_rn(cbnd, C.c)));
+  vn = (C.u > R(0)) ? sub_rn(C.v, mul_rn(mul_rn(mul_rn(p.dt, sub_rn(C.v, D.v)), C.u), inv_dxn1)) : e.vt;
+  const R dc = mul_rn(R(0.25), sub_rn(dP, dQ));
+  cn = add_rn(C.c, dc);
+  un = fma_rn(R(0.5), add_rn(dP, dQ), C.u);
   sn = state_step(C, dc, p);
 }
 

@@ -206,7 +206,7 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
   A.yv_o[q] = yo;
   if (A.hmax) {  // max-wave update (cliffs_main.f:347-355)
     A.hmax[q] = fmaxf(hm, eta_of(r.s, dq));
-    A.velmax[q] = fmaxf(vm, xo * xo + yo * yo);
+    A.velmax[q] = fmaxf(vm, fma_rn(xo, xo, mul_rn(yo, yo)));
   }
   if (!isfinite(r.s + xo + yo)) atomicOr(A.status, ST_NAN);
 }
@@ -268,8 +268,10 @@ __device__ __forceinline__ unsigned rest_cells(const SweepArgs& A, int L, int i0
 // in os/ou/ov where the cell is interior, wet between wet neighbours, and no
 // transcritical point can occur (a transcritical point needs a supercritical
 // neighbour).  Returns the cells that are not plain interior cells (bit r);
-// cour gets the max of (|u|+c) dt/(dx(m-1)+dx(m)) over the 4 cells.
-template <bool SHARED_ARGS>
+// cour gets the max of (|u|+c) dt/(dx(m-1)+dx(m)) over the 4 cells.  FLAT:
+// the line is known to have uniform spacing and no metric term (the caller
+// checked A.geo_uniform and A.scl == nullptr), so neither is read per cell.
+template <bool SHARED_ARGS, bool FLAT = false>
 __device__ __forceinline__ unsigned plain_cells(const SweepArgs& A, int i0, bool sup, const float (&d)[6],
                                                 const float (&e)[6], const float (&u)[6], const float (&v)[6],
                                                 const float (&H)[6], const float (&c)[6], const bool (&wet)[6],
@@ -290,8 +292,10 @@ __device__ __forceinline__ unsigned plain_cells(const SweepArgs& A, int i0, bool
     const CellState<float> j{u[w], c[w], e[w], d[w], v[w], H[w]};
     const CellState<float> b{u[w + 1], c[w + 1], e[w + 1], d[w + 1], v[w + 1], H[w + 1]};
     float cn;
-    const Geo<float> gk = SHARED_ARGS ? geo_at(A, k, alpha, ialpha) : geo_plain(A, min(k, n), g0, alpha, ialpha);
-    const OutCell<float> o = interior_update<float, false>(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], gk, p, &cn);
+    const Geo<float> gk =
+        FLAT ? g0 : SHARED_ARGS ? geo_at(A, k, alpha, ialpha) : geo_plain(A, min(k, n), g0, alpha, ialpha);
+    const OutCell<float> o =
+        interior_update<float, false, !FLAT>(a, j, b, FP[w - 1], FQ[w - 1], FP[w], FQ[w], gk, p, &cn);
     // (|u|+c) dt / ((dx(m-1)+dx(m))/2) = 2 (|u|+c) dtx, of the state read
     cour = fmaxf(cour, (fabsf(u[w]) + c[w]) * gk.dtx);
     os[r] = plain ? o.s : os[r];
@@ -302,7 +306,8 @@ __device__ __forceinline__ unsigned plain_cells(const SweepArgs& A, int i0, bool
   return rest;
 }
 
-template <int DIR, bool LOCAL, bool COH, bool TAIL = true, bool SHARED_ARGS = false, bool MAXOUT = true>
+template <int DIR, bool LOCAL, bool COH, bool TAIL = true, bool SHARED_ARGS = false, bool MAXOUT = true,
+          bool FLAT = false>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
@@ -314,8 +319,9 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
 // One tile of a sweep: the block's cells at block coordinates (bx, by) of the
 // sweep's grid (x: (columns / (4 * blockDim.x), rows); y: (rows / (4 * warps),
 // columns / 32)).  The whole block calls it.  MAXOUT = false leaves out the
-// max-wave update of the outputs (A.hmax is then ignored).
-template <int DIR, bool LOCAL, bool COH, bool SHARED_ARGS = false, bool MAXOUT = true>
+// max-wave update of the outputs (A.hmax is then ignored).  FLAT: uniform
+// spacing and no metric term (plain_cells).
+template <int DIR, bool LOCAL, bool COH, bool SHARED_ARGS = false, bool MAXOUT = true, bool FLAT = false>
 __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
   __shared__ uint32_t s_list[LOCAL ? 256 * 4 : 1];
   __shared__ unsigned s_n;
@@ -372,10 +378,10 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
         HI.y = fmaxf(HI.y, eta_of(E4.y, D4.y));
         HI.z = fmaxf(HI.z, eta_of(E4.z, D4.z));
         HI.w = fmaxf(HI.w, eta_of(E4.w, D4.w));
-        VI.x = fmaxf(VI.x, X4.x * X4.x + Y4.x * Y4.x);
-        VI.y = fmaxf(VI.y, X4.y * X4.y + Y4.y * Y4.y);
-        VI.z = fmaxf(VI.z, X4.z * X4.z + Y4.z * Y4.z);
-        VI.w = fmaxf(VI.w, X4.w * X4.w + Y4.w * Y4.w);
+        VI.x = fmaxf(VI.x, fma_rn(X4.x, X4.x, mul_rn(Y4.x, Y4.x)));
+        VI.y = fmaxf(VI.y, fma_rn(X4.y, X4.y, mul_rn(Y4.y, Y4.y)));
+        VI.z = fmaxf(VI.z, fma_rn(X4.z, X4.z, mul_rn(Y4.z, Y4.z)));
+        VI.w = fmaxf(VI.w, fma_rn(X4.w, X4.w, mul_rn(Y4.w, Y4.w)));
         *reinterpret_cast<float4*>(A.hmax_in + q0) = HI;
         *reinterpret_cast<float4*>(A.velmax_in + q0) = VI;
       }
@@ -430,7 +436,8 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
       }
     }
   }
-  sweep_cells<DIR, LOCAL, COH, true, SHARED_ARGS, MAXOUT>(A, L, i0, active, q0, d, e, u, v, hm, vm, s_list, &s_n);
+  sweep_cells<DIR, LOCAL, COH, true, SHARED_ARGS, MAXOUT, FLAT>(A, L, i0, active, q0, d, e, u, v, hm, vm, s_list,
+                                                                &s_n);
 }
 
 // The cells i0..i0+3 of line L from their loaded window: d depth, e surface
@@ -444,7 +451,7 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
 // lives in shared memory (the batched kernels), where every field read is a
 // load; the geometry is then read per cell instead of held in registers for
 // the whole line, which measured 14 % faster there (fewer spills).
-template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS, bool MAXOUT>
+template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS, bool MAXOUT, bool FLAT>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
@@ -489,7 +496,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
     float FP[5], FQ[5];  // face fluxes between window cells w and w+1
 #pragma unroll
     for (int f = 0; f < 5; ++f) face_flux(u[f], c[f], e[f], u[f + 1], c[f + 1], e[f + 1], p, FP[f], FQ[f]);
-    const unsigned rest = plain_cells<SHARED_ARGS>(A, i0, sup, d, e, u, v, H, c, wet, FP, FQ, alpha, ialpha, os, ou,
+    const unsigned rest = plain_cells<SHARED_ARGS, FLAT>(A, i0, sup, d, e, u, v, H, c, wet, FP, FQ, alpha, ialpha, os, ou,
                                                    ov, cour);
     if (rest) need = rest_cells(A, L, i0, rest, d, e, u, v, H, c, wet, ialpha, os, ou, ov);
   }
@@ -514,7 +521,7 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
     if (done) bad |= !isfinite(os[r] + xo[r] + yo[r]);
     if (MAXOUT && A.hmax && done) {  // max-wave update (cliffs_main.f:347-355)
       hm[r] = fmaxf(hm[r], eta_of(os[r], d[r + 1]));
-      vm[r] = fmaxf(vm[r], xo[r] * xo[r] + yo[r] * yo[r]);
+      vm[r] = fmaxf(vm[r], fma_rn(xo[r], xo[r], mul_rn(yo[r], yo[r])));
     }
   }
   if (!active) {
@@ -568,12 +575,15 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
 // launch attribute both instructions are no-ops.
 // MAXOUT = false: the variant without the max-wave update of the outputs
 // (the y-sweep of a two-dimensional step, whose end state the next x-sweep
-// folds in through hmax_in).
-template <int DIR, bool LOCAL, bool MAXOUT = true>
+// folds in through hmax_in).  FLAT = true: a grid whose lines of this
+// direction have uniform spacing and no metric term (A.geo_uniform,
+// A.scl == nullptr: every x-sweep of a grid with uniform dx, every y-sweep
+// of a Cartesian grid with uniform dy).
+template <int DIR, bool LOCAL, bool MAXOUT = true, bool FLAT = false>
 __global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  sweep_tile<DIR, LOCAL, false, false, MAXOUT>(A, blockIdx.x, blockIdx.y);
+  sweep_tile<DIR, LOCAL, false, false, MAXOUT, FLAT>(A, blockIdx.x, blockIdx.y);
 }
 
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
