@@ -28,6 +28,12 @@ the library's kernels, then --steps gated passes over 256 held-out
 scenarios against one-at-a-time solves; the metric is scenarios/s of the
 gated path (surrogate plus solver fallbacks).
 
+The default line (the shelf, one GPU) also carries "workloads": the other
+configurations of the benchmark set, each run whole in its own process after
+the shelf's measurements (the batched ensemble of 256 scenarios, the learned
+surrogate, the nested spherical chain over 6 model hours), with their own
+metrics and baselines; --kernels-only leaves them out.
+
 --impl reference times the CPU restatement of the reference solver (the
 Fortran reference cannot be compiled on these hosts) with all host threads on
 the same workload.  With N > 1 (torchrun) every rank runs an independent
@@ -395,6 +401,10 @@ def run_ours(args):
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
                 "gpu_launches": int(launches),
                 "hbm_frac_step": round(B_STEP * cells * args.steps / (ms / 1e3) / 1e9 / peak, 4)}
+        if world == 1 and args.workload == "shelf2048" and not args.kernels_only:
+            # this process's cached device memory goes back before the children run
+            torch.cuda.empty_cache()
+            line["workloads"] = side_workloads()
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -650,6 +660,83 @@ def surrogate_cpu_baseline(S, threads, steps=100):
             "steps": steps, "ms_per_step": round(1e3 * t, 3),
             "sample": f"one {S.SIDE}x{S.SIDE} scenario, {steps} time steps after 1 warm-up step, OpenMP over lines "
                       f"({threads} threads), FP64; scenarios/s of 2000-step runs"}
+
+
+def _json_lines(text):
+    out = []
+    for ln in text.splitlines():
+        ln = ln.strip()
+        if ln.startswith("{"):
+            try:
+                out.append(json.loads(ln))
+            except ValueError:
+                pass
+    return out
+
+
+def _child(cmd, timeout):
+    """Runs one workload in its own process (its own CUDA context: a failure
+    there leaves this process's line intact); returns its JSON lines, or an
+    error string."""
+    t0 = time.perf_counter()
+    try:
+        p = subprocess.run([sys.executable, *cmd], cwd=ROOT, capture_output=True, text=True, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return None, f"timed out after {timeout} s", time.perf_counter() - t0
+    lines = _json_lines(p.stdout)
+    if p.returncode != 0 or not lines:
+        tail = (p.stderr or p.stdout).strip().splitlines()[-1:] or [""]
+        return None, f"exit {p.returncode}: {tail[0][:200]}", time.perf_counter() - t0
+    return lines, None, time.perf_counter() - t0
+
+
+def side_workloads():
+    """The other configurations of the benchmark set, each run whole in its
+    own process after the main line's measurements and summarised into it:
+    the batched ensemble of 256 scenarios (200 timed steps against the same
+    scenarios one at a time), the learned surrogate (4096 training runs from
+    the batched solver, networks trained on the GPU, gated passes over 256
+    held-out scenarios against one-at-a-time solves) and the nested spherical
+    chain (4320 x 2160 master, 600^2 and 900^2 children, 6 model hours)."""
+    res = {}
+    lines, err, wall = _child(["bench.py", "--workload", "ensemble256", "--steps", "200", "--warmup", "5"], 900)
+    if err:
+        res["ensemble256"] = {"error": err}
+    else:
+        e = lines[-1]
+        res["ensemble256"] = {
+            "command": "python bench.py --workload ensemble256 --steps 200 --warmup 5",
+            "metric": e["metric"], "value": e["value"], "unit": e["unit"], "ms_per_step": e["ms_per_step"],
+            "one_at_a_time": e["sequential"], "speedup_vs_one_at_a_time": e["speedup_vs_sequential"],
+            "plan": e["config"].get("plan"), "autotune_ms_per_step": e["autotune_ms_per_step"],
+            "e2e": e["e2e"], "hbm_frac_step": e["roofline"]["frac"],
+            "cpu_baseline": e["cpu_baseline"], "gpu_launches": e["gpu_launches"], "wall_s": round(wall, 1)}
+    lines, err, wall = _child(["bench.py", "--workload", "surrogate", "--steps", "3", "--warmup", "1"], 1200)
+    if err:
+        res["surrogate"] = {"error": err}
+    else:
+        s = lines[-1]
+        res["surrogate"] = {
+            "command": "python bench.py --workload surrogate --steps 3 --warmup 1",
+            "metric": s["metric"], "value": s["value"], "unit": s["unit"],
+            "one_at_a_time_scenarios_per_s": s["one_at_a_time_scenarios_per_s"],
+            "speedup_vs_one_at_a_time": s["speedup_vs_one_at_a_time"],
+            "gauge_rel_err_gated_mean": s["gauge_rel_err_gated_mean"], "fallback": s["fallback"],
+            "map_iou_mean": s["map_iou_mean"], "infer_scenarios_per_s": s["infer_scenarios_per_s"],
+            "data_seconds": s["data_seconds"], "train_seconds": s["train_seconds"],
+            "roofline": s["roofline"], "wall_s": round(wall, 1)}
+    lines, err, wall = _child(["cliffs-src_gb300/nested.py", "--scale", "full", "--hours", "6"], 900)
+    if err:
+        res["nested_sphere"] = {"error": err}
+    else:
+        tot = lines[-1]
+        res["nested_sphere"] = {
+            "command": "python cliffs-src_gb300/nested.py --scale full --hours 6",
+            "levels": [{k: lv.get(k) for k in ("name", "shape", "t0", "steps", "wall_s", "cell_updates_per_s",
+                                               "status", "max_eta", "land_wetted") if k in lv} for lv in lines[:-1]],
+            "wall_s": tot["wall_s"], "cell_updates": tot["cell_updates"],
+            "mcell_updates_per_s": round(tot["cell_updates_per_s"] / 1e6, 1)}
+    return res
 
 
 def main():
