@@ -96,6 +96,11 @@ int make_map(CUtensorMap* m, const float* base, int nx, int ny, int pitch, int b
 }  // namespace
 
 struct cliffs_ctx {
+  // one device allocation holding the per-grid arrays (dep, the state
+  // copies, the max-wave fields, geometry, status words, worklist, edge
+  // tables, dep64, xfer), carved at 256-byte boundaries: cudaMalloc costs
+  // ~50 us per large block, one call for all of them a tenth of that
+  char* arena = nullptr;
   int dev = 0;
   int nx = 0, ny = 0, pitch = 0;
   bool xrun = false, yrun = false;
@@ -212,6 +217,16 @@ int dalloc(T** p, size_t n) {
   if (n == 0) n = 1;
   if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) return CLIFFS_ERR_NOMEM;
   return CLIFFS_OK;
+}
+
+// Reserves n elements of T at the next 256-byte boundary of an arena at
+// offset `off`; with base == nullptr it only advances the offset (the sizing
+// pass).
+template <typename T>
+void carve(char* base, size_t& off, T** p, size_t n) {
+  off = (off + 255) & ~(size_t)255;
+  if (base) *p = reinterpret_cast<T*>(base + off);
+  off += (n ? n : 1) * sizeof(T);
 }
 
 // dep64 is the caller's FP64 depth.  The device keeps FP32 depths, which a
@@ -736,7 +751,7 @@ int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double
       CK((launch_fast<0, false>(c, grid, (unsigned)c->blk_x, A)));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
-    const dim3 grid((A.n + rows - 1) / rows, (A.nlines + 31) / 32);
+    const dim3 grid((A.nlines + 31) / 32, (A.n + rows - 1) / rows);  // (column groups, bands)
     ++c->launches;
     if (maxm == MAXM_OUT)
       CK((launch_fast<1, true>(c, grid, (unsigned)(32 * c->warps_y), A)));
@@ -891,15 +906,33 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   };
   if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
   c->stream = c->own;
-  if (dalloc(&c->dep, cells) || dalloc(&c->srf[0], cells) || dalloc(&c->srf[1], cells) ||
-      dalloc(&c->xu[0], cells) || dalloc(&c->xu[1], cells) || dalloc(&c->yv[0], cells) ||
-      dalloc(&c->yv[1], cells) || dalloc(&c->hmax, cells) || dalloc(&c->velmax, cells) ||
-      dalloc(&c->geo_x, (size_t)c->nx) || dalloc(&c->geo_y, (size_t)c->ny) ||
-      dalloc(&c->scl_y, (size_t)c->ny) || dalloc(&c->lscale, (size_t)c->ny) ||
-      dalloc(&c->status, 2) || dalloc(&c->d_flag, 1) || dalloc(&c->list, (size_t)c->nx * c->ny) ||
-      dalloc(&c->edge_x, (size_t)c->ny * 6) || dalloc(&c->edge_y, (size_t)c->nx * 6) ||
-      dalloc(&c->cnt, 2) || dalloc(&c->dep64, (size_t)c->nx * c->ny))
-    return fail(CLIFFS_ERR_NOMEM);
+  const size_t n64 = (size_t)c->nx * c->ny;
+  auto layout = [&](char* base) {
+    size_t off = 0;
+    carve(base, off, &c->dep, cells);
+    for (int k = 0; k < 2; ++k) {
+      carve(base, off, &c->srf[k], cells);
+      carve(base, off, &c->xu[k], cells);
+      carve(base, off, &c->yv[k], cells);
+    }
+    carve(base, off, &c->hmax, cells);
+    carve(base, off, &c->velmax, cells);
+    carve(base, off, &c->geo_x, (size_t)c->nx);
+    carve(base, off, &c->geo_y, (size_t)c->ny);
+    carve(base, off, &c->scl_y, (size_t)c->ny);
+    carve(base, off, &c->lscale, (size_t)c->ny);
+    carve(base, off, &c->status, 2);
+    carve(base, off, &c->d_flag, 1);
+    carve(base, off, &c->list, n64);
+    carve(base, off, &c->edge_x, (size_t)c->ny * 6);
+    carve(base, off, &c->edge_y, (size_t)c->nx * 6);
+    carve(base, off, &c->cnt, 2);
+    carve(base, off, &c->dep64, n64);
+    carve(base, off, &c->xfer, 3 * n64);
+    return off;
+  };
+  if (dalloc(&c->arena, layout(nullptr))) return fail(CLIFFS_ERR_NOMEM);
+  layout(c->arena);
   // bathymetry: the FP64 depth as passed, and its rounding in padded rows
   if (cudaMemcpyAsync(c->dep64, d->dep, (size_t)c->nx * c->ny * sizeof(double), cudaMemcpyHostToDevice,
                       c->stream) != cudaSuccess)
@@ -951,14 +984,8 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
       cudaMemset(c->status, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(c->cnt, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
-  if (!d->row_scale) {
-    cudaFree(c->lscale);
-    c->lscale = nullptr;
-  }
-  if (!zeta_nonzero) {
-    cudaFree(c->scl_y);
-    c->scl_y = nullptr;
-  }
+  if (!d->row_scale) c->lscale = nullptr;  // (its arena slot stays unused)
+  if (!zeta_nonzero) c->scl_y = nullptr;
   // the staged sweep kernels: tensor maps of the y-sweep's fields and the
   // resident grid of each kernel; without them the context keeps fast_kernel
   {
@@ -987,11 +1014,8 @@ void cliffs_gpu_destroy(cliffs_ctx* c) {
   if (!c) return;
   cudaStreamSynchronize(c->stream);
   flush_profile(c);
-  void* ptrs[] = {c->dep, c->srf[0], c->srf[1], c->xu[0], c->xu[1], c->yv[0], c->yv[1],
-                  c->hmax, c->velmax, c->list, c->cnt,
-                  c->geo_x, c->geo_y, c->scl_y, c->lscale, c->fw, c->fe, c->fs, c->fn,
-                  c->edge_s[0], c->edge_s[1], c->status, c->red, c->d_flag, c->edge_x, c->edge_y,
-                  c->rise_q, c->ring_x, c->ring_y, c->ring_irec, c->ring_cc, c->dep64, c->xfer};
+  void* ptrs[] = {c->arena, c->fw, c->fe, c->fs, c->fn, c->edge_s[0], c->edge_s[1], c->red,
+                  c->rise_q, c->ring_x, c->ring_y, c->ring_irec, c->ring_cc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& n : c->nests) {

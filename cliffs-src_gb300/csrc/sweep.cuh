@@ -583,7 +583,15 @@ template <int DIR, bool LOCAL, bool MAXOUT = true, bool FLAT = false>
 __global__ void __launch_bounds__(256, 4) fast_kernel(const SweepArgs A) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  sweep_tile<DIR, LOCAL, false, false, MAXOUT, FLAT>(A, blockIdx.x, blockIdx.y);
+  if (DIR == 0 || !LOCAL) {  // the worklist variant: grid (bands, column groups) for the y-sweep
+    sweep_tile<DIR, LOCAL, false, false, MAXOUT, FLAT>(A, blockIdx.x, blockIdx.y);
+  } else {
+    // y tiles in bands of 4 * warps rows, the last band first: the x-sweep
+    // before this one wrote its rows first to last, so the bands it wrote
+    // last are read while they are still in L2; this sweep in turn writes the
+    // first bands last, which the next x-sweep reads first
+    sweep_tile<DIR, LOCAL, false, false, MAXOUT, FLAT>(A, (int)(gridDim.y - 1 - blockIdx.y), blockIdx.x);
+  }
 }
 
 // One thread per listed cell: the full wet/dry rules over its +-3 window.
