@@ -6,7 +6,7 @@ y-sweep over all columns), i.e. one pass of the hot path of
 cliffs_main.f:303-355.  Metric: Mcell-updates/s = nx*ny*steps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--kernels-only] [--workload shelf2048|sphere4320] [--sweep tiled|staged]
+                  [--kernels-only] [--workload shelf2048|sphere4320] [--sweep tiled|direct|staged]
 
 --kernels-only runs the device-resident passes alone (no end-to-end pass, no
 CPU sample): the command the ncu summaries under profiles/ capture.
@@ -311,7 +311,7 @@ def run_ours(args):
 
     # ---- device-resident throughput (value) ----------------------------------
     stream = torch.cuda.Stream()
-    kind = pkg.cliffs_gpu.STAGED if args.sweep == "staged" else pkg.cliffs_gpu.TILED
+    kind = {"tiled": pkg.cliffs_gpu.TILED, "direct": pkg.cliffs_gpu.DIRECT, "staged": pkg.cliffs_gpu.STAGED}[args.sweep]
     g = pkg.GpuGrid.from_case(case)
     g.set_stream(stream.cuda_stream)
     g.set_sweep_kernel(kind)
@@ -368,7 +368,8 @@ def run_ours(args):
         bx, by = B_Y, B_X
     else:
         names = ("x-sweep + max-wave of the previous step's end state: fast_kernel<0, true, false>",
-                 "y-sweep: fast_kernel<1, true, false>")
+                 "y-sweep: tile_y_kernel (tiles in and out by tensor-map copies)" if args.sweep == "tiled"
+                 else "y-sweep: fast_kernel<1, true, false>")
         bx, by = B_X, B_Y
     if ky >= kx:
         kname, kms, bpc = names[1], ky, by
@@ -747,7 +748,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernels-only", action="store_true")
     ap.add_argument("--workload", default="shelf2048", choices=["shelf2048", "sphere4320", "ensemble256", "surrogate"])
-    ap.add_argument("--sweep", default="tiled", choices=["tiled", "staged"],
+    ap.add_argument("--sweep", default="tiled", choices=["tiled", "direct", "staged"],
                     help="sweep kernels of the device-resident passes (cliffs_gpu_set_sweep_kernel)")
     args = ap.parse_args()
     if args.warmup < 3:

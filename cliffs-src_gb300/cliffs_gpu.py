@@ -70,7 +70,7 @@ class BatchPlan(ctypes.Structure):
 
 
 PERSISTENT, GRAPH = 0, 1
-TILED, STAGED = 0, 1  # cliffs_gpu_set_sweep_kernel
+TILED, STAGED, DIRECT = 0, 1, 2  # cliffs_gpu_set_sweep_kernel
 LATTICE_SURFACE, LATTICE_BOTTOM, LATTICE_XVEL, LATTICE_YVEL = 0, 1, 2, 3  # cliffs_gpu_apply_lattice
 
 

@@ -16,6 +16,7 @@
 #include "../../include/cliffs_gpu.h"
 #include "batch.cuh"
 #include "staged.cuh"
+#include "ytile.cuh"
 #include "depth_ssl.cuh"
 #include "boundary.cuh"
 
@@ -169,6 +170,10 @@ struct cliffs_ctx {
   int sweep_kind = CLIFFS_SWEEP_TILED;
   bool staged_ok = false;
   CUtensorMap m_dep, m_srf[2], m_xu[2], m_yv[2], m_hmax, m_velmax;
+  // the state copies with a 32 x kYRows box: the tile stores of tile_y_kernel
+  // (the y-sweep of the tiled kernels when ytile_ok)
+  CUtensorMap m_srf16[2], m_xu16[2], m_yv16[2];
+  bool ytile_ok = false;
   int grid_sx = 0, grid_sy = 0;  // resident blocks of staged_x / staged_y
   unsigned long long stage_ns = 2000000000ull;  // limit of one stage wait
   // fast-kernel sweeps launched as programmatic dependents of the previous
@@ -749,6 +754,27 @@ int launch_sweep(cliffs_ctx* c, int iu, int maxm, const double* fA, const double
       CK((launch_fast<0, true>(c, grid, (unsigned)c->blk_x, A)));
     else
       CK((launch_fast<0, false>(c, grid, (unsigned)c->blk_x, A)));
+  } else if (c->sweep_kind == CLIFFS_SWEEP_TILED && c->ytile_ok && maxm != MAXM_OUT && c->warps_y == 4) {
+    // the y-sweep of a two-dimensional step: tiles staged by the copy engine
+    const dim3 grid((A.nlines + 31) / 32, (A.n + kYRows - 1) / kYRows);  // (column groups, bands)
+    const int s = c->cur;
+    const YTileMaps M{c->m_dep, c->m_srf[s], c->m_xu[s], c->m_yv[s], c->m_srf16[1 - s], c->m_xu16[1 - s],
+                      c->m_yv16[1 - s]};
+    const StageCtl S{c->stage_ns, 0u};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kStagedThreads);
+    cfg.stream = c->stream;
+    cfg.attrs = at;
+    cfg.numAttrs = c->pdl ? 1 : 0;
+    ++c->launches;
+    if (A.geo_uniform && A.scl == nullptr)
+      CK(cudaLaunchKernelEx(&cfg, tile_y_kernel<true>, A, M, S));
+    else
+      CK(cudaLaunchKernelEx(&cfg, tile_y_kernel<false>, A, M, S));
   } else {
     const int rows = c->warps_y * kCellsPerThread;
     const dim3 grid((A.nlines + 31) / 32, (A.n + rows - 1) / rows);  // (column groups, bands)
@@ -1003,6 +1029,12 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
            !make_map(&c->m_xu[k], c->xu[k], nx, ny, pp, 32, kYWin) &&
            !make_map(&c->m_yv[k], c->yv[k], nx, ny, pp, 32, kYWin);
     c->staged_ok = ok;
+    bool yt = ok;
+    for (int k = 0; k < 2 && yt; ++k)
+      yt = !make_map(&c->m_srf16[k], c->srf[k], nx, ny, pp, 32, kYRows) &&
+           !make_map(&c->m_xu16[k], c->xu[k], nx, ny, pp, 32, kYRows) &&
+           !make_map(&c->m_yv16[k], c->yv[k], nx, ny, pp, 32, kYRows);
+    c->ytile_ok = yt;
     c->grid_sx = nsm * bx;
     c->grid_sy = nsm * by;
   }
@@ -2258,7 +2290,8 @@ int cliffs_gpu_courant(cliffs_ctx* c, double* courant) {
 }
 
 int cliffs_gpu_set_sweep_kernel(cliffs_ctx* c, int32_t kind) {
-  if (!c || (kind != CLIFFS_SWEEP_TILED && kind != CLIFFS_SWEEP_STAGED)) return CLIFFS_ERR_ARG;
+  if (!c || (kind != CLIFFS_SWEEP_TILED && kind != CLIFFS_SWEEP_STAGED && kind != CLIFFS_SWEEP_DIRECT))
+    return CLIFFS_ERR_ARG;
   if (c->have_state) RET(max_sync(c));  // the staged kernels fold nothing in
   c->sweep_kind = kind;
   return CLIFFS_OK;

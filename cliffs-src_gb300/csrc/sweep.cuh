@@ -175,19 +175,50 @@ __device__ __forceinline__ void enqueue(const SweepArgs& A, bool want, uint32_t 
 }
 
 constexpr int kCellsPerThread = 4;
+// cells of a y-sweep tile staged in shared memory: 16 rows (4 warps of 4) x 32 columns
+constexpr int kYTileCells = 16 * 32;
 
-// One listed cell through the full rules, written with its max-wave update.
+// Line L and position o of a worklist entry (line-1)*n + (position-1).
+__device__ __forceinline__ void entry_cell(const SweepArgs& A, uint32_t ent, int& L, int& o) {
+  L = (int)(ent / (uint32_t)A.n) + 1;
+  o = (int)(ent % (uint32_t)A.n) + 1;
+}
+
+// The value of line cell (L, o) through the full rules.
 template <int DIR, bool COH>
-__device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
+__device__ __forceinline__ OutCell<float> general_value(const SweepArgs& A, int L, int o) {
   const int n = A.n;
-  const int L = (int)(ent / (uint32_t)n) + 1;
-  const int o = (int)(ent % (uint32_t)n) + 1;
   float alpha = 1.f, ialpha = 1.f;
   if (DIR == 0 && A.lscale != nullptr) {
     const float2 s = A.lscale[L - 1];
     alpha = s.x;
     ialpha = s.y;
   }
+  const EdgeVals<float> eL = o == 1 ? edge_vals(A, L, 0) : EdgeVals<float>{0.f, 0.f, 0.f};
+  const EdgeVals<float> eR = o == n ? edge_vals(A, L, 1) : EdgeVals<float>{0.f, 0.f, 0.f};
+  return general_path<DIR, COH>(A, L, o, alpha, ialpha, eL, eR);
+}
+
+// One listed cell through the full rules into a y-sweep tile in shared
+// memory (kYTileCells per field, row-major 32 wide; row0/col0: the tile's
+// first row and column, 0-based); returns true when the value is finite.
+template <bool COH>
+__device__ __noinline__ bool general_to_tile(const SweepArgs& A, uint32_t ent, float* tile, int row0, int col0) {
+  int L, o;
+  entry_cell(A, ent, L, o);
+  const OutCell<float> r = general_value<1, COH>(A, L, o);
+  const int k = (o - 1 - row0) * 32 + (L - 1 - col0);
+  tile[k] = r.s;
+  tile[kYTileCells + k] = r.v;      // x velocity (tangential in the y-sweep)
+  tile[2 * kYTileCells + k] = r.u;  // y velocity (normal)
+  return isfinite(r.s + r.u + r.v);
+}
+
+// One listed cell through the full rules, written with its max-wave update.
+template <int DIR, bool COH>
+__device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
+  int L, o;
+  entry_cell(A, ent, L, o);
   const size_t q = cidx<DIR>(L, o, A.pitch);
   // every global read this cell needs goes out before the compute
   const float dq = __ldg(A.dep + q);
@@ -196,9 +227,7 @@ __device__ __noinline__ void general_store(const SweepArgs& A, uint32_t ent) {
     hm = ld_state<COH>(A.hmax + q);
     vm = ld_state<COH>(A.velmax + q);
   }
-  const EdgeVals<float> eL = o == 1 ? edge_vals(A, L, 0) : EdgeVals<float>{0.f, 0.f, 0.f};
-  const EdgeVals<float> eR = o == n ? edge_vals(A, L, 1) : EdgeVals<float>{0.f, 0.f, 0.f};
-  const OutCell<float> r = general_path<DIR, COH>(A, L, o, alpha, ialpha, eL, eR);
+  const OutCell<float> r = general_value<DIR, COH>(A, L, o);
   const float xo = DIR == 0 ? r.u : r.v;
   const float yo = DIR == 0 ? r.v : r.u;
   A.srf_o[q] = r.s;
@@ -307,11 +336,11 @@ __device__ __forceinline__ unsigned plain_cells(const SweepArgs& A, int i0, bool
 }
 
 template <int DIR, bool LOCAL, bool COH, bool TAIL = true, bool SHARED_ARGS = false, bool MAXOUT = true,
-          bool FLAT = false>
+          bool FLAT = false, bool YSMEM = false>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
-                                            uint32_t* s_list, unsigned* s_n);
+                                            uint32_t* s_list, unsigned* s_n, float* s_out = nullptr);
 
 // LOCAL: the block finishes its own listed cells after its fast cells (a
 // block-local list in shared memory); otherwise they go to the global
@@ -450,12 +479,16 @@ __device__ __forceinline__ void sweep_tile(const SweepArgs& A, int bx, int by) {
 // finish it after a barrier (the fast stores come first).  SHARED_ARGS: A
 // lives in shared memory (the batched kernels), where every field read is a
 // load; the geometry is then read per cell instead of held in registers for
-// the whole line, which measured 14 % faster there (fewer spills).
-template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS, bool MAXOUT, bool FLAT>
+// the whole line, which measured 14 % faster there (fewer spills).  YSMEM
+// (y-sweep): the outputs go to a shared-memory tile instead of global memory,
+// s_out[f * kYTileCells + r * 32] for field f (surface state, x velocity, y
+// velocity) and cell i0 + r (s_out points at the thread's first cell); the
+// caller stores the tile.
+template <int DIR, bool LOCAL, bool COH, bool TAIL, bool SHARED_ARGS, bool MAXOUT, bool FLAT, bool YSMEM>
 __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, bool active, size_t q0,
                                             float (&d)[6], float (&e)[6], float (&u)[6], float (&v)[6],
                                             float (&hm)[kCellsPerThread], float (&vm)[kCellsPerThread],
-                                            uint32_t* s_list, unsigned* s_n) {
+                                            uint32_t* s_list, unsigned* s_n, float* s_out) {
   const int n = A.n;
   const bool swept = active && L >= A.lo && L <= A.hi;
   const Phys<float>& p = A.ph;
@@ -534,6 +567,14 @@ __device__ __forceinline__ void sweep_cells(const SweepArgs& A, int L, int i0, b
     if (MAXOUT && A.hmax) {
       *reinterpret_cast<float4*>(A.hmax + q0) = make_float4(hm[0], hm[1], hm[2], hm[3]);
       *reinterpret_cast<float4*>(A.velmax + q0) = make_float4(vm[0], vm[1], vm[2], vm[3]);
+    }
+  } else if (YSMEM) {
+    // every row of the tile: rows past the grid are clipped by the tile store
+#pragma unroll
+    for (int r = 0; r < kCellsPerThread; ++r) {
+      s_out[r * 32] = os[r];
+      s_out[kYTileCells + r * 32] = xo[r];
+      s_out[2 * kYTileCells + r * 32] = yo[r];
     }
   } else {
 #pragma unroll

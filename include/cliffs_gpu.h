@@ -309,16 +309,21 @@ int cliffs_gpu_prepare_steps(cliffs_ctx *ctx, int32_t nsteps);
  * kernels. */
 int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
 
-/* The sweep kernels, two choices with identical results:
- * - CLIFFS_SWEEP_TILED (the default): one block per tile, loads straight into
- *   registers.
+/* The sweep kernels, three choices with identical results:
+ * - CLIFFS_SWEEP_TILED (the default): one block per tile.  The x-sweep loads
+ *   its window straight into registers; the y-sweep of a two-dimensional step
+ *   has its tile (16 rows x 32 columns and a halo row each side) brought into
+ *   shared memory by tensor-map copies (TMA) and stored back the same way.
+ * - CLIFFS_SWEEP_DIRECT: the tiled kernels with the y-sweep's window loaded
+ *   straight into registers too.
  * - CLIFFS_SWEEP_STAGED: persistent kernels, one resident grid walking the
  *   tiles.  Each block's window loads arrive in shared memory by bulk copies
- *   (TMA), one tile ahead of the compute.  On GB300 it is the slower of the
- *   two, by 3 % (y-sweep) to 30 % (x-sweep).
- * A context whose tensor maps could not be made runs the tiled kernels
- * whichever is chosen. */
-enum { CLIFFS_SWEEP_TILED = 0, CLIFFS_SWEEP_STAGED = 1 };
+ *   (TMA), one tile ahead of the compute.  On GB300 it is the slowest of the
+ *   three.
+ * A context whose tensor maps could not be made runs the direct kernels
+ * whichever is chosen; so does a y-sweep tiling (cliffs_gpu_set_tiling) other
+ * than 4 warps. */
+enum { CLIFFS_SWEEP_TILED = 0, CLIFFS_SWEEP_STAGED = 1, CLIFFS_SWEEP_DIRECT = 2 };
 int cliffs_gpu_set_sweep_kernel(cliffs_ctx *ctx, int32_t kind);
 /* Failure-detection check of the staged kernels' stage waits: one staged
  * x-sweep whose waits expect 16 bytes more than the copies bring, each wait
