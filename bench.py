@@ -23,7 +23,7 @@ a time (each grid's own step graphs).
 
 --workload surrogate runs the learned-surrogate study: 4096 training runs of
 2000 steps on a 512^2 grid from the batched solver, 4 gauge networks (MLP,
-1500 epochs) and a map network (MLP and conv decoder, 600 epochs) trained by
+3000 epochs) and a map network (MLP and conv decoder, 600 epochs) trained by
 the library's kernels, then --steps gated passes over 256 held-out
 scenarios against one-at-a-time solves; the metric is scenarios/s of the
 gated path (surrogate plus solver fallbacks).
@@ -572,7 +572,7 @@ def run_surrogate(args):
 
     rank, world, local = _env_rank()
     S = importlib.import_module("cliffs-src_gb300.surrogate")
-    epochs, map_epochs = 1500, 600
+    epochs, map_epochs = 3000, 600
     config = {"workload": f"learned surrogate of {S.SIDE}x{S.SIDE} shelf runs at {S.DX:g} m, 2000 steps each: 8 "
                           f"source parameters -> {S.NGAUGES} gauge maxima and a {S.MAP}x{S.MAP} max-inundation "
                           f"map; 4096 training runs from the batched solver, 256 held-out scenarios; 4 gauge "

@@ -26,7 +26,7 @@ the target; the solver then judges the surrogate's error on held-out
 scenarios.
 
     python cliffs-src_gb300/surrogate.py [--train 4096] [--test 256] [--steps 2000]
-                                         [--epochs 1500] [--map-epochs 600] [--map-members 1]
+                                         [--epochs 3000] [--map-epochs 600] [--map-members 1]
                                          [--target 0.045]
 
 prints one JSON line: data generation time, training losses, accuracy of the
@@ -387,7 +387,7 @@ def map_errors(Mp, M, floor=0.05):
                 map_iou_mean=float(iou.mean()), map_scenarios_inundated=int(has.sum()))
 
 
-def fit_and_judge(D, epochs=1500, map_epochs=600, target=0.045, seed=0, n_val=256, per_amp=True, width=512,
+def fit_and_judge(D, epochs=3000, map_epochs=600, target=0.045, seed=0, n_val=256, per_amp=True, width=512,
                   depth=3, members=4, map_members=1, single=None, batch=512, lr=1e-3, repeats=1, infer_batch=4096):
     """Train the ensemble on the training runs, calibrate its gate on the
     validation split, judge it on the held-out runs against the solver.
@@ -487,7 +487,7 @@ def fit_and_judge(D, epochs=1500, map_epochs=600, target=0.045, seed=0, n_val=25
     return res
 
 
-def run(n_train=4096, n_test=256, steps=2000, epochs=1500, target=0.045, seed=0, n_val=256, per_amp=True,
+def run(n_train=4096, n_test=256, steps=2000, epochs=3000, target=0.045, seed=0, n_val=256, per_amp=True,
         map_epochs=600, infer_batch=4096, map_members=1):
     """Data from the batched solver, the ensemble trained on n_train - n_val
     runs, its gate calibrated on the n_val others, judged on n_test held-out
@@ -502,7 +502,7 @@ def main():
     ap.add_argument("--train", type=int, default=4096)
     ap.add_argument("--test", type=int, default=256)
     ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--epochs", type=int, default=3000)
     ap.add_argument("--map-epochs", type=int, default=600)
     ap.add_argument("--map-members", type=int, default=1)
     ap.add_argument("--target", type=float, default=0.045)
