@@ -246,7 +246,10 @@ def run_e2e(pkg, case, args, barrier, dist, world):
     final state and max-wave fields back to the host.  The driver's arrays
     (inputs read from its files, outputs it writes) are pinned host memory
     (cliffs_gpu_host_alloc), allocated and filled before the clock starts, as
-    a driver that keeps its module arrays there does."""
+    a driver that keeps its module arrays there does.  The pass runs twice
+    and the second is timed: a process's first call of each kernel loads it
+    (CUDA's lazy module loading), which the device-resident passes leave to
+    their warm-up steps too."""
     import numpy as np
 
     cells = case["dep"].size
@@ -261,25 +264,33 @@ def run_e2e(pkg, case, args, barrier, dist, world):
     for k in ("dep", "H0", "u0", "v0"):
         inputs[k] = pin((ny, nx))
         inputs[k][...] = case[k]
+
+    def one_pass():
+        t0 = time.perf_counter()
+        dx, rs, dy, zeta = pkg.cliffs_gpu.metrics(case["xcrd"], case["ycrd"], case["cartesian"])
+        g2 = pkg.GpuGrid(inputs["dep"], dx=dx, row_scale=rs, dy=dy, zeta=zeta, ground=case["ground"],
+                         crough=case["crough"], dt=case["dt"])  # create: bathymetry H2D
+        g2.set_initial(inputs["H0"], inputs["u0"], inputs["v0"])  # initial state H2D
+        g2.set_graph_steps(10)  # one graph per gauge interval
+        last = -1
+        for k, s0 in enumerate(range(0, args.steps, 10)):
+            g2.step(min(10, args.steps - s0))
+            last = g2.gauges_async(I, J, (rec[k, 0], rec[k, 1], rec[k, 2]))
+        g2.download_state(out=state)
+        g2.maxwave(out=maxes)
+        g2.wait(last)
+        t = time.perf_counter() - t0
+        r, flags = g2.status()
+        g2.close()
+        if r != 0:
+            raise RuntimeError(f"solver status {r} flags {flags} (end-to-end pass)")
+        return t
+
+    # one untimed pass first, as the device-resident passes have their
+    # warm-up: the first call of each output kernel in a process loads it
+    one_pass()
     barrier()
-    t0 = time.perf_counter()
-    dx, rs, dy, zeta = pkg.cliffs_gpu.metrics(case["xcrd"], case["ycrd"], case["cartesian"])
-    g2 = pkg.GpuGrid(inputs["dep"], dx=dx, row_scale=rs, dy=dy, zeta=zeta, ground=case["ground"],
-                     crough=case["crough"], dt=case["dt"])  # create: bathymetry H2D
-    g2.set_initial(inputs["H0"], inputs["u0"], inputs["v0"])  # initial state H2D
-    g2.set_graph_steps(10)  # one graph per gauge interval
-    last = -1
-    for k, s0 in enumerate(range(0, args.steps, 10)):
-        g2.step(min(10, args.steps - s0))
-        last = g2.gauges_async(I, J, (rec[k, 0], rec[k, 1], rec[k, 2]))
-    g2.download_state(out=state)
-    g2.maxwave(out=maxes)
-    g2.wait(last)
-    t_e2e = time.perf_counter() - t0
-    r, flags = g2.status()
-    g2.close()
-    if r != 0:
-        raise RuntimeError(f"solver status {r} flags {flags} (end-to-end pass)")
+    t_e2e = one_pass()
     t_e2e = max_over_ranks(t_e2e, dist)
     h2d = cells * 8 * 4 + (nx + ny) * 8 * 3 + 64 * 8 * nrec  # dep, H0, u0, v0 (FP64), metrics, gauge indices
     d2h = cells * 8 * 3 + cells * 4 * 2 + nrec * 64 * 3 * 8
