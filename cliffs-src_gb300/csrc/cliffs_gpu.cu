@@ -982,17 +982,23 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   else gx.assign((size_t)c->nx, make_float4(0, 0, 0, 0));
   if (c->yrun) build_geo(c->ny, d->dy, gy, c->inv_dx1_y, c->inv_dxn1_y);
   else gy.assign((size_t)c->ny, make_float4(0, 0, 0, 0));
-  auto uniform = [](const std::vector<float4>& g, int n, float4& g0) {
+  // An axis is uniform when every spacing equals the first within 1e-9 of
+  // it: a longitude axis in FP64 degrees has spacings that differ in the
+  // 12th digit, below what the FP32 geometry keeps except in dx(m)-dx(m-1).
+  // A uniform axis takes the geometry of its first spacing everywhere (the
+  // table too, so that every kernel variant reads the same values): the
+  // table of an exactly uniform axis is unchanged by it.
+  auto uniform = [&](int n, const double* sp, std::vector<float4>& g, float4& g0) {
     if (n < 3) return false;
-    g0 = g[1];
-    for (int m = 2; m <= n - 1; ++m) {
-      const float4& a = g[m - 1];
-      if (a.x != g0.x || a.y != g0.y || a.z != g0.z || a.w != g0.w) return false;
-    }
+    const double s0 = sp[0];
+    for (int k = 1; k <= n - 2; ++k)
+      if (std::fabs(sp[k] - s0) > 1e-9 * std::fabs(s0)) return false;
+    g0 = make_float4((float)(1.0 / s0), (float)(1.0 / s0), (float)(d->dt / (s0 + s0)), 0.f);
+    for (int m = 2; m <= n - 1; ++m) g[m - 1] = g0;
     return true;
   };
-  if (c->xrun) c->geo_uni_x = uniform(gx, c->nx, c->geo0_x);
-  if (c->yrun) c->geo_uni_y = uniform(gy, c->ny, c->geo0_y);
+  if (c->xrun) c->geo_uni_x = uniform(c->nx, d->dx, gx, c->geo0_x);
+  if (c->yrun) c->geo_uni_y = uniform(c->ny, d->dy, gy, c->geo0_y);
   std::vector<float> sy((size_t)c->ny, 0.f);
   bool zeta_nonzero = false;
   if (d->zeta)
