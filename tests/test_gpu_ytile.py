@@ -6,8 +6,9 @@ and max-wave fields.
 Cases: a shelf whose wave runs up the coast (listed cells finished into the
 tile), a spherical grid with the metric term whose sizes are multiples of
 neither 32 columns nor 16 rows (tiles clipped at the grid's edges, rows
-outside the grid read 0), a grid 3 cells wide, a grid forced at all four
-edges (edge tables read by the tile), and the 2048 x 2048 benchmark shelf.
+outside the grid read 0), a grid 3 cells wide, a grid 9 rows high (one band,
+most of it outside the grid), a grid forced at all four edges (edge tables
+read by the tile), and the 2048 x 2048 benchmark shelf.
 """
 import importlib
 
@@ -62,7 +63,14 @@ def _narrow():
                 v0=np.zeros_like(dep), ground=0.01, crough=0.0, dt=float(0.8 * dx / np.sqrt(9.8 * 50.0)))
 
 
-@pytest.mark.parametrize("make,steps", [(_shelf, 300), (_sphere, 120), (_narrow, 200)])
+def _short():
+    """9 rows, 70 columns: one band of 16 rows, partly outside the grid."""
+    c = W.shelf_2d(seed=12, nx=70, ny=9, dx=2000.0, steps=0, ngauges=0, axes_km=(40, 6), centre_km=(60.0, 9.0))
+    c["crough"] = 0.000625
+    return c
+
+
+@pytest.mark.parametrize("make,steps", [(_shelf, 300), (_sphere, 120), (_narrow, 200), (_short, 150)])
 def test_tiled_y_equals_direct(make, steps):
     a, b = _pair(make())
     for n in (1, steps - 1):
