@@ -62,7 +62,9 @@ __device__ __forceinline__ int batch_scenario(const int* off, int n, int t) {
 // in shared memory once per entry.  MULTI = false: entries of one tile
 // (span 1), with no loop around the tile's code, which keeps the loop's
 // state out of the tile's register budget.
-template <int DIR, bool COH, bool MAXOUT, bool MULTI = true>
+// FLAT: every scenario's lines of this direction have uniform spacing and no
+// metric term (the single-grid kernels' flat variant: the same bits).
+template <int DIR, bool COH, bool MAXOUT, bool MULTI = true, bool FLAT = false>
 __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int stride) {
   __shared__ SweepArgs sA;
   const int* off = B.off + DIR * (B.n + 1);
@@ -76,7 +78,7 @@ __device__ __forceinline__ void batch_tiles(const BatchArgs& B, int first, int s
     if (threadIdx.x == 0) sA = B.args[2 * k + DIR];
     __syncthreads();
     if (!MULTI) {
-      sweep_tile<DIR, true, COH, true, MAXOUT>(sA, local % g, local / g);
+      sweep_tile<DIR, true, COH, true, MAXOUT, FLAT>(sA, local % g, local / g);
     } else if (DIR == 0) {  // g: column chunks; rows (local / g) * span ...
       const int bx = local % g, by0 = (local / g) * span;
       for (int r = 0; r < span && by0 + r < sA.nlines; ++r) sweep_tile<0, true, COH, true, MAXOUT>(sA, bx, by0 + r);
@@ -153,9 +155,9 @@ __global__ void __launch_bounds__(kBatchThreads, 6) batch_persistent(const Batch
 // 256-scenario ensemble), spills included.  MULTI: entries of more than one
 // tile (B.span[DIR] > 1); the one-tile variant has no loop around the tile
 // (2.34 against 2.70 ms per step with the loop at span 1).
-template <int DIR, bool MAXOUT, bool MULTI>
+template <int DIR, bool MAXOUT, bool MULTI, bool FLAT = false>
 __global__ void __launch_bounds__(kBatchThreads, 8) batch_phase(const BatchArgs B) {
-  batch_tiles<DIR, false, MAXOUT, MULTI>(B, blockIdx.x, gridDim.x);
+  batch_tiles<DIR, false, MAXOUT, MULTI, FLAT>(B, blockIdx.x, gridDim.x);
 }
 
 }  // namespace cliffs

@@ -2514,6 +2514,9 @@ struct cliffs_batch {
   int* d_gx = nullptr;
   unsigned* d_sync = nullptr;  // [0] barrier counter, [1] timeout flag
   int total[2] = {0, 0};
+  // every scenario flat along x / y (uniform spacing, no metric term): the
+  // one-tile phases run their flat variant
+  bool flat[2] = {false, false};
   // per scenario, in single-grid tiles: x (column chunks, rows), y (row
   // groups, column groups); the list of a plan's tile shape is built from them
   std::vector<int> tx, ty, lx, ly;
@@ -2613,8 +2616,11 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
   // set) or the previous end state folded in by the x-sweep (fold set)
   std::vector<SweepArgs> args(2 * (size_t)n), fold(2 * (size_t)n);
   std::vector<int> off(2 * ((size_t)n + 1), 0), gx(2 * (size_t)n, 0);
+  b->flat[0] = b->flat[1] = true;
   for (int k = 0; k < n; ++k) {
     cliffs_ctx* c = ctxs[k];
+    b->flat[0] = b->flat[0] && c->geo_uni_x;  // the x-sweep has no metric term
+    b->flat[1] = b->flat[1] && c->geo_uni_y && c->scl_y == nullptr;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
     args[2 * k] = sweep_args(c, 1, false, c->cur);
     args[2 * k + 1] = sweep_args(c, 2, true, 1 - c->cur);
@@ -2691,19 +2697,26 @@ int cliffs_batch_launch_count(const cliffs_batch* b, int64_t* n) {
 static int batch_launch_phases(cliffs_batch* b, int steps, bool fold) {
   const BatchArgs B = batch_args(b, 1, fold);
   const bool mx = B.span[0] > 1, my = B.span[1] > 1;
+  const bool fx = b->flat[0], fy = b->flat[1];
   for (int s = 0; s < steps; ++s) {
     if (mx)
       batch_phase<0, false, true><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
+    else if (fx)
+      batch_phase<0, false, false, true><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
     else
       batch_phase<0, false, false><<<b->total[0], kBatchThreads, 0, b->stream>>>(B);
     if (fold) {
       if (my)
         batch_phase<1, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      else if (fy)
+        batch_phase<1, false, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
       else
         batch_phase<1, false, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
     } else {
       if (my)
         batch_phase<1, true, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      else if (fy)
+        batch_phase<1, true, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
       else
         batch_phase<1, true, false><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
     }
