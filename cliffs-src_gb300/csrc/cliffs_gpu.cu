@@ -2316,6 +2316,25 @@ int cliffs_gpu_check_stage_timeout(cliffs_ctx* c, int32_t wait_ms) {
   CK(cudaMemcpyAsync(&f, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (!(f & ST_STALL)) return CLIFFS_OK;
+  if (c->yrun && c->ytile_ok) {
+    // the same for one tiled y-sweep (tile_y_kernel): its copy waits run out
+    const SweepArgs Ay = sweep_args(c, 2, false, c->cur);  // writes copy 1 - cur too
+    const int s = c->cur;
+    const YTileMaps M{c->m_dep, c->m_srf[s], c->m_xu[s], c->m_yv[s], c->m_srf16[1 - s], c->m_xu16[1 - s],
+                      c->m_yv16[1 - s]};
+    const dim3 grid((Ay.nlines + 31) / 32, (Ay.n + kYRows - 1) / kYRows);
+    ++c->launches;
+    if (Ay.geo_uniform && Ay.scl == nullptr)
+      tile_y_kernel<true><<<grid, kStagedThreads, 0, c->stream>>>(Ay, M, S);
+    else
+      tile_y_kernel<false><<<grid, kStagedThreads, 0, c->stream>>>(Ay, M, S);
+    CK(cudaGetLastError());
+    f = 0;
+    CK(cudaMemcpyAsync(&f, c->status, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->status, 0, sizeof(unsigned), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
   return (f & ST_STALL) ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
 }
 

@@ -325,11 +325,14 @@ int cliffs_gpu_set_tiling(cliffs_ctx *ctx, int32_t block_x, int32_t warps_y);
  * than 4 warps. */
 enum { CLIFFS_SWEEP_TILED = 0, CLIFFS_SWEEP_STAGED = 1, CLIFFS_SWEEP_DIRECT = 2 };
 int cliffs_gpu_set_sweep_kernel(cliffs_ctx *ctx, int32_t kind);
-/* Failure-detection check of the staged kernels' stage waits: one staged
- * x-sweep whose waits expect 16 bytes more than the copies bring, each wait
- * limited to wait_ms (1..2000).  Expected result: CLIFFS_ERR_TIMEOUT, read by
- * the host, with the device usable afterwards.  The state is unchanged: the
- * sweep writes the other state copy, which is not taken.
+/* Failure-detection check of the kernels' waits for their tensor-map and
+ * bulk copies: one staged x-sweep, then (on a two-dimensional grid) one tiled
+ * y-sweep, whose waits expect 16 bytes more than the copies bring, each wait
+ * limited to wait_ms (1..2000); a y block waits twice before it leaves, so
+ * the check takes about 2 * wait_ms per wave of y blocks.  Expected result:
+ * CLIFFS_ERR_TIMEOUT, read by the host, when both sweeps reported their
+ * waits running out, with the device usable afterwards.  The state is
+ * unchanged: the sweeps write the other state copy, which is not taken.
  * CLIFFS_ERR_STATE without a state, an x-sweep or the staged kernels. */
 int cliffs_gpu_check_stage_timeout(cliffs_ctx *ctx, int32_t wait_ms);
 

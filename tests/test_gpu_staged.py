@@ -85,9 +85,10 @@ def test_staged_equals_tiled_channel():
 
 
 def test_stage_wait_timeout_reported():
-    """The stage waits of one staged x-sweep expect bytes no copy brings: every
-    wait runs out after 50 ms, the host reads CLIFFS_ERR_TIMEOUT, the state is
-    unchanged and the next steps run as usual."""
+    """The copy waits of one staged x-sweep and of one tiled y-sweep expect
+    bytes no copy brings: every wait runs out after 50 ms, the host reads
+    CLIFFS_ERR_TIMEOUT (both sweeps reported it), the state is unchanged and
+    the next steps run as usual."""
     a, b = _pair(_shelf())
     a.step(20)
     b.step(20)
