@@ -1088,6 +1088,23 @@ int cliffs_gpu_set_stream(cliffs_ctx* c, void* stream) {
   return CLIFFS_OK;
 }
 
+// The device's address of a caller's host array when kernels can read and
+// write it in place: pinned memory (cliffs_gpu_host_alloc, cudaHostAlloc,
+// cudaHostRegister).  nullptr for pageable memory, which goes through the
+// staging area and the copy engines.  On GB300 a kernel moves pinned host
+// memory over the host link as fast as the copy engines do (~200 GB/s each
+// way), so converting in place saves the staging pass and overlaps the
+// conversion with the transfer.
+static void* host_mapped(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // The FP64 transfer staging of a context: three nx*ny arrays of doubles.
 static int xfer_area(cliffs_ctx* c, double** out) {
   if (!c->xfer && dalloc(&c->xfer, 3 * (size_t)c->nx * c->ny)) return CLIFFS_ERR_NOMEM;
@@ -1101,11 +1118,21 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
   const size_t n = (size_t)c->nx * c->ny;
   double* x = nullptr;
   RET(xfer_area(c, &x));
-  double *dsrc = x, *dx = xv ? x + n : nullptr, *dy = yv ? x + 2 * n : nullptr;
+  const double *dsrc = x, *dx = xv ? x + n : nullptr, *dy = yv ? x + 2 * n : nullptr;
   int r = CLIFFS_OK;
-  if (cudaMemcpyAsync(dsrc, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && xv && cudaMemcpyAsync(dx, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && yv && cudaMemcpyAsync(dy, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+  const double *ms = (const double*)host_mapped(src), *mx = (const double*)host_mapped(xv),
+               *my = (const double*)host_mapped(yv);
+  if (ms && (!xv || mx) && (!yv || my)) {  // pinned: k_init_state reads the caller's arrays in place
+    dsrc = ms;
+    dx = mx;
+    dy = my;
+  } else {
+    if (cudaMemcpyAsync(x, src, n * sizeof(double), cudaMemcpyHostToDevice, c->stream)) r = CLIFFS_ERR_CUDA;
+    if (!r && xv && cudaMemcpyAsync(x + n, xv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
+      r = CLIFFS_ERR_CUDA;
+    if (!r && yv && cudaMemcpyAsync(x + 2 * n, yv, n * sizeof(double), cudaMemcpyHostToDevice, c->stream))
+      r = CLIFFS_ERR_CUDA;
+  }
   if (!r && !reset_max && c->have_state) r = max_sync(c);  // the replaced state's pending end state
   if (!r) {
     c->max_pending = false;
@@ -1144,18 +1171,23 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   const size_t n = (size_t)c->nx * c->ny;
+  double *mc = (double*)host_mapped(cel), *mx = (double*)host_mapped(xv), *my = (double*)host_mapped(yv);
+  const bool direct = (!cel || mc) && (!xv || mx) && (!yv || my);  // pinned: converted in place
   double* x = nullptr;
-  RET(xfer_area(c, &x));
-  double *a = x, *b = x + n, *e = x + 2 * n;
+  if (!direct) RET(xfer_area(c, &x));
+  double *a = direct ? mc : (cel ? x : nullptr), *b = direct ? mx : (xv ? x + n : nullptr),
+         *e = direct ? my : (yv ? x + 2 * n : nullptr);
   int r = CLIFFS_OK;
   ++c->launches;
   k_download<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->dep64,
                                                         c->srf[c->cur], c->xu[c->cur], c->yv[c->cur], a, b, e,
                                                         kGrav);
   if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
-  if (!r && cel && cudaMemcpyAsync(cel, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && xv && cudaMemcpyAsync(xv, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && yv && cudaMemcpyAsync(yv, e, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!direct) {
+    if (!r && cel && cudaMemcpyAsync(cel, a, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+    if (!r && xv && cudaMemcpyAsync(xv, b, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+    if (!r && yv && cudaMemcpyAsync(yv, e, n * 8, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   return r;
 }
@@ -1892,16 +1924,20 @@ int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
   if (!c || !me || !mv) return CLIFFS_ERR_ARG;
   RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
+  float *ma = (float*)host_mapped(me), *mb = (float*)host_mapped(mv);
+  const bool direct = ma && mb;  // pinned: written in place
   double* x = nullptr;
-  RET(xfer_area(c, &x));
-  float *a = (float*)x, *b = (float*)(x + n);
+  if (!direct) RET(xfer_area(c, &x));
+  float *a = direct ? ma : (float*)x, *b = direct ? mb : (float*)(x + n);
   int r = CLIFFS_OK;
   ++c->launches;
   k_maxwave_out<<<grid2(c->nx, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep, c->hmax, c->velmax,
                                                            (float)c->ground, a, b);
   if (cudaGetLastError() != cudaSuccess) r = CLIFFS_ERR_CUDA;
-  if (!r && cudaMemcpyAsync(me, a, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
-  if (!r && cudaMemcpyAsync(mv, b, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  if (!direct) {
+    if (!r && cudaMemcpyAsync(me, a, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+    if (!r && cudaMemcpyAsync(mv, b, n * 4, cudaMemcpyDeviceToHost, c->stream)) r = CLIFFS_ERR_CUDA;
+  }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess && !r) r = CLIFFS_ERR_CUDA;
   return r;
 }

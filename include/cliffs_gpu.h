@@ -111,7 +111,12 @@ int cliffs_gpu_set_initial(cliffs_ctx *ctx, const double *H,
                            const double *xvel, const double *yvel);
 
 /* State in the reference's own form: celerity cel (= sqrt(g*H)), xvel, yvel
- * (module MASTER).  Upload does not touch hmax/velmax. */
+ * (module MASTER).  Upload does not touch hmax/velmax.
+ * Transfers (set_initial, upload_state, download_state, get_maxwave): when
+ * every array of the call is pinned host memory (cliffs_gpu_host_alloc,
+ * cudaHostAlloc, cudaHostRegister), the conversion kernel reads or writes it
+ * in place; pageable arrays go through a device staging area and the copy
+ * engines.  The results are the same; every transfer synchronises. */
 int cliffs_gpu_upload_state(cliffs_ctx *ctx, const double *cel,
                             const double *xvel, const double *yvel);
 int cliffs_gpu_download_state(cliffs_ctx *ctx, double *cel, double *xvel,
@@ -255,7 +260,8 @@ int cliffs_gpu_feed_child_async(cliffs_ctx *ctx, int32_t id, double cuke,
                                 int64_t *ticket);
 int cliffs_gpu_output_wait(cliffs_ctx *ctx, int64_t ticket);
 int cliffs_gpu_output_done(cliffs_ctx *ctx, int64_t ticket, int32_t *done);
-/* Pinned host memory for the asynchronous outputs. */
+/* Pinned host memory for the asynchronous outputs, and for transfers that
+ * convert in place. */
 int cliffs_gpu_host_alloc(int64_t bytes, void **p);
 void cliffs_gpu_host_free(void *p);
 
