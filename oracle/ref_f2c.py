@@ -527,6 +527,18 @@ def translate(src_path):
     return HEADER + "\n".join(body) + "\n}\n"
 
 
+# Where this recipe looks for the reference checkout when CLIFFS_REFERENCE is
+# not set: the checkout beside the build container's repository.
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_dir(need="cliffs.f"):
+    """The reference checkout ($CLIFFS_REFERENCE, else DEFAULT_REFERENCE) when
+    it holds `need`; None elsewhere (the GPU hosts have no checkout)."""
+    path = os.environ.get("CLIFFS_REFERENCE") or DEFAULT_REFERENCE
+    return path if os.path.exists(os.path.join(path, need)) else None
+
+
 def build(reference, force=False):
     src = os.path.join(reference, "cliffs.f")
     os.makedirs(REFDIR, exist_ok=True)
@@ -545,4 +557,4 @@ def build(reference, force=False):
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CLIFFS_REFERENCE", ""), force=True))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else reference_dir(), force=True))

@@ -1,4 +1,3 @@
-import json
 import os
 import sys
 
@@ -9,24 +8,11 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
-def _reference_path():
-    """The reference checkout: $CLIFFS_REFERENCE, else the `reference_path`
-    recorded beside the benchmark description at the repository root, else
-    none (the GPU hosts have no checkout)."""
-    env = os.environ.get("CLIFFS_REFERENCE")
-    if env:
-        return env
-    p = os.path.join(ROOT, "BASELINE.json")
-    if os.path.exists(p):
-        try:
-            with open(p) as f:
-                return json.load(f).get("reference_path")
-        except (OSError, ValueError):
-            return None
-    return None
+from oracle.ref_f2c import reference_dir as _reference_dir  # noqa: E402
 
-
-REFERENCE = _reference_path()
+# the reference checkout ($CLIFFS_REFERENCE or the recipe's default), present
+# only in the build container
+REFERENCE = _reference_dir("Examples")
 
 
 def pytest_configure(config):

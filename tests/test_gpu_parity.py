@@ -1,6 +1,6 @@
 """GPU parity against the FP64 oracle, through the C ABI.
 
-Tolerances (the spec bar, FP32 state): eta and max-wave elevation within
+Tolerances (the stated parity bar, FP32 state): eta and max-wave elevation within
 1e-4 of the source amplitude on cells wet in both runs; velocities within
 2e-4 m/s + 2e-4 relative; wet/dry mismatches counted and bounded; gauges
 within 1e-4 of the amplitude.  The GPU keeps the state as FP32 surface
