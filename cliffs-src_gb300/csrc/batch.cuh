@@ -24,6 +24,8 @@
 
 namespace cliffs {
 
+struct YTileMaps;
+
 struct BatchArgs {
   const SweepArgs* args;  // [2k] x-sweep, [2k+1] y-sweep of scenario k
   const int* off;         // [dir * (n+1) + k]: first tile of scenario k; [n] the total
@@ -38,6 +40,7 @@ struct BatchArgs {
   int span[2];            // tile shape: single-grid tiles per list entry, along
                           // the rows (x-sweep: rows of 512 cells; y-sweep:
                           // groups of 16 rows of 32 columns)
+  const YTileMaps* ymaps;  // per scenario, the y-sweep's tensor maps (batch_tile_y)
 };
 
 constexpr int kBatchThreads = 128;

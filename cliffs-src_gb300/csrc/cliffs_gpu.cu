@@ -2572,6 +2572,10 @@ struct cliffs_batch {
   // every scenario flat along x / y (uniform spacing, no metric term): the
   // one-tile phases run their flat variant
   bool flat[2] = {false, false};
+  // every scenario's tensor maps made: the one-tile y phase of the fold set
+  // runs batch_tile_y when flat along y
+  YTileMaps* d_ymaps = nullptr;
+  bool ytile = false;
   // per scenario, in single-grid tiles: x (column chunks, rows), y (row
   // groups, column groups); the list of a plan's tile shape is built from them
   std::vector<int> tx, ty, lx, ly;
@@ -2601,6 +2605,7 @@ static BatchArgs batch_args(const cliffs_batch* b, int steps, bool fold) {
   B.extra = 0;
   B.span[0] = std::max(1, b->plan.x_rows);
   B.span[1] = std::max(1, b->plan.y_groups);
+  B.ymaps = b->d_ymaps;
   return B;
 }
 
@@ -2634,6 +2639,7 @@ static void batch_free(cliffs_batch* b) {
   if (b->d_sync) cudaFree(b->d_sync);
   if (b->d_gauge) cudaFree(b->d_gauge);
   if (b->d_grec) cudaFree(b->d_grec);
+  if (b->d_ymaps) cudaFree(b->d_ymaps);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -2695,6 +2701,25 @@ int cliffs_batch_create(cliffs_ctx* const* ctxs, int32_t n, cliffs_batch** out) 
       cudaMemcpy(b->d_args_fold, fold.data(), fold.size() * sizeof(SweepArgs), cudaMemcpyHostToDevice) ||
       batch_lists(b) || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking))
     return fail(CLIFFS_ERR_CUDA);
+  {
+    // the y-sweep of scenario k reads state copy 1 - cur and writes cur
+    std::vector<YTileMaps> ym((size_t)n);
+    bool ok = true;
+    for (int k = 0; k < n && ok; ++k) {
+      const cliffs_ctx* c = ctxs[k];
+      ok = c->ytile_ok;
+      const int s = 1 - c->cur;
+      if (ok)
+        ym[k] = YTileMaps{c->m_dep, c->m_srf[s], c->m_xu[s], c->m_yv[s], c->m_srf16[c->cur], c->m_xu16[c->cur],
+                          c->m_yv16[c->cur]};
+    }
+    if (ok && b->flat[1]) {
+      if (dalloc(&b->d_ymaps, ym.size())) return fail(CLIFFS_ERR_NOMEM);
+      if (cudaMemcpy(b->d_ymaps, ym.data(), ym.size() * sizeof(YTileMaps), cudaMemcpyHostToDevice))
+        return fail(CLIFFS_ERR_CUDA);
+      b->ytile = true;
+    }
+  }
   b->plan.mode = b->max_ctas > 0 ? CLIFFS_BATCH_PERSISTENT : CLIFFS_BATCH_GRAPH;
   b->plan.ctas_per_sm = std::max(1, b->max_ctas);
   b->plan.graph_steps = 32;
@@ -2763,6 +2788,8 @@ static int batch_launch_phases(cliffs_batch* b, int steps, bool fold) {
     if (fold) {
       if (my)
         batch_phase<1, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
+      else if (fy && b->ytile)
+        batch_tile_y<true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
       else if (fy)
         batch_phase<1, false, false, true><<<b->total[1], kBatchThreads, 0, b->stream>>>(B);
       else

@@ -25,6 +25,7 @@
 // bounded (StageCtl::wait_ns); a block whose wait runs out records ST_STALL,
 // waits (bounded) for its copies once more and leaves without storing.
 #pragma once
+#include "batch.cuh"
 #include "staged.cuh"
 
 namespace cliffs {
@@ -118,6 +119,90 @@ __global__ void __launch_bounds__(128, 9)
     tma_store_2d(&M.yv_o, &s_out[2][0][0], c0, r0);
     bulk_commit();
     bulk_wait_read();  // the tile stays until the copies have read it
+  }
+}
+
+// The y phase of a batched step (one launch for every scenario's y tiles,
+// one tile per block): tile_y_kernel's body on the scenario that the list
+// entry names, with the scenario's arguments staged in shared memory and its
+// tensor maps read from B.ymaps (device memory, written before the launch).
+// FLAT: every scenario flat along y.
+template <bool FLAT>
+__global__ void __launch_bounds__(128, 9) batch_tile_y(const BatchArgs B) {
+  __shared__ SweepArgs sA;
+  __shared__ __align__(128) float s_in[4][kYWin][32];
+  __shared__ __align__(128) float s_out[3][kYRows][32];
+  __shared__ uint32_t s_list[kYTileCells];
+  __shared__ unsigned s_n;
+  __shared__ __align__(8) uint64_t bar;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int* off = B.off + (B.n + 1);
+  const int t = blockIdx.x;
+  const int k = batch_scenario(off, B.n, t);
+  const int local = t - __ldg(off + k);
+  const int g = __ldg(B.gx + B.n + k);  // row groups of the scenario
+  const int r0 = (local % g) * kYRows, c0 = (local / g) * 32;
+  const YTileMaps* M = B.ymaps + k;
+  constexpr uint32_t kWinBytes = kYWin * 32 * 4;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    s_n = 0u;
+    fence_mbar_init();
+    mbar_expect_tx(&bar, 4u * kWinBytes);
+    tma_load_2d(&s_in[0][0][0], &M->dep, &bar, c0, r0 - 1);
+    tma_load_2d(&s_in[1][0][0], &M->srf, &bar, c0, r0 - 1);
+    tma_load_2d(&s_in[2][0][0], &M->xu, &bar, c0, r0 - 1);
+    tma_load_2d(&s_in[3][0][0], &M->yv, &bar, c0, r0 - 1);
+    sA = B.args[2 * k + 1];
+  }
+  __syncthreads();
+  const bool ok = mbar_wait_ns(&bar, 0u, B.wait_ns);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) {
+      atomicOr(sA.status, ST_STALL);
+      atomicOr(B.err, 1u);
+      mbar_wait_ns(&bar, 0u, B.wait_ns);  // the copies in flight, before the block's memory goes
+    }
+    return;
+  }
+  const int L = c0 + lane + 1;
+  const int i0 = r0 + warp * kCellsPerThread + 1;
+  const bool active = L <= sA.nlines && i0 <= sA.n;
+  float d[6], e[6], u[6], v[6];
+  float hm[kCellsPerThread], vm[kCellsPerThread];
+#pragma unroll
+  for (int w = 0; w < 6; ++w) {
+    const int r = warp * kCellsPerThread + w;
+    d[w] = s_in[0][r][lane];
+    e[w] = s_in[1][r][lane];
+    v[w] = s_in[2][r][lane];  // tangential in the y-sweep
+    u[w] = s_in[3][r][lane];  // normal
+  }
+  float* mine = &s_out[0][warp * kCellsPerThread][lane];
+#pragma unroll
+  for (int r = 0; r < kCellsPerThread; ++r) {
+    hm[r] = vm[r] = 0.f;
+    if (!active) {
+      mine[r * 32] = 0.f;
+      mine[kYTileCells + r * 32] = 0.f;
+      mine[2 * kYTileCells + r * 32] = 0.f;
+    }
+  }
+  sweep_cells<1, true, false, false, true, false, FLAT, true>(sA, L, i0, active, 0, d, e, u, v, hm, vm, s_list,
+                                                              &s_n, mine);
+  __syncthreads();
+  const unsigned cnt = s_n;
+  bool bad = false;
+  for (unsigned q = tid; q < cnt; q += blockDim.x) bad |= !general_to_tile<false>(sA, s_list[q], &s_out[0][0][0], r0, c0);
+  if (bad) atomicOr(sA.status, ST_NAN);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    tma_store_2d(&M->srf_o, &s_out[0][0][0], c0, r0);
+    tma_store_2d(&M->xu_o, &s_out[1][0][0], c0, r0);
+    tma_store_2d(&M->yv_o, &s_out[2][0][0], c0, r0);
+    bulk_commit();
+    bulk_wait_read();
   }
 }
 
