@@ -3013,6 +3013,27 @@ int cliffs_batch_check_barrier_timeout(cliffs_batch* b, int32_t wait_ms) {
   if (cudaMemcpyAsync(flags, b->d_sync, sizeof(flags), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
       cudaStreamSynchronize(b->stream) != cudaSuccess)
     return CLIFFS_ERR_CUDA;
+  if (!flags[1]) return CLIFFS_OK;
+  if (b->ytile) {
+    // the copy waits of the batched y tiles: each expects 16 bytes more than
+    // its copies bring (B.extra), runs out, and the block leaves
+    BatchArgs By = batch_args(b, 1, true);
+    By.wait_ns = B.wait_ns;
+    By.extra = 1;
+    flags[1] = 0;
+    if (cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess) return CLIFFS_ERR_CUDA;
+    batch_tile_y<true><<<b->total[1], kBatchThreads, 0, b->stream>>>(By);
+    ++b->launches;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(flags, b->d_sync, sizeof(flags), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->d_sync, 0, 2 * sizeof(unsigned), b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess)
+      return CLIFFS_ERR_CUDA;
+    // the scenarios' status words carry ST_STALL from the blocks that gave up
+    for (cliffs_ctx* c : b->ctx)
+      if (cudaMemsetAsync(c->status, 0, sizeof(unsigned), b->stream) != cudaSuccess) return CLIFFS_ERR_CUDA;
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CLIFFS_ERR_CUDA;
+  }
   return flags[1] ? CLIFFS_ERR_TIMEOUT : CLIFFS_OK;
 }
 

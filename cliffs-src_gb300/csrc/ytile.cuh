@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(128, 9) batch_tile_y(const BatchArgs B) {
     mbar_init(&bar, 1);
     s_n = 0u;
     fence_mbar_init();
-    mbar_expect_tx(&bar, 4u * kWinBytes);
+    // B.extra (the timeout self-test): 16 bytes more than the copies bring
+    mbar_expect_tx(&bar, 4u * kWinBytes + (B.extra ? 16u : 0u));
     tma_load_2d(&s_in[0][0][0], &M->dep, &bar, c0, r0 - 1);
     tma_load_2d(&s_in[1][0][0], &M->srf, &bar, c0, r0 - 1);
     tma_load_2d(&s_in[2][0][0], &M->xu, &bar, c0, r0 - 1);

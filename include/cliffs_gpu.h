@@ -433,9 +433,13 @@ int cliffs_batch_step(cliffs_batch *b, int32_t nsteps);
 int cliffs_batch_autotune(cliffs_batch *b, int32_t probe_steps, double *ms_per_step);
 /* Failure-detection check of the grid barrier: one persistent launch whose
  * first barrier waits for an arrival that no block makes, with the wait
- * limited to wait_ms (1..2000).  Expected result: CLIFFS_ERR_TIMEOUT, read by
- * the host, with the device usable afterwards.  The launch applies the
- * x-sweep of one step to the contexts before the barrier. */
+ * limited to wait_ms (1..2000).  Then, when the batch's y phase runs on
+ * tiles by tensor-map copies, one such phase whose copy waits expect 16
+ * bytes more than the copies bring (each block waits twice, about
+ * 2 * wait_ms per wave of blocks).  Expected result: CLIFFS_ERR_TIMEOUT
+ * (both reported), read by the host, with the device usable afterwards.
+ * The persistent launch applies the x-sweep of one step to the contexts
+ * before the barrier: their state is undefined until uploaded again. */
 int cliffs_batch_check_barrier_timeout(cliffs_batch *b, int32_t wait_ms);
 /* Gauges of every scenario, sampled in one launch (output_gages.f:18-29 for
  * all contexts of the batch).  set_gauges takes counts[n] (gauges per
