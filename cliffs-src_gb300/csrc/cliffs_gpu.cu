@@ -1095,14 +1095,16 @@ int cliffs_gpu_set_stream(cliffs_ctx* c, void* stream) {
 // memory over the host link as fast as the copy engines do (~200 GB/s each
 // way), so converting in place saves the staging pass and overlaps the
 // conversion with the transfer.
-static void* host_mapped(const void* p) {
+static void* host_mapped(const void* p, int dev) {
   if (!p) return nullptr;
   cudaPointerAttributes a{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     (void)cudaGetLastError();
     return nullptr;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  // pinned for this context's device (an allocation made with another device
+  // current, and not portable, takes the staging path)
+  return a.type == cudaMemoryTypeHost && a.device == dev ? a.devicePointer : nullptr;
 }
 
 // The FP64 transfer staging of a context: three nx*ny arrays of doubles.
@@ -1120,8 +1122,8 @@ static int upload_common(cliffs_ctx* c, const double* src, int is_cel, const dou
   RET(xfer_area(c, &x));
   const double *dsrc = x, *dx = xv ? x + n : nullptr, *dy = yv ? x + 2 * n : nullptr;
   int r = CLIFFS_OK;
-  const double *ms = (const double*)host_mapped(src), *mx = (const double*)host_mapped(xv),
-               *my = (const double*)host_mapped(yv);
+  const double *ms = (const double*)host_mapped(src, c->dev), *mx = (const double*)host_mapped(xv, c->dev),
+               *my = (const double*)host_mapped(yv, c->dev);
   if (ms && (!xv || mx) && (!yv || my)) {  // pinned: k_init_state reads the caller's arrays in place
     dsrc = ms;
     dx = mx;
@@ -1171,7 +1173,8 @@ int cliffs_gpu_download_state(cliffs_ctx* c, double* cel, double* xv, double* yv
   if (!c) return CLIFFS_ERR_ARG;
   if (!c->have_state) return CLIFFS_ERR_STATE;
   const size_t n = (size_t)c->nx * c->ny;
-  double *mc = (double*)host_mapped(cel), *mx = (double*)host_mapped(xv), *my = (double*)host_mapped(yv);
+  double *mc = (double*)host_mapped(cel, c->dev), *mx = (double*)host_mapped(xv, c->dev),
+         *my = (double*)host_mapped(yv, c->dev);
   const bool direct = (!cel || mc) && (!xv || mx) && (!yv || my);  // pinned: converted in place
   double* x = nullptr;
   if (!direct) RET(xfer_area(c, &x));
@@ -1924,7 +1927,7 @@ int cliffs_gpu_get_maxwave(cliffs_ctx* c, float* me, float* mv) {
   if (!c || !me || !mv) return CLIFFS_ERR_ARG;
   RET(max_sync(c));
   const size_t n = (size_t)c->nx * c->ny;
-  float *ma = (float*)host_mapped(me), *mb = (float*)host_mapped(mv);
+  float *ma = (float*)host_mapped(me, c->dev), *mb = (float*)host_mapped(mv, c->dev);
   const bool direct = ma && mb;  // pinned: written in place
   double* x = nullptr;
   if (!direct) RET(xfer_area(c, &x));
