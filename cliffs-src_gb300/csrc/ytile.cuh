@@ -24,6 +24,10 @@
 // x-sweep wrote last are still in L2).  The wait for the window copies is
 // bounded (StageCtl::wait_ns); a block whose wait runs out records ST_STALL,
 // waits (bounded) for its copies once more and leaves without storing.
+//
+// batch_tile_y runs the same body for the y phase of a batched step (one
+// tile per list entry of batch.cuh), with each scenario's tensor maps in
+// device memory.
 #pragma once
 #include "batch.cuh"
 #include "staged.cuh"
