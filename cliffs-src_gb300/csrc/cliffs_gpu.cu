@@ -905,6 +905,10 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   if (d->nx > 2 && !d->dx) return CLIFFS_ERR_ARG;
   if (d->ny > 2 && !d->dy) return CLIFFS_ERR_ARG;
   if (!(d->dt > 0) || !(d->ground > 0) || d->crough < 0) return CLIFFS_ERR_ARG;
+  // launch limits: the x-sweep's grid has a block row per grid row, the
+  // y-sweep's one per band of 16 rows (65535 block rows at most)
+  if (d->nx > 2 && d->ny > 65535) return CLIFFS_ERR_ARG;
+  if (d->ny > 2 && (d->ny + 15) / 16 > 65535) return CLIFFS_ERR_ARG;
   int dev = 0;
   int r = check_device(&dev);
   if (r) return r;

@@ -96,7 +96,9 @@ int cliffs_gpu_metrics(int32_t nx, int32_t ny, int32_t cartesian,
 
 /* Allocate device state for one grid (replaces the allocate() calls of
  * cliffs_main.f:191-197 and 288).  hmax/velmax start at zero and edges at
- * still water, as in the reference. */
+ * still water, as in the reference.  CLIFFS_ERR_ARG for a grid past the
+ * launch limits: ny <= 65535 when the grid has an x-sweep (nx > 2), and
+ * ny <= 1,048,560 otherwise. */
 int cliffs_gpu_create(const cliffs_grid_desc *desc, cliffs_ctx **out);
 void cliffs_gpu_destroy(cliffs_ctx *ctx);
 

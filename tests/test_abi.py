@@ -78,3 +78,14 @@ def test_bad_descriptions_rejected_before_device(lib):
     with pytest.raises(pkg.CliffsError) as e:
         pkg.GpuGrid(np.ones((4, 5)), dx=np.ones(4), dy=np.ones(3), ground=0.01, crough=0, dt=0.0)
     assert e.value.code == -1
+
+
+def test_grids_past_the_launch_limits_rejected_before_device(lib):
+    # a grid with an x-sweep and more than 65535 rows (one block row per grid row)
+    with pytest.raises(pkg.CliffsError) as e:
+        pkg.GpuGrid(np.ones((65536, 3)), dx=np.ones(2), dy=np.ones(65535), ground=0.01, crough=0, dt=0.1)
+    assert e.value.code == -1
+    # a channel along y with more than 65535 bands of 16 rows
+    with pytest.raises(pkg.CliffsError) as e:
+        pkg.GpuGrid(np.ones((16 * 65535 + 1, 1)), dy=np.ones(16 * 65535), ground=0.01, crough=0, dt=0.1)
+    assert e.value.code == -1
