@@ -963,14 +963,15 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   };
   if (dalloc(&c->arena, layout(nullptr))) return fail(CLIFFS_ERR_NOMEM);
   layout(c->arena);
-  // bathymetry: the FP64 depth as passed, and its rounding in padded rows
+  // bathymetry: the FP64 depth as passed, and its rounding in padded rows;
+  // the host builds the geometry meanwhile, and one synchronisation at the
+  // end covers both
   if (cudaMemcpyAsync(c->dep64, d->dep, (size_t)c->nx * c->ny * sizeof(double), cudaMemcpyHostToDevice,
                       c->stream) != cudaSuccess)
     return fail(CLIFFS_ERR_CUDA);
   ++c->launches;
   k_dep_from64<<<grid2(c->pitch, c->ny), 128, 0, c->stream>>>(c->nx, c->ny, c->pitch, c->dep64, c->dep);
-  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
-    return fail(CLIFFS_ERR_CUDA);
+  if (cudaGetLastError() != cudaSuccess) return fail(CLIFFS_ERR_CUDA);
   // geometry tables
   auto build_geo = [&](int n, const double* s, std::vector<float4>& geo, float& i1, float& in1) {
     geo.assign((size_t)n, make_float4(0, 0, 0, 0));
@@ -1013,24 +1014,52 @@ int cliffs_gpu_create(const cliffs_grid_desc* d, cliffs_ctx** out) {
   std::vector<float2> ls((size_t)c->ny, make_float2(1.f, 1.f));
   if (d->row_scale)
     for (int j = 0; j < c->ny; ++j) ls[j] = make_float2((float)d->row_scale[j], (float)(1.0 / d->row_scale[j]));
-  if (cudaMemcpy(c->geo_x, gx.data(), gx.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(c->geo_y, gy.data(), gy.size() * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(c->scl_y, sy.data(), sy.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(c->lscale, ls.data(), ls.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(c->status, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
-      cudaMemset(c->cnt, 0, 2 * sizeof(uint32_t)) != cudaSuccess)
-    return fail(CLIFFS_ERR_CUDA);
+  {
+    // the four tables lie one after another in the arena: one copy of their
+    // span, laid out on the host as there
+    char* const lo = reinterpret_cast<char*>(c->geo_x);
+    char* const hi = reinterpret_cast<char*>(c->lscale + c->ny);
+    std::vector<char> span((size_t)(hi - lo), 0);
+    auto put = [&](const void* dev, const void* src, size_t bytes) {
+      std::memcpy(span.data() + (reinterpret_cast<const char*>(dev) - lo), src, bytes);
+    };
+    put(c->geo_x, gx.data(), gx.size() * sizeof(float4));
+    put(c->geo_y, gy.data(), gy.size() * sizeof(float4));
+    put(c->scl_y, sy.data(), sy.size() * sizeof(float));
+    put(c->lscale, ls.data(), ls.size() * sizeof(float2));
+    if (cudaMemcpyAsync(lo, span.data(), span.size(), cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+        cudaMemsetAsync(c->status, 0, 2 * sizeof(unsigned), c->stream) != cudaSuccess ||
+        cudaMemsetAsync(c->cnt, 0, 2 * sizeof(uint32_t), c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess)
+      return fail(CLIFFS_ERR_CUDA);
+  }
   if (!d->row_scale) c->lscale = nullptr;  // (its arena slot stays unused)
   if (!zeta_nonzero) c->scl_y = nullptr;
   // the staged sweep kernels: tensor maps of the y-sweep's fields and the
   // resident grid of each kernel; without them the context keeps fast_kernel
   {
+    // the device's SM count and the staged kernels' resident blocks, asked
+    // once per device and process
+    static std::mutex occ_mu;
+    static int occ[64][3] = {};
     int nsm = 0, bx = 0, by = 0;
-    bool ok = get_encoder() == CLIFFS_OK &&
-              cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, staged_x, kStagedThreads, 0) == cudaSuccess &&
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, staged_y, kStagedThreads, 0) == cudaSuccess &&
-              bx > 0 && by > 0;
+    {
+      std::lock_guard<std::mutex> lk(occ_mu);
+      const bool cached = dev < 64 && occ[dev][0] > 0;
+      if (cached) {
+        nsm = occ[dev][0];
+        bx = occ[dev][1];
+        by = occ[dev][2];
+      } else if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bx, staged_x, kStagedThreads, 0) == cudaSuccess &&
+                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&by, staged_y, kStagedThreads, 0) == cudaSuccess &&
+                 dev < 64 && nsm > 0) {
+        occ[dev][0] = nsm;
+        occ[dev][1] = bx;
+        occ[dev][2] = by;
+      }
+    }
+    bool ok = get_encoder() == CLIFFS_OK && nsm > 0 && bx > 0 && by > 0;
     const int nx = c->nx, ny = c->ny, pp = c->pitch;
     ok = ok && !make_map(&c->m_dep, c->dep, nx, ny, pp, 32, kYWin) && !make_map(&c->m_hmax, c->hmax, nx, ny, pp, 32, kYRows) &&
          !make_map(&c->m_velmax, c->velmax, nx, ny, pp, 32, kYRows);
