@@ -1790,14 +1790,39 @@ static int plain_graph_len(const cliffs_ctx* c, int remaining) {
   return len >= 2 ? len : 0;
 }
 
+// The instantiated graph of `len` steps for the current state copy and
+// tiling, or nullptr.
+static cliffs_ctx::PlainGraph* plain_graph_find(cliffs_ctx* c, int len) {
+  for (int s = 0; s < cliffs_ctx::kPlainGraphs; ++s)
+    if (plain_graph_valid(c, c->pgraph[s], len)) {
+      c->pgraph[s].used = ++c->pgraph_clock;
+      return &c->pgraph[s];
+    }
+  return nullptr;
+}
+
+static int one_step(cliffs_ctx* c, double* t);
+
 static int graph_steps(cliffs_ctx* c, int nsteps, double* t, int32_t* steps_done, int* done_out) {
   *done_out = 0;
   if (!plain_graphs_apply(c) || nsteps < 2) return CLIFFS_OK;
   const int per = (c->xrun ? 1 : 0) + (c->yrun ? 1 : 0);
   int done = 0;
   for (int len; (len = plain_graph_len(c, nsteps - done)) > 0;) {
-    cliffs_ctx::PlainGraph* pg = nullptr;
-    RET(plain_graph(c, len, &pg));
+    cliffs_ctx::PlainGraph* pg = plain_graph_find(c, len);
+    if (!pg) {
+      // no graph of this length yet: these steps run launch by launch, and
+      // the graph is captured and instantiated while the device works on
+      // them, for the calls that follow (cliffs_gpu_prepare_steps builds it
+      // ahead instead)
+      for (int s = 0; s < len; ++s) {
+        RET(one_step(c, t));
+        if (steps_done) *steps_done += 1;
+      }
+      RET(plain_graph(c, len, &pg));
+      done += len;
+      continue;
+    }
     CK(cudaGraphLaunch(pg->exec, c->stream));
     c->launches += (int64_t)per * len;
     c->sweeps += (unsigned)(per * len);
