@@ -298,8 +298,10 @@ int cliffs_gpu_launch_count(cliffs_ctx *ctx, int64_t *n);
  * no graph).  Steps without profiling or a rising source are replayed from
  * a graph, one launch per k steps; the last steps of a call, when fewer than
  * k but at least 2, from a graph of their own length (a few such lengths are
- * kept per context).  A fresh state's first step (after set_initial, an
- * upload, a source, a single sweep) runs on its own.  With boundary forcing
+ * kept per context).  Plain steps that find no graph of their length yet
+ * run launch by launch while the graph is captured for the calls that
+ * follow.  A fresh state's first step (after set_initial, an upload, a
+ * source, a single sweep) runs on its own.  With boundary forcing
  * (two-dimensional grids) the graph first fills the k steps' edge tables in
  * one kernel, from the records and weights the library's cursor gives each
  * step; a chunk in which the forcing ends runs step by step. */
